@@ -1,0 +1,185 @@
+/*
+ * xfluids_gb300.h - C ABI of the GB300-native convective right-hand side of XFluids.
+ *
+ * The reference host code (class XFLUIDS, src/XFLUIDS.cpp) drives one fluid through the methods of
+ * class Fluid (src/global_class.h:14-55, implemented in src/Fluids.cpp). Every entry point below
+ * replaces one of those methods, or the block function underneath it, for the path
+ *
+ *     BoundaryCondition -> UpdateFluidStates -> ComputeFluidLU -> UpdateFluidURK3   (per RK stage)
+ *     GetFluidDt                                                                    (per step)
+ *
+ * The signatures use plain C types only: parameter blocks mirror the reference's POD structs
+ * (Block/MeshSize/Thermal, src/include/global_setup.h:162-208) and the compile-time macros that
+ * select the scheme (SCHEME_ORDER, Artificial_type, COP, NUM_SPECIES, GhostSpecies, Thermo,
+ * NCOP_Gamma) become run-time fields of xfg_scheme.
+ *
+ * Conventions
+ *  - Cell index id = Xmax*Ymax*k + Xmax*j + i (x fastest), as in the reference.
+ *  - Arrays crossing the ABI use the reference's layouts: conserved state AoS U[Emax*id + n],
+ *    primitives SoA of length Xmax*Ymax*Zmax, mass fractions AoS y[NUM_SPECIES*id + s].
+ *    Pointers may be host or device memory (the copies use unified addressing).
+ *  - Inside the handle the state is stored SoA (U[n*pitch + id]) in device memory.
+ *  - Every function returns an int status: 0 ok, >0 a numerical error code in the reference's
+ *    encoding (10000 negative density, 1100/1200 NaN/Inf state, 21/22 NaN/Inf right-hand side,
+ *    src/Fluids.cpp:1024-1029), <0 a CUDA or argument error (message in xfg_last_error()).
+ *    No function calls exit().
+ */
+#ifndef XFLUIDS_GB300_H
+#define XFLUIDS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XFG_MAX_SPECIES 9   /* largest NUM_SPECIES built into the kernels */
+#define XFG_MAX_EQ (XFG_MAX_SPECIES + 4)
+
+/* Boundary condition ids, src/include/global_setup.h:96-105 (enum BConditions). */
+enum xfg_bc { XFG_INFLOW = 0, XFG_OUTFLOW = 1, XFG_SYMMETRY = 2, XFG_PERIODIC = 3,
+              XFG_NSLIPWALL = 4, XFG_VISCWALL = 5, XFG_SLIPWALL = 6, XFG_INNERBLOCK = 7 };
+
+/* Mesh block, the fields of Block/MeshSize the path reads (global_setup.h:162-200, filled by
+ * Setup::init, src/read_ini/src/iniset.cpp:290-369). Absent dimensions have inner=1, Bwidth=0. */
+typedef struct xfg_block {
+    int Xmax, Ymax, Zmax;
+    int X_inner, Y_inner, Z_inner;
+    int Bwidth_X, Bwidth_Y, Bwidth_Z;
+    int DimX, DimY, DimZ;
+    double dx, dy, dz;
+    double _dx, _dy, _dz;
+    double CFLnumber;
+    int Boundarys[6];          /* XMIN, XMAX, YMIN, YMAX, ZMIN, ZMAX (Setup::Boundarys) */
+} xfg_block;
+
+/* Thermo tables as Setup::ReadThermal leaves them (src/read_ini/src/thermal.cpp:36-178):
+ * Hia[n*21 + coeff*3 + range], Hib[n*6 + k*3 + range], Wi in kg/mol, Ri = Ru/Wi, _Wi = 1/Wi. */
+typedef struct xfg_thermal {
+    int num_species;
+    double Wi[XFG_MAX_SPECIES];
+    double _Wi[XFG_MAX_SPECIES];
+    double Ri[XFG_MAX_SPECIES];
+    double Hia[XFG_MAX_SPECIES * 21];
+    double Hib[XFG_MAX_SPECIES * 6];
+} xfg_thermal;
+
+/* Scheme selection: the reference's compile-time switches (cmake/init_options.cmake:23-90,
+ * cmake/init_sample.cmake:216-282) as run-time values. */
+enum xfg_artificial { XFG_ROE = 1, XFG_LLF = 2, XFG_GLF = 3 };  /* Artificial_type */
+enum xfg_precision { XFG_FP64 = 0, XFG_MIXED = 1 };
+
+typedef struct xfg_scheme {
+    int cop;               /* COP: multi-component (Emax = NUM_SPECIES + 4) or single gas (Emax = 5) */
+    int num_species;       /* NUM_SPECIES (1 without COP) */
+    int scheme_order;      /* SCHEME_ORDER: 5 (WENO5-JS) or 7 (WENO7) */
+    int artificial_type;   /* Artificial_type: 1 Roe, 2 local LF, 3 global LF */
+    int thermo;            /* Thermo: 1 NASA-9, 0 JANAF / NASA-7 */
+    int ghost_species;     /* GhostSpecies: renormalise Y and write it back into U */
+    double ncop_gamma;     /* NCOP_Gamma, ratio of specific heats without COP */
+    int precision;         /* xfg_precision: FP64 path or FP32 reconstruction with FP64 state */
+} xfg_scheme;
+
+/* Arrays a caller can read back (xfg_get_array). */
+enum xfg_array {
+    XFG_U = 0, XFG_U1 = 1, XFG_LU = 2,                /* AoS, Emax per cell */
+    XFG_RHO = 3, XFG_P = 4, XFG_U_VEL = 5, XFG_V_VEL = 6, XFG_W_VEL = 7,
+    XFG_C = 8, XFG_H = 9, XFG_T = 10, XFG_GAMMA = 11, XFG_E = 12, XFG_CP = 13, XFG_R = 14,
+    XFG_Y = 15,                                       /* AoS, NUM_SPECIES per cell */
+    XFG_FWX = 16, XFG_FWY = 17, XFG_FWZ = 18          /* face fluxes Fwall, AoS Emax per cell */
+};
+
+typedef struct xfg_handle xfg_handle;
+
+/* Text of the last error raised on this host thread. */
+const char *xfg_last_error(void);
+
+/* Library build information: kernel instantiations, architecture. */
+const char *xfg_build_info(void);
+
+/* Create the device state of one fluid block: replaces Fluid::Fluid + Fluid::AllocateFluidMemory
+ * (src/Fluids.cpp:90-100, :270-583) and Setup::CpyToGPU (src/read_ini/src/gpucopy.cpp:5-36).
+ * device: CUDA ordinal. All device memory of the handle is allocated here. */
+int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_thermal *thermal,
+               int device, xfg_handle **out);
+
+/* Free the handle: replaces Fluid::~Fluid (src/Fluids.cpp:103-252). */
+int xfg_destroy(xfg_handle *h);
+
+/* Load the conserved state U (AoS, Emax*Xmax*Ymax*Zmax doubles) and, for COP, the temperature
+ * that warm-starts the Newton iteration (Xmax*Ymax*Zmax doubles, may be NULL: keeps the stored T).
+ * Replaces the U/T writes of Fluid::InitialU and XFLUIDS::Read_Ubak (src/XFLUIDS.cpp:689-724).
+ * Also copies U into U1, as InitialUFKernel does (sample ini_sample.hpp). */
+int xfg_set_state(xfg_handle *h, const double *U_aos, const double *T);
+
+/* Copy one array out (host or device pointer): replaces the q.memcpy reads of Fluid's public
+ * buffers in XFLUIDS::Output / CopyDataFromDevice (src/XFLUIDS.cpp:644-656, :726-828). */
+int xfg_get_array(xfg_handle *h, int which, double *out);
+
+/* Ghost-cell fill of U (flag 0) or U1 (flag != 0): replaces Fluid::BoundaryCondition
+ * (src/Fluids.cpp:922-933) -> FluidBoundaryCondition (src/solver_BCs/BCs_block.cpp:4-218). */
+int xfg_boundary(xfg_handle *h, int flag);
+
+/* Primitive recovery and physical fluxes on all cells of U (flag 0) or U1: replaces
+ * Fluid::UpdateFluidStates (src/Fluids.cpp:935-944) -> UpdateFluidStateFlux
+ * (src/solver_UpdateStates/UpdateStates_block.cpp:7-191). *error receives the reference's
+ * "error captured" flag; timers4 (may be NULL) gets the 4 timers the reference returns. */
+int xfg_update_states(xfg_handle *h, int flag, int *error, float *timers4);
+
+/* Convective right-hand side LU of U (flag 0) or U1: replaces Fluid::ComputeFluidLU
+ * (src/Fluids.cpp:951-961) -> GetLU (src/solver_Reconstruction/FDM_Method/ConVenction_block.hpp:10-617).
+ * timers23 (may be NULL) gets the 23 timers the reference returns (unused ones are 0). */
+int xfg_compute_lu(xfg_handle *h, int flag, float *timers23);
+
+/* SSP-RK3 stage combination: replaces Fluid::UpdateFluidURK3 (src/Fluids.cpp:946-949) ->
+ * UpdateURK3rd (src/solver_UpdateStates/UpdateStates_block.cpp:193-211). */
+int xfg_update_rk3(xfg_handle *h, int flag, double dt);
+
+/* CFL time step from the primitives of the last xfg_update_states: replaces Fluid::GetFluidDt
+ * (src/Fluids.cpp:897-920) -> GetDt (src/solver_GetDt/GlobalDt_block.hpp:6-114). */
+int xfg_get_dt(xfg_handle *h, double *dt);
+
+/* NaN / Inf / negative-density check of the stage state and LU: replaces Fluid::EstimateFluidNAN
+ * (src/Fluids.cpp:963-1040). *error = 1 when captured; error_pos (may be NULL) receives
+ * Emax+4 ints in the reference's layout (per-component codes, then i, j, k). */
+int xfg_estimate_nan(xfg_handle *h, int flag, int *error, int *error_pos);
+
+/* One full time step as XFLUIDS::Evolution runs it (src/XFLUIDS.cpp:196-214 and
+ * SinglePhaseSolverRK3rd :377-411): dt from the primitives left by the previous stage-3
+ * UpdateStates, clipped to target_t, then three RK stages, fused into few kernels. On return *t
+ * is the new time and *dt the step taken. Call xfg_update_states once before the first step, as
+ * main.cpp:45-47 does. */
+int xfg_step(xfg_handle *h, double target_t, double *t, double *dt);
+
+/* Advance up to nsteps steps toward target_t with the step sequence of xfg_step, dt kept on the
+ * device and the launches replayed from a captured CUDA graph. Stops early once target_t is
+ * reached. *t and *steps_done report the result; the call synchronises once at the end. */
+int xfg_advance(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done);
+
+/* One fused step like xfg_step with CUDA events between the launches: ms_out[7] receives the
+ * device time of each phase summed over the three stages: [0] dt, [1] boundary, [2] primitive
+ * recovery, [3..5] face fluxes x/y/z, [6] divergence + RK update. Advances the state. */
+int xfg_time_phases(xfg_handle *h, double target_t, float *ms_out);
+
+/* Current simulated time of the handle (set by xfg_step / xfg_advance, reset by xfg_set_time). */
+int xfg_set_time(xfg_handle *h, double t);
+int xfg_get_time(xfg_handle *h, double *t);
+
+/* Wait for all work of the handle's stream. */
+int xfg_synchronize(xfg_handle *h);
+
+/* Device pointer of a handle array (SoA inside the handle) and its pitch in elements, for callers
+ * that keep their own device-side post-processing. */
+int xfg_device_array(xfg_handle *h, int which, double **ptr, size_t *pitch);
+
+/* Measure this GPU's FP64 and FP32 FMA throughput (FLOP/s, FMA = 2) with a register-resident
+ * FMA chain; used as the roofline denominator of the compute-bound kernels. out[0] = FP64,
+ * out[1] = FP32, out[2] = SM clock (MHz) reported by the driver during the run (0 if unknown). */
+int xfg_measure_pipe_peaks(int device, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XFLUIDS_GB300_H */

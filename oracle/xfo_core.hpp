@@ -1,0 +1,893 @@
+// xfo_core.hpp - CPU restatement of the XFluids convective right-hand side (test infrastructure).
+//
+// This is the ORACLE: a plain, serial/OpenMP restatement of the reference algorithm that the CUDA
+// path is checked against. It is only used by tests/, __graft_entry__.smoke() and the CPU arms of
+// bench.py. The product library never links or calls it.
+//
+// Every function restates one reference function with the same operation order (parenthesised
+// exactly as C++ parses the reference expressions), so that built with -ffp-contract=off it
+// reproduces the reference CPU build bit for bit. The reference's compile-time switches become
+// fields of Scheme. Two deliberate differences, both bit-neutral for finite values:
+//   * eigenvector entries that are structural zeros are skipped in the projections
+//     (x + U*0.0 == x) and structural +-1 entries become additions/subtractions (x + U*1.0 == x+U);
+//   * per-call invariants the reference recomputes in each helper (MARCO_PREEIGEN) are computed once.
+// The scalar type R is a template parameter so that the same code runs on double (oracle) and on
+// a counting scalar (algorithmic flop count, xfo_count.hpp).
+#pragma once
+
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../include/xfluids_gb300.h"
+
+namespace xfo {
+
+constexpr int kMaxS = XFG_MAX_SPECIES;
+constexpr int kMaxE = XFG_MAX_EQ;
+
+// Physical constants, src/include/global_setup.h:48-54 (Ru in J/mol/K).
+constexpr double kAvogadro = 6.02214076e26;
+constexpr double kBoltzmann = 1.380649e-23;
+constexpr double kUniversalGas = kAvogadro * kBoltzmann;
+constexpr double kRu = kUniversalGas * 1.0E-3;
+constexpr double kOT = 1.0 / 3.0;    // _OT, global_setup.h:35
+constexpr double kSix = 1.0 / 6.0;   // _six, schemes/Utils_schemes.hpp:5
+
+inline double dval(double x) { return x; }
+
+// ---------------------------------------------------------------------------------------------
+// Thermodynamics of species n (src/solver_Ini/Thermo_device.h)
+// ---------------------------------------------------------------------------------------------
+struct ThermoTable {
+    int ns;
+    int nasa;  // Thermo: 1 NASA-9, 0 JANAF
+    const double *Hia, *Hib, *Ri, *Wi, *_Wi;
+};
+
+// HeatCapacity_NASA, Thermo_device.h:10-23
+template <class R>
+R cp_nasa(const ThermoTable &t, R T0, double Ri, int n) {
+    using std::fmax;
+    R T = fmax(T0, R(200.0));
+    R _T = R(1.0) / T;
+    // range 1 for [1000, 6000), 0 below, 2 from 6000 K; none (Cp = 0) when T is NaN
+    int rg = (T >= R(1000.0) && T < R(6000.0)) ? 1 : (T < R(1000.0) ? 0 : (T >= R(6000.0) ? 2 : -1));
+    if (rg < 0) return R(0.0);
+    const double *a = t.Hia + n * 21 + rg;
+    return Ri * ((a[0] * _T + a[3]) * _T + a[6] + (a[9] + (a[12] + (a[15] + a[18] * T) * T) * T) * T);
+}
+// HeatCapacity_JANAF, Thermo_device.h:29-40
+template <class R>
+R cp_janaf(const ThermoTable &t, R T0, double Ri, int n) {
+    using std::fmax;
+    R T = fmax(T0, R(200.0));
+    int rg = (T > R(1000.0)) ? 0 : 1;
+    const double *a = t.Hia + n * 21 + rg;
+    return Ri * (a[0] + (a[3] + (a[6] + (a[9] + a[12] * T) * T) * T) * T);
+}
+template <class R>
+R heat_capacity(const ThermoTable &t, R T0, double Ri, int n) {
+    return t.nasa ? cp_nasa(t, T0, Ri, n) : cp_janaf(t, T0, Ri, n);
+}
+// get_Enthalpy_NASA, Thermo_device.h:62-80
+template <class R>
+R h_nasa(const ThermoTable &t, R T0, double Ri, int n) {
+    using std::fmax;
+    using std::log;
+    R TT = T0, T = fmax(T0, R(200.0));
+    int rg = (T >= R(1000.0) && T < R(6000.0)) ? 1 : (T < R(1000.0) ? 0 : (T >= R(6000.0) ? 2 : -1));
+    R hi = R(0.0);
+    if (rg >= 0) {
+        const double *a = t.Hia + n * 21 + rg;
+        const double b0 = t.Hib[n * 6 + rg];
+        hi = Ri * (-a[0] / T + a[3] * log(T) +
+                   (a[6] + (0.5 * a[9] + (a[12] * kOT + (0.25 * a[15] + 0.2 * a[18] * T) * T) * T) * T) * T + b0);
+    }
+    if (TT < R(200.0)) {
+        R Cpi = cp_nasa(t, R(200.0), Ri, n);
+        hi += Cpi * (TT - R(200.0));
+    }
+    return hi;
+}
+// get_Enthalpy_JANAF, Thermo_device.h:86-102
+template <class R>
+R h_janaf(const ThermoTable &t, R T0, double Ri, int n) {
+    using std::fmax;
+    R TT = T0, T = fmax(T0, R(200.0));
+    int rg = (T > R(1000.0)) ? 0 : 1;
+    const double *a = t.Hia + n * 21 + rg;
+    R hi = Ri * (T * (a[0] + T * (a[3] * 0.5 + T * (a[6] * kOT + T * (a[9] * 0.25 + a[12] * T * 0.2)))) + a[15]);
+    if (TT < R(200.0)) {
+        R Cpi = cp_janaf(t, R(200.0), Ri, n);
+        hi += Cpi * (TT - R(200.0));
+    }
+    return hi;
+}
+template <class R>
+R enthalpy(const ThermoTable &t, R T0, double Ri, int n) {
+    return t.nasa ? h_nasa(t, T0, Ri, n) : h_janaf(t, T0, Ri, n);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Mixture functions (src/solver_Ini/Mixing_device.h)
+// ---------------------------------------------------------------------------------------------
+template <class R>  // get_CopR :49-56
+R mix_R(const ThermoTable &t, const R *yi) {
+    R s = R(0.0);
+    for (int n = 0; n < t.ns; n++) s += yi[n] * t._Wi[n];
+    return s * kRu;
+}
+template <class R>  // get_CopCp :61-68
+R mix_Cp(const ThermoTable &t, const R *yi, R T) {
+    R s = R(0.0);
+    for (int n = 0; n < t.ns; n++) s += yi[n] * heat_capacity(t, T, t.Ri[n], n);
+    return s;
+}
+template <class R>  // get_CopGamma(thermal, yi, Cp, T) :114-126 (guarded form used by GetStates)
+R mix_gamma_guarded(const ThermoTable &t, const R *yi, R Cp) {
+    R w = R(0.0);
+    for (int n = 0; n < t.ns; n++) w += yi[n] * t._Wi[n];
+    R CopW = R(1.0) / w;  // get_CopW :91-97
+    R g = Cp / (Cp - kRu / CopW);
+    if (g > R(1.0)) return g;
+    return R(-1.0);
+}
+template <class R>  // get_CopGamma(thermal, yi, T) :102-109 = Cp / get_CopCv (:73-86)
+R mix_gamma_cpcv(const ThermoTable &t, const R *yi, R T, R Cp) {
+    // Cp = get_CopCp(yi, T); get_CopCv recomputes the same sum and subtracts Ru * sum(yi/Wi).
+    R w = R(0.0);
+    for (int n = 0; n < t.ns; n++) w += yi[n] * t._Wi[n];
+    R Cv = Cp - kRu * w;
+    return Cp / Cv;
+}
+template <class R>  // get_Coph :131-140
+R mix_h(const ThermoTable &t, const R *yi, R T) {
+    R h = R(0.0);
+    for (int n = 0; n < t.ns; n++) h += enthalpy(t, T, t.Ri[n], n) * yi[n];
+    return h;
+}
+// get_T :171-193 with sub_FuncT :159-166. Newton on h(T) - R T - e = 0, warm-started from T0.
+template <class R>
+R newton_T(const ThermoTable &t, const R *yi, R e, R T0) {
+    using std::fabs;
+    using std::fmax;
+    using std::fmin;
+    R T = T0;
+    for (int it = 1; it < 101; it++) {
+        R h = mix_h(t, yi, T);
+        R Rm = mix_R(t, yi);
+        R Cp = mix_Cp(t, yi, T);
+        R f = h - Rm * T - e;
+        R df_ = Cp - Rm;
+        R df = fmin(f / (df_ + R(1.0e-30)), R(1e-3) * T);
+        df = fmax(df, -R(1e-2) * T);
+        T = T - df;
+        if (fabs(df) <= R(1.0e-6)) break;
+    }
+    return T;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Configuration
+// ---------------------------------------------------------------------------------------------
+struct Config {
+    xfg_block bl;
+    xfg_scheme sc;
+    xfg_thermal th;
+    int E() const { return sc.cop ? sc.num_species + 4 : 5; }
+    int NS() const { return sc.num_species; }
+    int NCOP() const { return sc.cop ? sc.num_species - 1 : 0; }
+    size_t ncell() const { return (size_t)bl.Xmax * bl.Ymax * bl.Zmax; }
+    ThermoTable table() const { return ThermoTable{th.num_species, sc.thermo, th.Hia, th.Hib, th.Ri, th.Wi, th._Wi}; }
+};
+
+// Arrays of one fluid, in the reference's layouts (AoS U, SoA primitives, AoS y).
+template <class R>
+struct Fields {
+    std::vector<R> U, U1, LU;
+    std::vector<R> rho, p, u, v, w, c, gamma, e, H, T, Cp, Rm, y;
+    std::vector<R> FluxF, FluxG, FluxH, Fw[3];
+    std::vector<R> eig[3];        // eigen_local_{x,y,z}, AoS Emax
+    R eigen_block[3][kMaxE];      // GLF maxima
+    R uvw_c_max[3];
+    void alloc(const Config &cf) {
+        size_t n = cf.ncell(), E = cf.E();
+        for (std::vector<R> *a : {&U, &U1, &LU, &FluxF, &FluxG, &FluxH, &Fw[0], &Fw[1], &Fw[2], &eig[0], &eig[1], &eig[2]})
+            a->assign(n * E, R(0.0));
+        for (std::vector<R> *a : {&rho, &p, &u, &v, &w, &this->c, &gamma, &e, &H, &T, &Cp, &Rm}) a->assign(n, R(0.0));
+        y.assign(n * cf.NS(), R(0.0));
+        for (int d = 0; d < 3; d++)
+            for (int k = 0; k < kMaxE; k++) eigen_block[d][k] = R(0.0);
+        for (int d = 0; d < 3; d++) uvw_c_max[d] = R(0.0);
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Boundary conditions, src/solver_BCs/BCs_kernels.hpp:9-258 driven as BCs_block.cpp:4-218:
+// X faces over all (j,k), then Y faces over all (i,k), then Z faces over all (i,j).
+// ---------------------------------------------------------------------------------------------
+template <class R>
+void bc_cell(const Config &cf, R *U, int d, int BC, int i, int j, int k, int mirror_offset, int index_inner, int sign) {
+    const xfg_block &b = cf.bl;
+    const int E = cf.E(), NCOP = cf.NCOP();
+    const int Xmax = b.Xmax, Ymax = b.Ymax;
+    const int inner = d == 0 ? b.X_inner : (d == 1 ? b.Y_inner : b.Z_inner);
+    const int bw = d == 0 ? b.Bwidth_X : (d == 1 ? b.Bwidth_Y : b.Bwidth_Z);
+    int c = d == 0 ? i : (d == 1 ? j : k);  // coordinate along the face normal
+    auto at = [&](int cc) -> size_t {
+        int ii = d == 0 ? cc : i, jj = d == 1 ? cc : j, kk = d == 2 ? cc : k;
+        return (size_t)Xmax * Ymax * kk + (size_t)Xmax * jj + ii;
+    };
+    size_t id = at(c);
+    int src;
+    int vel = 1 + d;
+    switch (BC) {
+    case XFG_SYMMETRY: {
+        src = 2 * (bw + mirror_offset) - 1 - c;
+        size_t t = at(src);
+        for (int n = 0; n < E; n++) U[E * id + n] = U[E * t + n];
+        U[E * id + vel] = -U[E * t + vel];
+    } break;
+    case XFG_PERIODIC: {
+        size_t t = at(c + sign * inner);
+        for (int n = 0; n < E; n++) U[E * id + n] = U[E * t + n];
+    } break;
+    case XFG_OUTFLOW: {
+        size_t t = at(index_inner);
+        for (int n = 0; n < E; n++) U[E * id + n] = U[E * t + n];
+    } break;
+    case XFG_NSLIPWALL:
+    case XFG_VISCWALL:
+    case XFG_SLIPWALL: {
+        src = 2 * (bw + mirror_offset) - 1 - c;
+        size_t t = at(src);
+        U[E * id + 0] = U[E * t + 0];
+        U[E * id + 1] = -U[E * t + 1];
+        U[E * id + 2] = -U[E * t + 2];
+        U[E * id + 3] = -U[E * t + 3];
+        U[E * id + 4] = U[E * t + 4];
+        for (int n = E - NCOP; n < E; n++) U[E * id + n] = U[E * t + n];
+    } break;
+    default:  // Inflow, innerBlock: untouched
+        break;
+    }
+}
+
+template <class R>
+void boundary(const Config &cf, R *U) {
+    const xfg_block &b = cf.bl;
+    if (b.DimX)
+        for (int k = 0; k < b.Zmax; k++)
+            for (int j = 0; j < b.Ymax; j++)
+                for (int g = 0; g < b.Bwidth_X; g++) {
+                    bc_cell(cf, U, 0, b.Boundarys[0], g, j, k, 0, b.Bwidth_X, 1);
+                    bc_cell(cf, U, 0, b.Boundarys[1], g + b.Xmax - b.Bwidth_X, j, k, b.X_inner, b.Xmax - b.Bwidth_X - 1, -1);
+                }
+    if (b.DimY)
+        for (int k = 0; k < b.Zmax; k++)
+            for (int g = 0; g < b.Bwidth_Y; g++)
+                for (int i = 0; i < b.Xmax; i++) {
+                    bc_cell(cf, U, 1, b.Boundarys[2], i, g, k, 0, b.Bwidth_Y, 1);
+                    bc_cell(cf, U, 1, b.Boundarys[3], i, g + b.Ymax - b.Bwidth_Y, k, b.Y_inner, b.Ymax - b.Bwidth_Y - 1, -1);
+                }
+    if (b.DimZ)
+        for (int g = 0; g < b.Bwidth_Z; g++)
+            for (int j = 0; j < b.Ymax; j++)
+                for (int i = 0; i < b.Xmax; i++) {
+                    bc_cell(cf, U, 2, b.Boundarys[4], i, j, g, 0, b.Bwidth_Z, 1);
+                    bc_cell(cf, U, 2, b.Boundarys[5], i, j, g + b.Zmax - b.Bwidth_Z, b.Z_inner, b.Zmax - b.Bwidth_Z - 1, -1);
+                }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Primitive recovery (src/solver_UpdateStates/Update_device.hpp)
+// ---------------------------------------------------------------------------------------------
+// Getrhoyi :7-29
+template <class R>
+void get_rho_yi(const Config &cf, R *U, R &rho, R *yi) {
+    rho = U[0];
+    R rho1 = R(1.0) / rho;
+    if (!cf.sc.cop) return;
+    const int NCOP = cf.NCOP(), E = cf.E();
+    if (cf.sc.ghost_species) {
+        yi[NCOP] = R(0.0);
+        R sum = R(0.0);
+        for (int s = 0; s < NCOP; s++) yi[s] = U[s + 5] * rho1, sum += yi[s];
+        sum = R(1.0) / sum;
+        for (int s = 0; s < NCOP; s++) yi[s] *= sum, U[s + 5] = rho * yi[s];
+    } else {
+        yi[NCOP] = R(1.0);
+        for (int s = 5; s < E; s++) yi[s - 5] = U[s] * rho1, yi[NCOP] += -yi[s - 5];
+    }
+}
+
+// GetStates :33-54 and GetPhysFlux :81-110
+template <class R>
+void get_states(const Config &cf, const ThermoTable &tt, const R *U, R rho, R &u, R &v, R &w, R &p, R &H, R &c,
+                R &gamma, R &T, R &e, R &Cp, R &Rm, const R *yi) {
+    using std::sqrt;
+    R rho1 = R(1.0) / rho;
+    u = U[1] * rho1, v = U[2] * rho1, w = U[3] * rho1;
+    R tme = U[4] * rho1 - R(0.5) * (u * u + v * v + w * w);
+    if (cf.sc.cop) {
+        R R_ = mix_R(tt, yi);
+        T = newton_T(tt, yi, tme, T);
+        p = rho * R_ * T, Rm = R_;
+        Cp = mix_Cp(tt, yi, T);
+        gamma = mix_gamma_guarded(tt, yi, Cp);
+    } else {
+        gamma = R(cf.sc.ncop_gamma);
+        p = (cf.sc.ncop_gamma - 1.0) * rho * tme;
+    }
+    H = (U[4] + p) * rho1;
+    c = sqrt(gamma * p * rho1);
+    e = tme;
+}
+
+template <class R>
+void phys_flux(const Config &cf, const R *U, const R *yi, R *F, R *G, R *Hf, R u, R v, R w, R p) {
+    F[0] = U[1]; F[1] = U[1] * u + p; F[2] = U[1] * v; F[3] = U[1] * w; F[4] = (U[4] + p) * u;
+    G[0] = U[2]; G[1] = U[2] * u; G[2] = U[2] * v + p; G[3] = U[2] * w; G[4] = (U[4] + p) * v;
+    Hf[0] = U[3]; Hf[1] = U[3] * u; Hf[2] = U[3] * v; Hf[3] = U[3] * w + p; Hf[4] = (U[4] + p) * w;
+    if (cf.sc.cop)
+        for (int n = 5; n < cf.E(); n++) F[n] = U[1] * yi[n - 5], G[n] = U[2] * yi[n - 5], Hf[n] = U[3] * yi[n - 5];
+}
+
+// UpdateFluidStateFlux (UpdateStates_block.cpp:7-191): Updaterhoyi on all cells, then
+// UpdateFuidStatesKernel on all cells. Returns 0.
+template <class R>
+void update_states(const Config &cf, Fields<R> &f, std::vector<R> &UI) {
+    const ThermoTable tt = cf.table();
+    const long n = (long)cf.ncell();
+    const int E = cf.E(), NS = cf.NS();
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < n; id++) get_rho_yi(cf, &UI[E * id], f.rho[id], &f.y[NS * id]);
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < n; id++) {
+        const R *U = &UI[E * id];
+        get_states(cf, tt, U, f.rho[id], f.u[id], f.v[id], f.w[id], f.p[id], f.H[id], f.c[id], f.gamma[id], f.T[id],
+                   f.e[id], f.Cp[id], f.Rm[id], &f.y[NS * id]);
+        phys_flux(cf, U, &f.y[NS * id], &f.FluxF[E * id], &f.FluxG[E * id], &f.FluxH[E * id], f.u[id], f.v[id], f.w[id],
+                  f.p[id]);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Eigensystem (src/solver_Reconstruction/FDM_Method/positive-definite_eigen)
+// ---------------------------------------------------------------------------------------------
+// An eigenvector row/column entry: structural zero, +1, -1 or a general value.
+enum Kind : uint8_t { KZ = 0, KP1 = 1, KM1 = 2, KG = 3 };
+template <class R>
+struct Vec {
+    R v[kMaxE];
+    uint8_t k[kMaxE];
+    void zero(int E) { for (int n = 0; n < E; n++) v[n] = R(0.0), k[n] = KZ; }
+    void set(int n, R x) { v[n] = x, k[n] = KG; }
+    void one(int n) { v[n] = R(1.0), k[n] = KP1; }
+    void mone(int n) { v[n] = R(-1.0), k[n] = KM1; }
+};
+// sum_n a[n] * vec[n], accumulated in ascending n from 0.0 as the reference loops do.
+template <class R>
+R dot(const Vec<R> &l, const R *a, int E) {
+    R acc = R(0.0);
+    bool first = true;
+    for (int n = 0; n < E; n++) {
+        switch (l.k[n]) {
+        case KZ: break;
+        case KP1: acc = first ? a[n] : acc + a[n]; first = false; break;
+        case KM1: acc = first ? -a[n] : acc - a[n]; first = false; break;
+        default: acc = first ? a[n] * l.v[n] : acc + a[n] * l.v[n]; first = false; break;
+        }
+    }
+    return acc;
+}
+
+// Roe-averaged face state and the quantities MARCO_PREEIGEN derives from it.
+template <class R>
+struct Face {
+    R D, D1, _u, _v, _w, _H, _P, _rho;
+    R c2, b1, b3, Gamma0;
+    R z[kMaxS], _yi[kMaxS];
+    R q2, _c, b2, _c1;
+};
+
+// ReconstructSoundSpeed + SoundSpeedMultiSpecies, Utils_device.hpp:42-79, :102-140.
+template <class R>
+R cop_sound_speed(const Config &cf, const ThermoTable &tt, const Fields<R> &f, size_t id_l, size_t id_r, Face<R> &F) {
+    const int NS = cf.NS(), NCOP = cf.NCOP();
+    const R *yl = &f.y[NS * id_l], *yr = &f.y[NS * id_r];
+    const R D = F.D, D1 = F.D1;
+    auto roe = [&](R a, R b) { return (a + D * b) * D1; };  // get_RoeAverage, Recon_device.hpp:14-17
+    R hl[kMaxS], hr[kMaxS], dpdrhoi[kMaxS], drhoi[kMaxS];
+    const R Tl = f.T[id_l], Tr = f.T[id_r];
+    for (int n = 0; n < NS; n++) {
+        hl[n] = enthalpy(tt, Tl, tt.Ri[n], n);
+        hr[n] = enthalpy(tt, Tr, tt.Ri[n], n);
+        F._yi[n] = (yl[n] + D * yr[n]) * D1;
+    }
+    R Cpl = mix_Cp(tt, yl, Tl), Cpr = mix_Cp(tt, yr, Tr);
+    R gl = mix_gamma_cpcv(tt, yl, Tl, Cpl), gr = mix_gamma_cpcv(tt, yr, Tr, Cpr);
+    F.Gamma0 = roe(gl, gr);
+    const R ul = f.u[id_l], vl = f.v[id_l], wl = f.w[id_l], ur = f.u[id_r], vr = f.v[id_r], wr = f.w[id_r];
+    R q2l = ul * ul + vl * vl + wl * wl, q2r = ur * ur + vr * vr + wr * wr;
+    R Rl = mix_R(tt, yl), Rr = mix_R(tt, yr);
+    const R rl = f.rho[id_l], rr = f.rho[id_r], pl = f.p[id_l], pr = f.p[id_r];
+    R el = f.H[id_l] - R(0.5) * q2l - pl / rl, er = f.H[id_r] - R(0.5) * q2r - pr / rr;
+    const double RN = tt.Ri[NCOP];
+    auto dpdrho = [&](R hN, R q2, R Cp, R Rm, R T, R g) {  // get_DpDrho :14-19
+        R RNT = RN * T;
+        return (g - R(1.0)) * (R(0.5) * q2 - hN + Cp * RNT / Rm);
+    };
+    auto dpdrhoi_of = [&](R hin, double Rin, R hiN, R T, R Cp, R Rm, R g) {  // get_DpDrhoi :29-35
+        R hN_minus_hi = -hin + hiN;
+        R Ri_minus_RN = R(Rin - RN);
+        return (g - R(1.0)) * (hN_minus_hi + Cp * Ri_minus_RN * T / Rm);
+    };
+    R _dpdrho = roe(dpdrho(hl[NCOP], q2l, Cpl, Rl, Tl, gl), dpdrho(hr[NCOP], q2r, Cpr, Rr, Tr, gr));
+    for (int n = 0; n < NCOP; n++) {
+        dpdrhoi[n] = roe(dpdrhoi_of(hl[n], tt.Ri[n], hl[NCOP], Tl, Cpl, Rl, gl), dpdrhoi_of(hr[n], tt.Ri[n], hr[NCOP], Tr, Cpr, Rr, gr));
+        drhoi[n] = rr * yr[n] - rl * yl[n];
+    }
+    R _prho = roe(pl / rl, pr / rr) +
+              R(0.5) * D * D1 * D1 * ((ur - ul) * (ur - ul) + (vr - vl) * (vr - vl) + (wr - wl) * (wr - wl));
+    R _dpdE = roe(gl - R(1.0), gr - R(1.0));
+    R _dpde = roe((gl - R(1.0)) * rl, (gr - R(1.0)) * rr);
+    // SoundSpeedMultiSpecies
+    R dp = pr - pl, drho = rr - rl, de = er - el;
+    R Sum_dpdrhoi = R(0.0), Sum_dpdrhoi2 = R(0.0), Sum_Yidpdrhoi = R(0.0);
+    for (int n = 0; n < NCOP; n++) {
+        Sum_dpdrhoi += dpdrhoi[n] * drhoi[n];
+        Sum_dpdrhoi2 += dpdrhoi[n] * drhoi[n] * dpdrhoi[n] * drhoi[n];
+    }
+    R temp1 = dp - (_dpdrho * drho + _dpde * de + Sum_dpdrhoi);
+    R temp = temp1 / (_dpdrho * _dpdrho * drho * drho + _dpde * de * _dpde * de + Sum_dpdrhoi2 + R(1e-19));
+    for (int n = 0; n < NCOP; n++) Sum_Yidpdrhoi += F._yi[n] * dpdrhoi[n];
+    R _dpdE_new = _dpdE + _dpdE * _dpdE * de * F._rho * temp;
+    R _dpdrho_new = _dpdrho + _dpdrho * _dpdrho * drho * temp;
+    R dpdrhoi_new[kMaxS];
+    for (int n = 0; n < NCOP; n++) dpdrhoi_new[n] = dpdrhoi[n] + dpdrhoi[n] * dpdrhoi[n] * drhoi[n] * temp;
+    R csqr = _dpdrho_new + _dpdE_new * _prho + Sum_Yidpdrhoi;
+    F.b1 = _dpdE_new / csqr;
+    F.b3 = R(0.0);
+    for (int n = 0; n < NCOP; n++) {
+        F.z[n] = -dpdrhoi_new[n] / _dpdE_new;
+        F.b3 += F._yi[n] * F.z[n];
+    }
+    F.b3 *= F.b1;
+    // c2 <= 0 fallback (sycl::step(c2, 0) is 1 when c2 <= 0)
+    R c2w = (R(0.0) < csqr) ? R(0.0) : R(1.0);
+    R c2 = F.Gamma0 * F._P * F._rho * c2w + (R(1.0) - c2w) * csqr;
+    return c2;
+}
+
+// MARCO_ROE (global_marco.h:26-37) + MARCO_NOCOPC2 / MARCO_COPC2 + MARCO_PREEIGEN.
+template <class R>
+void face_state(const Config &cf, const ThermoTable &tt, const Fields<R> &f, size_t id_l, size_t id_r, Face<R> &F) {
+    using std::sqrt;
+    F.D = sqrt(f.rho[id_r] / f.rho[id_l]);
+    F.D1 = R(1.0) / (F.D + R(1.0));
+    F._u = (f.u[id_l] + F.D * f.u[id_r]) * F.D1;
+    F._v = (f.v[id_l] + F.D * f.v[id_r]) * F.D1;
+    F._w = (f.w[id_l] + F.D * f.w[id_r]) * F.D1;
+    F._H = (f.H[id_l] + F.D * f.H[id_r]) * F.D1;
+    F._P = (f.p[id_l] + F.D * f.p[id_r]) * F.D1;
+    F._rho = sqrt(f.rho[id_r] * f.rho[id_l]);
+    if (cf.sc.cop) {
+        F.c2 = cop_sound_speed(cf, tt, f, id_l, id_r, F);
+    } else {
+        F.Gamma0 = R(cf.sc.ncop_gamma);
+        F.c2 = F.Gamma0 * F._P / F._rho;
+        F.b1 = (F.Gamma0 - R(1.0)) / F.c2;
+        F.b3 = R(0.0);
+    }
+    F.q2 = F._u * F._u + F._v * F._v + F._w * F._w;
+    F._c = sqrt(F.c2);
+    F.b2 = R(1.0) + F.b1 * F.q2 - F.b1 * F._H;
+    F._c1 = R(1.0) / F._c;
+}
+
+// RoeAverageLeft_{x,y,z} (Eigen_matrix.hpp:7-84, :157-234, :307-384): row n of L and |lambda_n|.
+// d = 0,1,2 for x,y,z. Velocity components are permuted so that un is normal, ut1/ut2 follow the
+// reference's row layout for that direction.
+template <class R>
+void left_row(const Config &cf, int d, int n, const Face<R> &F, Vec<R> &l, R &ev) {
+    using std::fabs;
+    const int E = cf.E(), NCOP = cf.NCOP();
+    const R b1 = F.b1, b2 = F.b2, b3 = F.b3, _c1 = F._c1, _c = F._c;
+    const R vel[3] = {F._u, F._v, F._w};
+    const R un = vel[d];
+    l.zero(E);
+    const R hb1 = R(0.5) * b1;
+    if (n == 0 || n == E - 1) {
+        const R un_c = un * _c1;
+        const R s = (n == 0) ? R(1.0) : R(-1.0);
+        // n = 0: 0.5*(b2 + un_c + b3), -0.5*(b1*u_m [+ _c1 if m == d]);
+        // n = E-1: 0.5*(b2 - un_c + b3), 0.5*(-b1*u_m [+ _c1 if m == d]).
+        if (n == 0) l.set(0, R(0.5) * (b2 + un_c + b3));
+        else l.set(0, R(0.5) * (b2 - un_c + b3));
+        for (int m = 0; m < 3; m++) {
+            if (n == 0) l.set(1 + m, m == d ? -R(0.5) * (b1 * vel[m] + _c1) : -R(0.5) * (b1 * vel[m]));
+            else l.set(1 + m, m == d ? R(0.5) * (-b1 * vel[m] + _c1) : R(0.5) * (-b1 * vel[m]));
+        }
+        l.set(4, hb1);
+        for (int m = 0; m < NCOP; m++) l.set(m + E - NCOP, -R(0.5) * b1 * F.z[m]);
+        ev = (n == 0) ? fabs(un - _c) : fabs(un + _c);
+        (void)s;
+        return;
+    }
+    ev = fabs(un);
+    // rows 1..3: one of them is the entropy-like row (the one whose index is d+1), the others the
+    // shear rows, in the order the reference lays them out per direction.
+    if (n >= 1 && n <= 3) {
+        const int dn = d + 1;  // row with (1-b2-b3)/b1, u, v, w, -1
+        if (n == dn) {
+            l.set(0, (R(1.0) - b2 - b3) / b1);
+            l.set(1, F._u); l.set(2, F._v); l.set(3, F._w);
+            l.mone(4);
+            for (int m = 0; m < NCOP; m++) l.set(m + E - NCOP, F.z[m]);
+            return;
+        }
+        // shear rows: x: n=2 -> (v, 0, -1, 0, 0), n=3 -> (-w, 0, 0, 1, 0)
+        //             y: n=1 -> (-u, 1, 0, 0, 0), n=3 -> (w, 0, 0, -1, 0)
+        //             z: n=1 -> (u, -1, 0, 0, 0), n=2 -> (-v, 0, 1, 0, 0)
+        if (d == 0) {
+            if (n == 2) { l.set(0, F._v); l.mone(2); }
+            else { l.set(0, -F._w); l.one(3); }
+        } else if (d == 1) {
+            if (n == 1) { l.set(0, -F._u); l.one(1); }
+            else { l.set(0, F._w); l.mone(3); }
+        } else {
+            if (n == 1) { l.set(0, F._u); l.mone(1); }
+            else { l.set(0, -F._v); l.one(2); }
+        }
+        return;
+    }
+    // species rows n = 4 .. E-2
+    const int s = n + cf.NS() - E;
+    l.set(0, -F._yi[s]);
+    l.one(5 + s);
+}
+
+// RoeAverageRight_{x,y,z} (Eigen_matrix.hpp:86-155, :236-305, :386-455): column n of R.
+template <class R>
+void right_col(const Config &cf, int d, int n, const Face<R> &F, Vec<R> &r) {
+    const int E = cf.E(), NCOP = cf.NCOP();
+    const R b1 = F.b1, _c = F._c, _H = F._H;
+    const R vel[3] = {F._u, F._v, F._w};
+    const R un = vel[d];
+    r.zero(E);
+    if (n == 0 || n == E - 1) {
+        r.one(0);
+        for (int m = 0; m < 3; m++) {
+            if (m == d) r.set(1 + m, n == 0 ? vel[m] - _c : vel[m] + _c);
+            else r.set(1 + m, vel[m]);
+        }
+        r.set(4, n == 0 ? _H - un * _c : _H + un * _c);
+        for (int m = 0; m < NCOP; m++) r.set(m + E - NCOP, F._yi[m]);
+        return;
+    }
+    if (n >= 1 && n <= 3) {
+        const int dn = d + 1;
+        if (n == dn) {
+            r.set(0, b1);
+            r.set(1, F._u * b1); r.set(2, F._v * b1); r.set(3, F._w * b1);
+            if (d == 2) { r.set(1, b1 * F._u); r.set(2, b1 * F._v); r.set(3, b1 * F._w); }
+            r.set(4, _H * b1 - R(1.0));
+            for (int m = 0; m < NCOP; m++) r.set(m + E - NCOP, b1 * F._yi[m]);
+            return;
+        }
+        // x: n=2 -> (0,0,-1,0,-v), n=3 -> (0,0,0,1,w)
+        // y: n=1 -> (0,1,0,0,u),   n=3 -> (0,0,0,-1,-w)
+        // z: n=1 -> (0,-1,0,0,-u), n=2 -> (0,0,1,0,v)
+        if (d == 0) {
+            if (n == 2) { r.mone(2); r.set(4, -F._v); }
+            else { r.one(3); r.set(4, F._w); }
+        } else if (d == 1) {
+            if (n == 1) { r.one(1); r.set(4, F._u); }
+            else { r.mone(3); r.set(4, -F._w); }
+        } else {
+            if (n == 1) { r.mone(1); r.set(4, -F._u); }
+            else { r.one(2); r.set(4, F._v); }
+        }
+        return;
+    }
+    const int s = n + cf.NS() - E;
+    r.set(4, F.z[s]);
+    r.one(5 + s);
+}
+
+// ---------------------------------------------------------------------------------------------
+// WENO schemes (src/solver_Reconstruction/schemes)
+// ---------------------------------------------------------------------------------------------
+// weno5old_BODY, WENO5s_schemes.hpp:12-69 (double-precision branch)
+template <class R>
+R weno5_body(R v1, R v2, R v3, R v4, R v5) {
+    R a1, a2, a3;
+    const R dtwo = R(2.0), dtre = R(3.0);
+    a1 = v1 - dtwo * v2 + v3;
+    R s1 = R(13.0) * a1 * a1;
+    a1 = v1 - R(4.0) * v2 + dtre * v3;
+    s1 += dtre * a1 * a1;
+    a1 = v2 - dtwo * v3 + v4;
+    R s2 = R(13.0) * a1 * a1;
+    a1 = v2 - v4;
+    s2 += dtre * a1 * a1;
+    a1 = v3 - dtwo * v4 + v5;
+    R s3 = R(13.0) * a1 * a1;
+    a1 = dtre * v3 - R(4.0) * v4 + v5;
+    s3 += dtre * a1 * a1;
+    const R tol = R(1.0E-6);
+    s1 += tol, s2 += tol, s3 += tol;
+    a1 = R(0.1) * s2 * s2 * s3 * s3;
+    a2 = R(0.6) * s1 * s1 * s3 * s3;
+    a3 = R(0.3) * s1 * s1 * s2 * s2;
+    R tw1 = R(1.0) / (a1 + a2 + a3);
+    a1 = a1 * tw1, a2 = a2 * tw1, a3 = a3 * tw1;
+    s1 = a1 * (dtwo * v1 - R(7.0) * v2 + R(11.0) * v3);
+    s2 = a2 * (-v2 + R(5.0) * v3 + dtwo * v4);
+    s3 = a3 * (dtwo * v3 + R(5.0) * v4 - v5);
+    return (s1 + s2 + s3);
+}
+// weno5old_GPU :71-95; f and m point at index 3 of the 8-point stencil arrays.
+template <class R>
+R weno5(const R *f, const R *m) {
+    R temf = weno5_body(f[-2], f[-1], f[0], f[1], f[2]);
+    R temm = weno5_body(m[3], m[2], m[1], m[0], m[-1]);
+    return (temf + temm) * R(kSix);
+}
+// weno7_P / weno7_M body, WENO7s_schemes.hpp:8-67 (v1..v7 in upwind order)
+template <class R>
+R weno7_body(R v1, R v2, R v3, R v4, R v5, R v6, R v7) {
+    const R ep = R(1.0e-7);
+    const R C0 = R(1.0 / 35.0), C1 = R(12.0 / 35.0), C2 = R(18.0 / 35.0), C3 = R(4.0 / 35.0);
+    R S10 = R(-2.0 / 6.0) * v1 + R(9.0 / 6.0) * v2 - R(18.0 / 6.0) * v3 + R(11.0 / 6.0) * v4;
+    R S11 = R(1.0 / 6.0) * v2 - R(6.0 / 6.0) * v3 + R(3.0 / 6.0) * v4 + R(2.0 / 6.0) * v5;
+    R S12 = R(-2.0 / 6.0) * v3 - R(3.0 / 6.0) * v4 + R(6.0 / 6.0) * v5 - R(1.0 / 6.0) * v6;
+    R S13 = R(-11.0 / 6.0) * v4 + R(18.0 / 6.0) * v5 - R(9.0 / 6.0) * v6 + R(2.0 / 6.0) * v7;
+    R S20 = -v1 + R(4.0) * v2 - R(5.0) * v3 + R(2.0) * v4;
+    R S21 = v3 - R(2.0) * v4 + v5;
+    R S22 = v4 - R(2.0) * v5 + v6;
+    R S23 = R(2.0) * v4 - R(5.0) * v5 + R(4.0) * v6 - R(1.0) * v7;
+    R S30 = -v1 + R(3.0) * v2 - R(3.0) * v3 + v4;
+    R S31 = -v2 + R(3.0) * v3 - R(3.0) * v4 + v5;
+    R S32 = -v3 + R(3.0) * v4 - R(3.0) * v5 + v6;
+    R S33 = -v4 + R(3.0) * v5 - R(3.0) * v6 + v7;
+    const R k13 = R(13.0 / 12.0), k1043 = R(1043.0 / 960.0), k112 = R(1.0 / 12.0);
+    R S0 = S10 * S10 + k13 * S20 * S20 + k1043 * S30 * S30 + k112 * S10 * S30;
+    R S1 = S11 * S11 + k13 * S21 * S21 + k1043 * S31 * S31 + k112 * S11 * S31;
+    R S2 = S12 * S12 + k13 * S22 * S22 + k1043 * S32 * S32 + k112 * S12 * S32;
+    R S3 = S13 * S13 + k13 * S23 * S23 + k1043 * S33 * S33 + k112 * S13 * S33;
+    R a0 = C0 / ((ep + S0) * (ep + S0));
+    R a1 = C1 / ((ep + S1) * (ep + S1));
+    R a2 = C2 / ((ep + S2) * (ep + S2));
+    R a3 = C3 / ((ep + S3) * (ep + S3));
+    R sum = a0 + a1 + a2 + a3;
+    R W0 = a0 / sum, W1 = a1 / sum, W2 = a2 / sum, W3 = a3 / sum;
+    R q0 = R(-3.0 / 12.0) * v1 + R(13.0 / 12.0) * v2 - R(23.0 / 12.0) * v3 + R(25.0 / 12.0) * v4;
+    R q1 = R(1.0 / 12.0) * v2 - R(5.0 / 12.0) * v3 + R(13.0 / 12.0) * v4 + R(3.0 / 12.0) * v5;
+    R q2 = R(-1.0 / 12.0) * v3 + R(7.0 / 12.0) * v4 + R(7.0 / 12.0) * v5 - R(1.0 / 12.0) * v6;
+    R q3 = R(3.0 / 12.0) * v4 + R(13.0 / 12.0) * v5 - R(5.0 / 12.0) * v6 + R(1.0 / 12.0) * v7;
+    return W0 * q0 + W1 * q1 + W2 * q2 + W3 * q3;
+}
+// weno7_P(&pp[3]) + weno7_M(&mm[3]), WENO7s_schemes.hpp:8-128
+template <class R>
+R weno7(const R *f, const R *m) {
+    R tp = weno7_body(f[-3], f[-2], f[-1], f[0], f[1], f[2], f[3]);
+    R tm = weno7_body(m[4], m[3], m[2], m[1], m[0], m[-1], m[-2]);
+    return tp + tm;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Convective flux at face (i+1/2) in direction d:
+// ReconstructFlux{X,Y,Z}, Reconstruction_kernels.hpp:8-199 with MARCO_FLUXWALL_WENO5 / _WENO7
+// (Eigen_callback.h:127-230).
+// ---------------------------------------------------------------------------------------------
+template <class R>
+void face_flux(const Config &cf, const ThermoTable &tt, const Fields<R> &f, const std::vector<R> &UI, int d, int i, int j,
+               int k, R *Fwall_out) {
+    using std::fabs;
+    using std::fmax;
+    const xfg_block &b = cf.bl;
+    const int E = cf.E();
+    const size_t Xmax = b.Xmax, Ymax = b.Ymax;
+    const size_t stride = d == 0 ? 1 : (d == 1 ? Xmax : Xmax * Ymax);
+    const size_t id_l = Xmax * Ymax * k + Xmax * j + i;
+    const size_t id_r = id_l + stride;
+    const std::vector<R> &Fl = d == 0 ? f.FluxF : (d == 1 ? f.FluxG : f.FluxH);
+    const std::vector<R> &eig = f.eig[d];
+    Face<R> F;
+    face_state(cf, tt, f, id_l, id_r, F);
+    const int order = cf.sc.scheme_order;
+    const int at = cf.sc.artificial_type;
+    R out[kMaxE];
+    for (int n = 0; n < E; n++) out[n] = R(0.0);
+    R acc[kMaxE];
+    bool first[kMaxE];
+    for (int n = 0; n < E; n++) first[n] = true;
+    for (int n = 0; n < E; n++) {
+        Vec<R> l;
+        R ev;
+        left_row(cf, d, n, F, l, ev);
+        R av;
+        if (order == 7) {
+            R elm = ev;
+            R ll = eig[E * id_l + n], lr = eig[E * id_r + n];
+            if (ll * lr < R(0.0))
+                for (int m = -3; m < 5; m++) elm = fmax(elm, fabs(eig[E * (id_l + (long)m * (long)stride) + n]));
+            av = at == XFG_ROE ? ev : (at == XFG_LLF ? elm : f.eigen_block[d][n]);
+        } else {
+            R elm = R(0.0);
+            for (int m = -2; m < 4; m++) elm = fmax(elm, fabs(eig[E * (id_l + (long)m * (long)stride) + n]));
+            av = at == XFG_ROE ? ev : (at == XFG_LLF ? elm : f.eigen_block[d][n]);
+        }
+        // project U and F at points m = -3..4 (index m+3); WENO5 reads m = -2..3 only
+        R pp[8], mm[8];
+        const int m0 = order == 7 ? -3 : -2, m1 = order == 7 ? 4 : 3;
+        for (int m = m0; m <= m1; m++) {
+            size_t idm = id_l + (long)m * (long)stride;
+            R uf = dot(l, &UI[E * idm], E);
+            R ff = dot(l, &Fl[E * idm], E);
+            pp[m + 3] = R(0.5) * (ff + av * uf);
+            mm[m + 3] = R(0.5) * (ff - av * uf);
+        }
+        R f_flux = order == 7 ? weno7(&pp[3], &mm[3]) : weno5(&pp[3], &mm[3]);
+        Vec<R> r;
+        right_col(cf, d, n, F, r);
+        // _p[n][n1] = f_flux * r[n1]; Fwall[n1] = sum_n _p[n][n1]
+        for (int n1 = 0; n1 < E; n1++) {
+            R t;
+            switch (r.k[n1]) {
+            case KZ: continue;
+            case KP1: t = f_flux; break;
+            case KM1: t = -f_flux; break;
+            default: t = f_flux * r.v[n1]; break;
+            }
+            acc[n1] = first[n1] ? t : acc[n1] + t;
+            first[n1] = false;
+        }
+    }
+    for (int n = 0; n < E; n++) Fwall_out[n] = first[n] ? R(0.0) : acc[n];
+    (void)out;
+}
+
+// GetLocalEigen, Eigen_value.hpp:5-36, for direction d on all cells.
+template <class R>
+void local_eigen(const Config &cf, Fields<R> &f, int d) {
+    const long n = (long)cf.ncell();
+    const int E = cf.E();
+    std::vector<R> &eig = f.eig[d];
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < n; id++) {
+        if (cf.sc.scheme_order == 7) {
+            for (int m = 0; m < E; m++) eig[E * id + m] = R(0.0);
+            continue;
+        }
+        const R AA = R(d == 0 ? 1.0 : 0.0), BB = R(d == 1 ? 1.0 : 0.0), CC = R(d == 2 ? 1.0 : 0.0);
+        // uu = AA*u + BB*v + CC*w, evaluated exactly (the zero terms contribute +0.0)
+        R uu = d == 0 ? f.u[id] : (d == 1 ? f.v[id] : f.w[id]);
+        (void)AA, (void)BB, (void)CC;
+        R uuPc = uu + f.c[id], uuMc = uu - f.c[id];
+        eig[E * id + 0] = uuMc;
+        for (int m = 1; m < E - 1; m++) eig[E * id + m] = uu;
+        eig[E * id + E - 1] = uuPc;
+    }
+}
+
+// GetLU, ConVenction_block.hpp:10-617 (inviscid, no positivity preserving), in its three phases:
+// local eigenvalues + global LF maxima, face fluxes per direction, flux divergence.
+template <class R>
+void lu_eigen(const Config &cf, Fields<R> &f) {
+    using std::fabs;
+    using std::fmax;
+    const xfg_block &b = cf.bl;
+    const int E = cf.E();
+    const int dims[3] = {b.DimX, b.DimY, b.DimZ};
+    const long ncell = (long)cf.ncell();
+    for (int d = 0; d < 3; d++) {
+        if (!dims[d]) continue;
+        local_eigen(cf, f, d);
+        for (int n = 0; n < E; n++) {  // ConVenction_block.hpp:115-215
+            R mx = R(0.0);
+            for (long id = 0; id < ncell; id++) mx = fmax(mx, fabs(f.eig[d][E * id + n]));
+            f.eigen_block[d][n] = mx;
+        }
+    }
+}
+
+// ReconstructFlux{X,Y,Z} launch ranges, ConVenction_block.hpp:217-320: faces i+1/2 for
+// i in [Bwidth-1, inner+Bwidth) along d, inner cells along the other directions.
+template <class R>
+void lu_faces(const Config &cf, Fields<R> &f, const std::vector<R> &UI, int d) {
+    const xfg_block &b = cf.bl;
+    const ThermoTable tt = cf.table();
+    const int E = cf.E();
+    const int i0 = b.Bwidth_X - (d == 0 ? 1 : 0), j0 = b.Bwidth_Y - (d == 1 ? 1 : 0), k0 = b.Bwidth_Z - (d == 2 ? 1 : 0);
+    const int i1 = b.X_inner + b.Bwidth_X, j1 = b.Y_inner + b.Bwidth_Y, k1 = b.Z_inner + b.Bwidth_Z;
+    std::vector<R> &Fw = f.Fw[d];
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = k0; k < k1; k++)
+        for (int j = j0; j < j1; j++)
+            for (int i = i0; i < i1; i++) {
+                size_t id = (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i;
+                face_flux(cf, tt, f, UI, d, i, j, k, &Fw[E * id]);
+            }
+}
+
+// UpdateFluidLU, Reconstruction_kernels.hpp:201-234, inner cells.
+template <class R>
+void lu_divergence(const Config &cf, Fields<R> &f) {
+    const xfg_block &b = cf.bl;
+    const int E = cf.E();
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = b.Bwidth_Z; k < b.Z_inner + b.Bwidth_Z; k++)
+        for (int j = b.Bwidth_Y; j < b.Y_inner + b.Bwidth_Y; j++)
+            for (int i = b.Bwidth_X; i < b.X_inner + b.Bwidth_X; i++) {
+                size_t id = (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i;
+                size_t im = id - 1, jm = id - b.Xmax, km = id - (size_t)b.Xmax * b.Ymax;
+                for (int n = 0; n < E; n++) {
+                    R LU0 = R(0.0);
+                    bool first = true;  // 0.0 + t == t
+                    if (b.DimX) { R t = (f.Fw[0][E * im + n] - f.Fw[0][E * id + n]) * b._dx; LU0 = t; first = false; }
+                    if (b.DimY) { R t = (f.Fw[1][E * jm + n] - f.Fw[1][E * id + n]) * b._dy; LU0 = first ? t : LU0 + t; first = false; }
+                    if (b.DimZ) { R t = (f.Fw[2][E * km + n] - f.Fw[2][E * id + n]) * b._dz; LU0 = first ? t : LU0 + t; first = false; }
+                    f.LU[E * id + n] = LU0;
+                }
+            }
+}
+
+template <class R>
+void compute_lu(const Config &cf, Fields<R> &f, const std::vector<R> &UI) {
+    const int dims[3] = {cf.bl.DimX, cf.bl.DimY, cf.bl.DimZ};
+    lu_eigen(cf, f);
+    for (int d = 0; d < 3; d++)
+        if (dims[d]) lu_faces(cf, f, UI, d);
+    lu_divergence(cf, f);
+}
+
+// UpdateURK3rdKernel, Update_kernels.hpp:64-94, inner cells.
+template <class R>
+void update_rk3(const Config &cf, Fields<R> &f, int flag, R dt) {
+    const xfg_block &b = cf.bl;
+    const int E = cf.E();
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = b.Bwidth_Z; k < b.Z_inner + b.Bwidth_Z; k++)
+        for (int j = b.Bwidth_Y; j < b.Y_inner + b.Bwidth_Y; j++)
+            for (int i = b.Bwidth_X; i < b.X_inner + b.Bwidth_X; i++) {
+                size_t id = (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i;
+                for (int n = 0; n < E; n++) {
+                    size_t q = E * id + n;
+                    if (flag == 1) f.U1[q] = f.U[q] + dt * f.LU[q];
+                    else if (flag == 2) f.U1[q] = R(0.75) * f.U[q] + R(0.25) * f.U1[q] + R(0.25) * dt * f.LU[q];
+                    else f.U[q] = (f.U[q] + R(2.0) * f.U1[q] + R(2.0) * dt * f.LU[q]) * R(kOT);
+                }
+            }
+}
+
+// GetDt, GlobalDt_block.hpp:6-114: max over all cells of |u_d| + sqrt(1.4 p / rho).
+template <class R>
+R get_dt(const Config &cf, Fields<R> &f) {
+    using std::fabs;
+    using std::fmax;
+    using std::sqrt;
+    const xfg_block &b = cf.bl;
+    const long n = (long)cf.ncell();
+    const std::vector<R> *vel[3] = {&f.u, &f.v, &f.w};
+    const int dims[3] = {b.DimX, b.DimY, b.DimZ};
+    for (int d = 0; d < 3; d++) {
+        f.uvw_c_max[d] = R(0.0);
+        if (!dims[d]) continue;
+        R mx = R(0.0);
+        for (long id = 0; id < n; id++) {
+            R c_local = sqrt(R(1.4) * f.p[id] / f.rho[id]);
+            mx = fmax(mx, fabs((*vel[d])[id]) + c_local);
+        }
+        f.uvw_c_max[d] = mx;
+    }
+    R dtref = f.uvw_c_max[0] * b._dx + f.uvw_c_max[1] * b._dy + f.uvw_c_max[2] * b._dz;
+    return R(b.CFLnumber) / dtref;
+}
+
+}  // namespace xfo

@@ -1,0 +1,76 @@
+"""The C-ABI library loads, exports every declared entry point, and its structs match ctypes.
+No compute calls (no GPU here)."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from xfluids_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "xfluids_gb300.h")
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(xfg_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(cuda_lib):
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(cuda_lib, s)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", abi.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (xfg_\w+)", out))
+    assert set(syms) <= exported
+
+
+def test_build_info_lists_kernels(cuda_lib):
+    info = cuda_lib.xfg_build_info().decode()
+    assert "sm_103a" in info and "ncop1/weno5" in info and "cop5/weno7" in info
+
+
+PROBE = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "xfluids_gb300.h"
+int main(void) {
+    printf("%zu %zu %zu\n", sizeof(xfg_block), sizeof(xfg_thermal), sizeof(xfg_scheme));
+    printf("%zu %zu %zu\n", offsetof(xfg_block, dx), offsetof(xfg_block, CFLnumber), offsetof(xfg_block, Boundarys));
+    printf("%zu %zu\n", offsetof(xfg_thermal, Hia), offsetof(xfg_thermal, Hib));
+    printf("%zu %zu\n", offsetof(xfg_scheme, ncop_gamma), offsetof(xfg_scheme, precision));
+    return 0;
+}
+"""
+
+
+def test_struct_layouts_match_header():
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "probe.c")
+        exe = os.path.join(d, "probe")
+        open(src, "w").write(PROBE)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+        vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    B, T, S = abi.Block, abi.Thermal, abi.Scheme
+    expect = [C.sizeof(B), C.sizeof(T), C.sizeof(S), B.dx.offset, B.CFLnumber.offset, B.Boundarys.offset,
+              T.Hia.offset, T.Hib.offset, S.ncop_gamma.offset, S.precision.offset]
+    assert vals == expect
+
+
+def test_create_rejects_bad_arguments(cuda_lib):
+    from xfluids_gb300 import cases
+    b, s, th, U, T = cases.sod(32)
+    s.scheme_order = 6
+    h = C.c_void_p()
+    rc = cuda_lib.xfg_create(C.byref(b), C.byref(s), C.byref(th), 0, C.byref(h))
+    assert rc == -1 and not h.value
+    assert "scheme_order" in cuda_lib.xfg_last_error().decode()
+    s.scheme_order = 5
+    b.Bwidth_X = 2
+    rc = cuda_lib.xfg_create(C.byref(b), C.byref(s), C.byref(th), 0, C.byref(h))
+    assert rc == -1 and "Bwidth" in cuda_lib.xfg_last_error().decode()

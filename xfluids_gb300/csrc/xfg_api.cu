@@ -1,0 +1,619 @@
+// xfg_api.cu - C ABI of the library (include/xfluids_gb300.h): handle, device memory, the
+// stage-by-stage entry points that replace class Fluid's methods, the fused step and the
+// graph-replayed multi-step advance.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/xfluids_gb300.h"
+#include "xfg_kernels.cuh"
+#include "xfg_ops.h"
+
+using namespace xfg;
+
+// ---------------------------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------------------------
+static thread_local std::string g_err;
+static int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+#define CK(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail(-2, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                        \
+    } while (0)
+
+// ---------------------------------------------------------------------------------------------
+// launcher registry
+// ---------------------------------------------------------------------------------------------
+namespace xfg {
+static std::vector<const Ops *> &registry() {
+    static std::vector<const Ops *> r;
+    return r;
+}
+void register_ops(const Ops *ops) { registry().push_back(ops); }
+const Ops *find_ops(int cop, int ns, int order) {
+    for (const Ops *o : registry())
+        if (o->cop == cop && o->ns == ns && o->order == order) return o;
+    return nullptr;
+}
+}  // namespace xfg
+
+// ---------------------------------------------------------------------------------------------
+// helper kernels
+// ---------------------------------------------------------------------------------------------
+__global__ void k_aos_to_soa(const double *__restrict__ aos, double *__restrict__ soa, int E, long long N,
+                             long long P) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * E) return;
+    long long id = t / E;
+    int n = (int)(t % E);
+    soa[n * P + id] = aos[t];
+}
+__global__ void k_soa_to_aos(const double *__restrict__ soa, double *__restrict__ aos, int E, long long N,
+                             long long P) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * E) return;
+    long long id = t / E;
+    int n = (int)(t % E);
+    aos[t] = soa[n * P + id];
+}
+__global__ void k_set_time(double *dtbuf, double t, double target) {
+    dtbuf[0] = 0.0, dtbuf[1] = t, dtbuf[2] = target, dtbuf[3] = 0.0, dtbuf[4] = 0.0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// handle
+// ---------------------------------------------------------------------------------------------
+struct xfg_handle {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    xfg_block bl;
+    xfg_scheme sc;
+    const Ops *ops = nullptr;
+    LaunchCtx ctx;
+    int E = 5, NS = 1;
+    long long N = 0, P = 0;
+    void *pool = nullptr;
+    size_t pool_bytes = 0;
+    double *stage = nullptr;          // AoS staging for transposes
+    unsigned long long *glf = nullptr;
+    double *host_dtbuf = nullptr;     // pinned mirror of dtbuf
+    int *host_err = nullptr;          // pinned mirror of err
+    double t = 0.0;
+    bool states_ready = false;
+    cudaGraphExec_t graph = nullptr;  // one fused step, replayed by xfg_advance
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *t) {
+    if (!b || !s || !t) return fail(-1, "null argument");
+    if (s->scheme_order != 5 && s->scheme_order != 7) return fail(-1, "scheme_order must be 5 or 7 (got %d)", s->scheme_order);
+    if (s->artificial_type < 1 || s->artificial_type > 3) return fail(-1, "artificial_type must be 1..3");
+    if (s->cop && (s->num_species < 2 || s->num_species > XFG_MAX_SPECIES))
+        return fail(-1, "num_species %d out of range for COP", s->num_species);
+    if (!s->cop && s->num_species != 1) return fail(-1, "num_species must be 1 without COP");
+    if (s->cop && t->num_species != s->num_species) return fail(-1, "thermal.num_species != scheme.num_species");
+    const int dims[3] = {b->DimX, b->DimY, b->DimZ};
+    const int inner[3] = {b->X_inner, b->Y_inner, b->Z_inner};
+    const int bw[3] = {b->Bwidth_X, b->Bwidth_Y, b->Bwidth_Z};
+    const int mx[3] = {b->Xmax, b->Ymax, b->Zmax};
+    const int need = s->scheme_order == 7 ? 4 : 3;
+    for (int d = 0; d < 3; d++) {
+        if (dims[d]) {
+            if (bw[d] < need) return fail(-1, "Bwidth of direction %d is %d, the scheme needs >= %d", d, bw[d], need);
+            if (inner[d] < bw[d]) return fail(-1, "inner size %d of direction %d below Bwidth %d", inner[d], d, bw[d]);
+            if (mx[d] != inner[d] + 2 * bw[d]) return fail(-1, "Xmax/Ymax/Zmax inconsistent in direction %d", d);
+        } else if (mx[d] != 1 || inner[d] != 1 || bw[d] != 0) {
+            return fail(-1, "absent direction %d must have max = inner = 1 and Bwidth = 0", d);
+        }
+    }
+    if (!(dims[0] || dims[1] || dims[2])) return fail(-1, "no active direction");
+    return 0;
+}
+
+extern "C" {
+
+const char *xfg_last_error(void) { return g_err.c_str(); }
+
+const char *xfg_build_info(void) {
+    static std::string info;
+    if (info.empty()) {
+        info = "xfluids_gb300 sm_103a; kernels:";
+        for (const Ops *o : registry()) {
+            char b[64];
+            snprintf(b, sizeof b, " %s%d/weno%d", o->cop ? "cop" : "ncop", o->ns, o->order);
+            info += b;
+        }
+    }
+    return info.c_str();
+}
+
+int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_thermal *thermal, int device,
+               xfg_handle **out) {
+    if (!out) return fail(-1, "null out");
+    *out = nullptr;
+    int v = validate(block, scheme, thermal);
+    if (v) return v;
+    const Ops *ops = find_ops(scheme->cop ? 1 : 0, scheme->cop ? scheme->num_species : 1, scheme->scheme_order);
+    if (!ops) return fail(-1, "no kernels built for cop=%d num_species=%d order=%d", scheme->cop, scheme->num_species, scheme->scheme_order);
+    CK(cudaSetDevice(device));
+    xfg_handle *h = new xfg_handle();
+    h->device = device;
+    h->bl = *block;
+    h->sc = *scheme;
+    h->ops = ops;
+    h->NS = scheme->cop ? scheme->num_species : 1;
+    h->E = scheme->cop ? scheme->num_species + 4 : 5;
+    h->N = (long long)block->Xmax * block->Ymax * block->Zmax;
+    h->P = (long long)align_up((size_t)h->N, 64);
+    const int E = h->E, NS = h->NS;
+    const bool mixed = scheme->precision == XFG_MIXED;
+    const int dims[3] = {block->DimX, block->DimY, block->DimZ};
+    const size_t arr8 = (size_t)h->P * 8, arr4 = align_up((size_t)h->P * 4, 256);
+    // layout of the pool
+    size_t nd = 3 * E + 12 + (scheme->cop ? NS : 0);           // U, U1, LU, primitives, y
+    for (int d = 0; d < 3; d++)
+        if (dims[d] && !mixed) nd += 2 * E;                       // F, Fw
+    size_t nf = 0;
+    if (mixed) {
+        nf = E + 7;
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) nf += 2 * E;                             // Ff, Fwf
+    }
+    const size_t stage_elems = (size_t)h->N * (E > NS ? E : NS);
+    const size_t small = 4096;
+    size_t bytes = nd * arr8 + nf * arr4 + align_up(stage_elems * 8, 256) + small;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&h->pool, bytes);
+    if (e != cudaSuccess) {
+        if (h->st) cudaStreamDestroy(h->st);
+        delete h;
+        return fail(-3, "device allocation of %.3f GB failed: %s", bytes / 1e9, cudaGetErrorString(e));
+    }
+    h->pool_bytes = bytes;
+    cudaMemsetAsync(h->pool, 0, bytes, h->st);
+    char *p = (char *)h->pool;
+    auto take8 = [&](size_t count) { double *r = (double *)p; p += count * arr8; return r; };
+    auto take4 = [&](size_t count) { float *r = (float *)p; p += count * arr4; return r; };
+    DevFields &f = h->ctx.f;
+    std::memset(&f, 0, sizeof f);
+    f.U = take8(E), f.U1 = take8(E), f.LU = take8(E);
+    f.rho = take8(1), f.u = take8(1), f.v = take8(1), f.w = take8(1), f.p = take8(1), f.H = take8(1);
+    f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
+    if (scheme->cop) f.y = take8(NS);
+    for (int d = 0; d < 3; d++)
+        if (dims[d] && !mixed) f.F[d] = take8(E), f.Fw[d] = take8(E);
+    if (mixed) {
+        f.Uf = take4(E);
+        f.primf = take4(7);
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) f.Ff[d] = take4(E), f.Fwf[d] = take4(E);
+    }
+    h->stage = (double *)p;
+    p += align_up(stage_elems * 8, 256);
+    f.lam = (unsigned long long *)p;              // 3 x u64
+    h->glf = (unsigned long long *)(p + 64);      // 9 x u64
+    f.dtbuf = (double *)(p + 256);                // 8 doubles
+    f.err = (int *)(p + 512);                     // 8 ints (+ NaN estimate scratch after)
+    // launch context
+    Geo &g = h->ctx.g;
+    g.Xmax = block->Xmax, g.Ymax = block->Ymax, g.Zmax = block->Zmax;
+    g.Xi = block->X_inner, g.Yi = block->Y_inner, g.Zi = block->Z_inner;
+    g.Bx = block->Bwidth_X, g.By = block->Bwidth_Y, g.Bz = block->Bwidth_Z;
+    g.dimx = block->DimX, g.dimy = block->DimY, g.dimz = block->DimZ;
+    g._dx = block->_dx, g._dy = block->_dy, g._dz = block->_dz;
+    g.pitch = h->P;
+    DevThermo &th = h->ctx.th;
+    std::memset(&th, 0, sizeof th);
+    for (int n = 0; n < XFG_MAX_SPECIES; n++) th.Ri[n] = thermal->Ri[n], th._Wi[n] = thermal->_Wi[n];
+    for (int q = 0; q < XFG_MAX_SPECIES * 21; q++) th.Hia[q] = thermal->Hia[q];
+    for (int q = 0; q < XFG_MAX_SPECIES * 6; q++) th.Hib[q] = thermal->Hib[q];
+    th.nasa = scheme->thermo ? 1 : 0;
+    th.ncop_gamma = scheme->ncop_gamma;
+    h->ctx.st = h->st;
+    h->ctx.artificial = scheme->artificial_type;
+    h->ctx.ghost = scheme->ghost_species;
+    for (int q = 0; q < 6; q++) h->ctx.bc[q] = block->Boundarys[q];
+    h->ctx.glf = scheme->artificial_type == XFG_GLF ? (const double *)h->glf : nullptr;
+    h->ctx.precision = scheme->precision;
+    e = cudaMallocHost(&h->host_dtbuf, 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&h->host_err, 64 * sizeof(int));
+    for (int q = 0; q < 4 && e == cudaSuccess; q++) e = cudaEventCreate(&h->ev[q]);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) {
+        xfg_destroy(h);
+        return fail(-2, "handle setup failed: %s", cudaGetErrorString(e));
+    }
+    *out = h;
+    return 0;
+}
+
+int xfg_destroy(xfg_handle *h) {
+    if (!h) return 0;
+    cudaSetDevice(h->device);
+    if (h->st) cudaStreamSynchronize(h->st);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (int q = 0; q < 4; q++)
+        if (h->ev[q]) cudaEventDestroy(h->ev[q]);
+    if (h->pool) cudaFree(h->pool);
+    if (h->host_dtbuf) cudaFreeHost(h->host_dtbuf);
+    if (h->host_err) cudaFreeHost(h->host_err);
+    if (h->st) cudaStreamDestroy(h->st);
+    delete h;
+    return 0;
+}
+
+static double *stage_U(xfg_handle *h, int flag) { return flag == 0 ? h->ctx.f.U : h->ctx.f.U1; }
+
+int xfg_set_state(xfg_handle *h, const double *U_aos, const double *T) {
+    if (!h || !U_aos) return fail(-1, "null argument");
+    CK(cudaSetDevice(h->device));
+    const size_t bytes = (size_t)h->N * h->E * sizeof(double);
+    CK(cudaMemcpyAsync(h->stage, U_aos, bytes, cudaMemcpyDefault, h->st));
+    const long long tot = h->N * h->E;
+    k_aos_to_soa<<<grid_for(tot, 256), 256, 0, h->st>>>(h->stage, h->ctx.f.U, h->E, h->N, h->P);
+    CK(cudaMemcpyAsync(h->ctx.f.U1, h->ctx.f.U, (size_t)h->P * h->E * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    if (T) CK(cudaMemcpyAsync(h->ctx.f.T, T, (size_t)h->N * sizeof(double), cudaMemcpyDefault, h->st));
+    CK(cudaMemsetAsync(h->ctx.f.err, 0, 64 * sizeof(int), h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->states_ready = false;
+    return 0;
+}
+
+int xfg_get_array(xfg_handle *h, int which, double *out) {
+    if (!h || !out) return fail(-1, "null argument");
+    CK(cudaSetDevice(h->device));
+    DevFields &f = h->ctx.f;
+    const double *src = nullptr;
+    int comps = 1;
+    switch (which) {
+    case XFG_U: src = f.U, comps = h->E; break;
+    case XFG_U1: src = f.U1, comps = h->E; break;
+    case XFG_LU: src = f.LU, comps = h->E; break;
+    case XFG_RHO: src = f.rho; break;
+    case XFG_P: src = f.p; break;
+    case XFG_U_VEL: src = f.u; break;
+    case XFG_V_VEL: src = f.v; break;
+    case XFG_W_VEL: src = f.w; break;
+    case XFG_C: src = f.c; break;
+    case XFG_H: src = f.H; break;
+    case XFG_T: src = f.T; break;
+    case XFG_GAMMA: src = f.gamma; break;
+    case XFG_E: src = f.e; break;
+    case XFG_CP: src = f.Cp; break;
+    case XFG_R: src = f.R; break;
+    case XFG_Y: src = f.y, comps = h->NS; break;
+    case XFG_FWX: src = f.Fw[0], comps = h->E; break;
+    case XFG_FWY: src = f.Fw[1], comps = h->E; break;
+    case XFG_FWZ: src = f.Fw[2], comps = h->E; break;
+    default: return fail(-1, "unknown array %d", which);
+    }
+    if (!src) return fail(-1, "array %d is not kept by this handle", which);
+    if (comps == 1) {
+        CK(cudaMemcpyAsync(out, src, (size_t)h->N * sizeof(double), cudaMemcpyDefault, h->st));
+    } else {
+        const long long tot = h->N * comps;
+        k_soa_to_aos<<<grid_for(tot, 256), 256, 0, h->st>>>(src, h->stage, comps, h->N, h->P);
+        CK(cudaMemcpyAsync(out, h->stage, (size_t)tot * sizeof(double), cudaMemcpyDefault, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return 0;
+}
+
+int xfg_boundary(xfg_handle *h, int flag) {
+    if (!h) return fail(-1, "null handle");
+    CK(cudaSetDevice(h->device));
+    h->ops->bc(h->ctx, stage_U(h, flag), nullptr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+    return 0;
+}
+
+int xfg_update_states(xfg_handle *h, int flag, int *error, float *timers4) {
+    if (!h) return fail(-1, "null handle");
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemsetAsync(h->ctx.f.lam, 0, 3 * sizeof(unsigned long long), h->st));
+    CK(cudaMemsetAsync(h->ctx.f.err + ERR_PRIM, 0, sizeof(int), h->st));
+    CK(cudaEventRecord(h->ev[0], h->st));
+    h->ops->states(h->ctx, stage_U(h, flag), 1, 0);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[1], h->st));
+    CK(cudaMemcpyAsync(h->host_err, h->ctx.f.err, 8 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->states_ready = true;
+    if (error) *error = h->host_err[ERR_PRIM] ? 1 : 0;
+    if (timers4) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+        timers4[0] = timers4[1] = timers4[2] = 0.f;
+        timers4[3] = ms * 1e-3f;  // runtime_states, seconds like OutThisTime
+    }
+    return 0;
+}
+
+static void launch_lu(xfg_handle *h, double *UI, int guard) {
+    const int dims[3] = {h->bl.DimX, h->bl.DimY, h->bl.DimZ};
+    if (h->sc.artificial_type == XFG_GLF) h->ops->glf(h->ctx, h->glf, guard);
+    for (int d = 0; d < 3; d++)
+        if (dims[d]) h->ops->faces(h->ctx, d, UI, guard);
+}
+
+int xfg_compute_lu(xfg_handle *h, int flag, float *timers23) {
+    if (!h) return fail(-1, "null handle");
+    CK(cudaSetDevice(h->device));
+    CK(cudaEventRecord(h->ev[0], h->st));
+    launch_lu(h, stage_U(h, flag), 0);
+    CK(cudaEventRecord(h->ev[1], h->st));
+    h->ops->div_rk(h->ctx, 0, 0.0, nullptr, 0, 1, 0);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->ev[2], h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (timers23) {
+        for (int q = 0; q < 23; q++) timers23[q] = 0.f;
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, h->ev[0], h->ev[1]);
+        cudaEventElapsedTime(&b, h->ev[1], h->ev[2]);
+        timers23[11] = a * 1e-3f;  // runtime_flux
+        timers23[22] = b * 1e-3f;  // runtime_updatelu
+    }
+    return 0;
+}
+
+int xfg_update_rk3(xfg_handle *h, int flag, double dt) {
+    if (!h) return fail(-1, "null handle");
+    if (flag < 1 || flag > 3) return fail(-1, "flag must be 1..3");
+    CK(cudaSetDevice(h->device));
+    h->ops->rk(h->ctx, flag, dt);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->st));
+    return 0;
+}
+
+int xfg_get_dt(xfg_handle *h, double *dt) {
+    if (!h || !dt) return fail(-1, "null argument");
+    if (!h->states_ready) return fail(-1, "xfg_get_dt needs a preceding xfg_update_states");
+    CK(cudaSetDevice(h->device));
+    unsigned long long lam[3];
+    CK(cudaMemcpyAsync(lam, h->ctx.f.lam, sizeof lam, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    double l[3];
+    for (int q = 0; q < 3; q++) std::memcpy(&l[q], &lam[q], 8);
+    const double dtref = l[0] * h->bl._dx + l[1] * h->bl._dy + l[2] * h->bl._dz;
+    *dt = h->bl.CFLnumber / dtref;
+    return 0;
+}
+
+int xfg_estimate_nan(xfg_handle *h, int flag, int *error, int *error_pos) {
+    if (!h) return fail(-1, "null handle");
+    CK(cudaSetDevice(h->device));
+    int *pos = h->ctx.f.err + 16;  // scratch after the error words
+    CK(cudaMemsetAsync(pos, 0, 40 * sizeof(int), h->st));
+    const double *UI = (flag == 1 || flag == 2) ? h->ctx.f.U1 : h->ctx.f.U;  // src/Fluids.cpp:966-983
+    h->ops->estimate_nan(h->ctx, UI, pos);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->host_err + 16, pos, 40 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const int *hp = h->host_err + 16;
+    const int E = h->E;
+    if (error) *error = hp[E] ? 1 : 0;
+    if (error_pos) {
+        for (int n = 0; n < E; n++) error_pos[n] = hp[n];
+        error_pos[E] = 0;
+        for (int q = 1; q <= 3; q++) error_pos[E + q] = hp[E + q];
+    }
+    return hp[E] ? 10000 : 0;
+}
+
+// The launches of one fused step, all guarded by the device "done" flag so that replays past
+// the target time do nothing.
+static void launch_step(xfg_handle *h) {
+    DevFields &f = h->ctx.f;
+    k_dt_step<<<1, 1, 0, h->st>>>(h->ctx.g, f, h->bl.CFLnumber);
+    for (int flag = 1; flag <= 3; flag++) {
+        double *UI = flag == 1 ? f.U : f.U1;
+        h->ops->bc(h->ctx, UI, f.dtbuf);
+        h->ops->states(h->ctx, UI, flag == 3 ? 1 : 0, 1);
+        launch_lu(h, UI, 1);
+        h->ops->div_rk(h->ctx, flag, 0.0, f.dtbuf, 1, 0, 1);
+    }
+}
+
+static int finish(xfg_handle *h, double *t, double *dt, int *steps) {
+    CK(cudaMemcpyAsync(h->host_dtbuf, h->ctx.f.dtbuf, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->host_err, h->ctx.f.err, 8 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->t = h->host_dtbuf[1];
+    if (t) *t = h->t;
+    if (dt) *dt = h->host_dtbuf[0];
+    if (steps) *steps = (int)h->host_dtbuf[3];
+    if (h->host_err[ERR_STATE]) return 10000;
+    if (h->host_err[ERR_PRIM]) return 1;
+    return 0;
+}
+
+int xfg_step(xfg_handle *h, double target_t, double *t, double *dt) {
+    if (!h) return fail(-1, "null handle");
+    if (!h->states_ready) return fail(-1, "xfg_step needs a preceding xfg_update_states (main.cpp:45-47)");
+    CK(cudaSetDevice(h->device));
+    k_set_time<<<1, 1, 0, h->st>>>(h->ctx.f.dtbuf, h->t, target_t);
+    launch_step(h);
+    CK(cudaGetLastError());
+    return finish(h, t, dt, nullptr);
+}
+
+int xfg_advance(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done) {
+    if (!h) return fail(-1, "null handle");
+    if (!h->states_ready) return fail(-1, "xfg_advance needs a preceding xfg_update_states (main.cpp:45-47)");
+    CK(cudaSetDevice(h->device));
+    k_set_time<<<1, 1, 0, h->st>>>(h->ctx.f.dtbuf, h->t, target_t);
+    CK(cudaGetLastError());
+    if (!h->graph) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+        launch_step(h);
+        cudaError_t e = cudaStreamEndCapture(h->st, &g);
+        if (e != cudaSuccess) return fail(-2, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&h->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(-2, "graph instantiate failed: %s", cudaGetErrorString(e));
+    }
+    for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(h->graph, h->st));
+    return finish(h, t, nullptr, steps_done);
+}
+
+// Per-phase device times of one fused step (ms, summed over the 3 stages): [0] dt, [1] boundary,
+// [2] states, [3..5] faces x/y/z, [6] divergence + RK. Events on the handle's stream.
+int xfg_time_phases(xfg_handle *h, double target_t, float *ms_out) {
+    if (!h || !ms_out) return fail(-1, "null argument");
+    if (!h->states_ready) return fail(-1, "xfg_time_phases needs a preceding xfg_update_states");
+    CK(cudaSetDevice(h->device));
+    DevFields &f = h->ctx.f;
+    const int dims[3] = {h->bl.DimX, h->bl.DimY, h->bl.DimZ};
+    cudaEvent_t ev[32];
+    int ne = 0;
+    for (int q = 0; q < 32; q++) CK(cudaEventCreate(&ev[q]));
+    int phase_of[32];
+    k_set_time<<<1, 1, 0, h->st>>>(f.dtbuf, h->t, target_t);
+    CK(cudaEventRecord(ev[ne++], h->st));
+    k_dt_step<<<1, 1, 0, h->st>>>(h->ctx.g, f, h->bl.CFLnumber);
+    phase_of[ne] = 0;
+        CK(cudaEventRecord(ev[ne++], h->st));
+    for (int flag = 1; flag <= 3; flag++) {
+        double *UI = flag == 1 ? f.U : f.U1;
+        h->ops->bc(h->ctx, UI, f.dtbuf);
+        phase_of[ne] = 1;
+        CK(cudaEventRecord(ev[ne++], h->st));
+        h->ops->states(h->ctx, UI, flag == 3 ? 1 : 0, 1);
+        phase_of[ne] = 2;
+        CK(cudaEventRecord(ev[ne++], h->st));
+        if (h->sc.artificial_type == XFG_GLF) h->ops->glf(h->ctx, h->glf, 1);
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) {
+                h->ops->faces(h->ctx, d, UI, 1);
+                phase_of[ne] = 3 + d;
+        CK(cudaEventRecord(ev[ne++], h->st));
+            }
+        h->ops->div_rk(h->ctx, flag, 0.0, f.dtbuf, 1, 0, 1);
+        phase_of[ne] = 6;
+        CK(cudaEventRecord(ev[ne++], h->st));
+    }
+    CK(cudaGetLastError());
+    int rc = finish(h, nullptr, nullptr, nullptr);
+    for (int q = 0; q < 7; q++) ms_out[q] = 0.f;
+    for (int q = 1; q < ne; q++) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[q - 1], ev[q]);
+        ms_out[phase_of[q]] += ms;
+    }
+    for (int q = 0; q < 32; q++) cudaEventDestroy(ev[q]);
+    return rc < 0 ? rc : 0;
+}
+
+int xfg_set_time(xfg_handle *h, double t) {
+    if (!h) return fail(-1, "null handle");
+    h->t = t;
+    return 0;
+}
+int xfg_get_time(xfg_handle *h, double *t) {
+    if (!h || !t) return fail(-1, "null argument");
+    *t = h->t;
+    return 0;
+}
+int xfg_synchronize(xfg_handle *h) {
+    if (!h) return fail(-1, "null handle");
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->st));
+    return 0;
+}
+int xfg_device_array(xfg_handle *h, int which, double **ptr, size_t *pitch) {
+    if (!h || !ptr) return fail(-1, "null argument");
+    DevFields &f = h->ctx.f;
+    double *a = nullptr;
+    switch (which) {
+    case XFG_U: a = f.U; break;
+    case XFG_U1: a = f.U1; break;
+    case XFG_LU: a = f.LU; break;
+    case XFG_RHO: a = f.rho; break;
+    case XFG_P: a = f.p; break;
+    case XFG_T: a = f.T; break;
+    default: return fail(-1, "array %d has no device view", which);
+    }
+    *ptr = a;
+    if (pitch) *pitch = (size_t)h->P;
+    return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// FMA throughput probe (roofline denominators of the compute-bound kernels)
+// ---------------------------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(256) k_fma_chain(T *out, int iters, T a, T b) {
+    T x0 = (T)threadIdx.x, x1 = x0 + T(1), x2 = x0 + T(2), x3 = x0 + T(3);
+    T x4 = x0 + T(4), x5 = x0 + T(5), x6 = x0 + T(6), x7 = x0 + T(7);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            x0 = fma(x0, a, b), x1 = fma(x1, a, b), x2 = fma(x2, a, b), x3 = fma(x3, a, b);
+            x4 = fma(x4, a, b), x5 = fma(x5, a, b), x6 = fma(x6, a, b), x7 = fma(x7, a, b);
+        }
+    }
+    T s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == T(-1.2345)) out[threadIdx.x] = s;  // keeps the chain live
+}
+
+template <class T>
+static double run_fma(int sms, int iters, cudaStream_t st, T *scratch) {
+    const int blocks = sms * 8, threads = 256;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a), cudaEventCreate(&b);
+    k_fma_chain<T><<<blocks, threads, 0, st>>>(scratch, iters / 8, T(0.999999), T(1e-7));  // warm-up
+    cudaEventRecord(a, st);
+    k_fma_chain<T><<<blocks, threads, 0, st>>>(scratch, iters, T(0.999999), T(1e-7));
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a), cudaEventDestroy(b);
+    const double flops = 2.0 * 8.0 * 8.0 * (double)iters * blocks * threads;
+    return flops / (ms * 1e-3);
+}
+
+extern "C" int xfg_measure_pipe_peaks(int device, double *out) {
+    if (!out) return fail(-1, "null out");
+    CK(cudaSetDevice(device));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    void *scratch;
+    CK(cudaMalloc(&scratch, 256 * sizeof(double)));
+    out[0] = run_fma<double>(sms, 2048, st, (double *)scratch);
+    out[1] = run_fma<float>(sms, 65536, st, (float *)scratch);
+    int clk = 0;
+    cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
+    out[2] = clk / 1000.0;
+    cudaError_t e = cudaGetLastError();
+    cudaFree(scratch);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return fail(-2, "peak probe failed: %s", cudaGetErrorString(e));
+    return 0;
+}

@@ -1,0 +1,364 @@
+// xfg_device.cuh - device functions of the convective right-hand side (FP64 and FP32 forms).
+//
+// Each function restates one reference device function (cited per function) with its operation
+// order. The state lives in HBM as SoA arrays (component n of cell id at n*pitch + id), so that a
+// warp reads 32 consecutive cells of one component per load. Compile-time template parameters:
+//   NS  - NUM_SPECIES (1 without COP), E = NS + 4 with COP else 5
+//   COP - multi-component mixture
+//   D   - sweep direction 0/1/2 (x/y/z)
+//   T   - arithmetic type of the reconstruction (double, or float in the mixed form)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/xfluids_gb300.h"
+
+namespace xfg {
+
+constexpr double kRu = 6.02214076e26 * 1.380649e-23 * 1.0E-3;  // global_setup.h:48-54
+constexpr double kOT = 1.0 / 3.0;
+constexpr double kSix = 1.0 / 6.0;
+
+template <bool COP, int NS>
+struct Sys {
+    static constexpr int E = COP ? NS + 4 : 5;
+    static constexpr int NCOP = COP ? NS - 1 : 0;
+};
+
+// Thermo tables passed by value to the kernels (lands in the constant bank).
+struct DevThermo {
+    double Ri[XFG_MAX_SPECIES];
+    double _Wi[XFG_MAX_SPECIES];
+    double Hia[XFG_MAX_SPECIES * 21];
+    double Hib[XFG_MAX_SPECIES * 6];
+    int nasa;
+    double ncop_gamma;
+};
+
+// Geometry of a block, x fastest.
+struct Geo {
+    int Xmax, Ymax, Zmax;
+    int Xi, Yi, Zi;   // inner sizes
+    int Bx, By, Bz;   // ghost widths
+    int dimx, dimy, dimz;
+    double _dx, _dy, _dz;
+    long long pitch;  // elements between components of a SoA array
+    __host__ __device__ long long ncell() const { return (long long)Xmax * Ymax * Zmax; }
+};
+
+// Device arrays of one block. All SoA with the block pitch.
+struct DevFields {
+    double *U, *U1, *LU;
+    double *rho, *u, *v, *w, *p, *H, *c, *T, *gamma, *e, *Cp, *R;
+    double *y;                 // NS components (COP)
+    double *F[3];              // physical fluxes per direction (E components)
+    double *Fw[3];             // face fluxes per direction (E components)
+    float *Uf, *Ff[3];         // FP32 copies of U and of the physical fluxes (mixed form)
+    float *primf;              // FP32 rho, u, v, w, H, p, c (7 components, mixed form)
+    float *Fwf[3];             // FP32 face fluxes (mixed form)
+    unsigned long long *lam;   // dt wave-speed maxima (3 x bit patterns of non-negative doubles)
+    double *dtbuf;             // [0] dt of the step, [1] time, [2] target time, [3] steps done
+    int *err;                  // error words: [0] state NaN code, [1] primitive error, [2] i, [3] j, [4] k
+};
+
+// ---------------------------------------------------------------------------------------------
+// Thermodynamics, src/solver_Ini/Thermo_device.h
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ int nasa_range(double T) {
+    return (T >= 1000.0 && T < 6000.0) ? 1 : (T < 1000.0 ? 0 : (T >= 6000.0 ? 2 : -1));
+}
+// HeatCapacity_NASA :10-23 / HeatCapacity_JANAF :29-40
+__device__ __forceinline__ double heat_capacity(const DevThermo &t, double T0, int n) {
+    const double Ri = t.Ri[n];
+    double T = fmax(T0, 200.0);
+    if (t.nasa) {
+        double _T = 1.0 / T;
+        int rg = nasa_range(T);
+        if (rg < 0) return 0.0;
+        const double *a = t.Hia + n * 21 + rg;
+        return Ri * ((a[0] * _T + a[3]) * _T + a[6] + (a[9] + (a[12] + (a[15] + a[18] * T) * T) * T) * T);
+    }
+    int rg = (T > 1000.0) ? 0 : 1;
+    const double *a = t.Hia + n * 21 + rg;
+    return Ri * (a[0] + (a[3] + (a[6] + (a[9] + a[12] * T) * T) * T) * T);
+}
+// get_Enthalpy_NASA :62-80 / get_Enthalpy_JANAF :86-102
+__device__ __forceinline__ double enthalpy(const DevThermo &t, double T0, int n) {
+    const double Ri = t.Ri[n];
+    double TT = T0, T = fmax(T0, 200.0), hi = 0.0;
+    if (t.nasa) {
+        int rg = nasa_range(T);
+        if (rg >= 0) {
+            const double *a = t.Hia + n * 21 + rg;
+            const double b0 = t.Hib[n * 6 + rg];
+            hi = Ri * (-a[0] / T + a[3] * log(T) +
+                       (a[6] + (0.5 * a[9] + (a[12] * kOT + (0.25 * a[15] + 0.2 * a[18] * T) * T) * T) * T) * T + b0);
+        }
+    } else {
+        int rg = (T > 1000.0) ? 0 : 1;
+        const double *a = t.Hia + n * 21 + rg;
+        hi = Ri * (T * (a[0] + T * (a[3] * 0.5 + T * (a[6] * kOT + T * (a[9] * 0.25 + a[12] * T * 0.2)))) + a[15]);
+    }
+    if (TT < 200.0) hi += heat_capacity(t, 200.0, n) * (TT - 200.0);
+    return hi;
+}
+
+// Mixture functions, src/solver_Ini/Mixing_device.h
+template <int NS>
+__device__ __forceinline__ double mix_R(const DevThermo &t, const double *yi) {  // get_CopR :49-56
+    double s = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; n++) s += yi[n] * t._Wi[n];
+    return s * kRu;
+}
+template <int NS>
+__device__ __forceinline__ double mix_W_inv(const DevThermo &t, const double *yi) {
+    double s = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; n++) s += yi[n] * t._Wi[n];
+    return s;
+}
+template <int NS>
+__device__ __forceinline__ double mix_Cp(const DevThermo &t, const double *yi, double T) {  // get_CopCp :61-68
+    double s = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; n++) s += yi[n] * heat_capacity(t, T, n);
+    return s;
+}
+template <int NS>
+__device__ __forceinline__ double mix_h(const DevThermo &t, const double *yi, double T) {  // get_Coph :131-140
+    double h = 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; n++) h += enthalpy(t, T, n) * yi[n];
+    return h;
+}
+// get_T :171-193 (Newton on h(T) - R T - e, clamped steps, <= 100 iterations, |dT| <= 1e-6 K)
+template <int NS>
+__device__ double newton_T(const DevThermo &t, const double *yi, double e, double T0) {
+    double T = T0;
+    const double Rm = mix_R<NS>(t, yi);
+    for (int it = 1; it < 101; it++) {
+        double h = 0.0, Cp = 0.0;
+#pragma unroll
+        for (int n = 0; n < NS; n++) {
+            h += enthalpy(t, T, n) * yi[n];
+            Cp += yi[n] * heat_capacity(t, T, n);
+        }
+        double f = h - Rm * T - e;
+        double df_ = Cp - Rm;
+        double df = fmin(f / (df_ + 1.0e-30), 1e-3 * T);
+        df = fmax(df, -1e-2 * T);
+        T = T - df;
+        if (fabs(df) <= 1.0e-6) break;
+    }
+    return T;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Eigensystem entries (Eigen_matrix.hpp OROC form). Kinds: 0 structural zero, 1 +1, 2 -1,
+// 3 general. They depend only on (direction, E, row/column, component) and fold at compile time.
+// ---------------------------------------------------------------------------------------------
+__host__ __device__ constexpr int left_kind(int D, int E, int n, int k) {
+    if (n == 0 || n == E - 1) return 3;
+    if (n >= 1 && n <= 3) {
+        if (n == D + 1) return k == 4 ? 2 : 3;
+        // shear rows: x: n=2 (v,0,-1,0,0), n=3 (-w,0,0,1,0); y: n=1 (-u,1,..), n=3 (w,0,0,-1,0);
+        // z: n=1 (u,-1,0,0,0), n=2 (-v,0,1,0,0)
+        if (k == 0) return 3;
+        if (D == 0) return (n == 2) ? (k == 2 ? 2 : 0) : (k == 3 ? 1 : 0);
+        if (D == 1) return (n == 1) ? (k == 1 ? 1 : 0) : (k == 3 ? 2 : 0);
+        return (n == 1) ? (k == 1 ? 2 : 0) : (k == 2 ? 1 : 0);
+    }
+    // species rows n = 4..E-2: (-y_s, 0, 0, 0, 0, delta_{s})
+    if (k == 0) return 3;
+    return (k == 5 + (n - 4)) ? 1 : 0;
+}
+__host__ __device__ constexpr int right_kind(int D, int E, int n, int k) {
+    if (n == 0 || n == E - 1) return k == 0 ? 1 : 3;
+    if (n >= 1 && n <= 3) {
+        if (n == D + 1) return 3;
+        if (k == 4) return 3;
+        if (D == 0) return (n == 2) ? (k == 2 ? 2 : 0) : (k == 3 ? 1 : 0);
+        if (D == 1) return (n == 1) ? (k == 1 ? 1 : 0) : (k == 3 ? 2 : 0);
+        return (n == 1) ? (k == 1 ? 2 : 0) : (k == 2 ? 1 : 0);
+    }
+    if (k == 4) return 3;
+    return (k == 5 + (n - 4)) ? 1 : 0;
+}
+
+// Roe state of a face: MARCO_ROE (global_marco.h:26-37), c^2 and MARCO_PREEIGEN.
+template <class T, int NS>
+struct FaceStateT {
+    T _u, _v, _w, _H, _P, _rho, D, D1;
+    T c2, b1, b3, q2, _c, b2, _c1;
+    T z[NS > 1 ? NS - 1 : 1];
+    T _yi[NS];
+};
+template <int NS>
+using FaceState = FaceStateT<double, NS>;
+
+// General entry (kind 3) of row n of L for direction D, component k (RoeAverageLeft_*).
+template <int D, int E, class T, int NS>
+__device__ __forceinline__ T left_val(const FaceStateT<T, NS> &F, int n, int k) {
+    const T b1 = F.b1, b2 = F.b2, b3 = F.b3, _c1 = F._c1;
+    const T vel[3] = {F._u, F._v, F._w};
+    const T un = vel[D];
+    const T h = T(0.5);
+    if (n == 0) {
+        if (k == 0) return h * (b2 + un * _c1 + b3);
+        if (k >= 1 && k <= 3) return (k - 1 == D) ? -h * (b1 * vel[k - 1] + _c1) : -h * (b1 * vel[k - 1]);
+        if (k == 4) return h * b1;
+        return -h * b1 * F.z[k - 5];
+    }
+    if (n == E - 1) {
+        if (k == 0) return h * (b2 - un * _c1 + b3);
+        if (k >= 1 && k <= 3) return (k - 1 == D) ? h * (-b1 * vel[k - 1] + _c1) : h * (-b1 * vel[k - 1]);
+        if (k == 4) return h * b1;
+        return -h * b1 * F.z[k - 5];
+    }
+    if (n >= 1 && n <= 3) {
+        if (n == D + 1) {
+            if (k == 0) return (T(1.0) - b2 - b3) / b1;
+            if (k >= 1 && k <= 3) return vel[k - 1];
+            return F.z[k - 5];
+        }
+        // column 0 of the shear rows
+        if (D == 0) return n == 2 ? F._v : -F._w;
+        if (D == 1) return n == 1 ? -F._u : F._w;
+        return n == 1 ? F._u : -F._v;
+    }
+    return -F._yi[n - 4];
+}
+
+// General entry (kind 3) of column n of R for direction D, component k (RoeAverageRight_*).
+template <int D, int E, class T, int NS>
+__device__ __forceinline__ T right_val(const FaceStateT<T, NS> &F, int n, int k) {
+    const T vel[3] = {F._u, F._v, F._w};
+    const T un = vel[D], _c = F._c, _H = F._H, b1 = F.b1;
+    if (n == 0 || n == E - 1) {
+        const bool m = n == 0;
+        if (k >= 1 && k <= 3) return (k - 1 == D) ? (m ? vel[k - 1] - _c : vel[k - 1] + _c) : vel[k - 1];
+        if (k == 4) return m ? _H - un * _c : _H + un * _c;
+        return F._yi[k - 5];
+    }
+    if (n >= 1 && n <= 3) {
+        if (n == D + 1) {
+            if (k == 0) return b1;
+            if (k >= 1 && k <= 3) return vel[k - 1] * b1;
+            if (k == 4) return _H * b1 - T(1.0);
+            return b1 * F._yi[k - 5];
+        }
+        if (D == 0) return n == 2 ? -F._v : F._w;
+        if (D == 1) return n == 1 ? F._u : -F._w;
+        return n == 1 ? -F._u : F._v;
+    }
+    return F.z[n - 4];
+}
+
+// ---------------------------------------------------------------------------------------------
+// WENO schemes
+// ---------------------------------------------------------------------------------------------
+// weno5old_BODY, WENO5s_schemes.hpp:12-69 (double branch; product-form weights)
+__device__ __forceinline__ double weno5_body(double v1, double v2, double v3, double v4, double v5) {
+    double a1, a2, a3;
+    a1 = v1 - 2.0 * v2 + v3;
+    double s1 = 13.0 * a1 * a1;
+    a1 = v1 - 4.0 * v2 + 3.0 * v3;
+    s1 += 3.0 * a1 * a1;
+    a1 = v2 - 2.0 * v3 + v4;
+    double s2 = 13.0 * a1 * a1;
+    a1 = v2 - v4;
+    s2 += 3.0 * a1 * a1;
+    a1 = v3 - 2.0 * v4 + v5;
+    double s3 = 13.0 * a1 * a1;
+    a1 = 3.0 * v3 - 4.0 * v4 + v5;
+    s3 += 3.0 * a1 * a1;
+    s1 += 1.0E-6, s2 += 1.0E-6, s3 += 1.0E-6;
+    a1 = 0.1 * s2 * s2 * s3 * s3;
+    a2 = 0.6 * s1 * s1 * s3 * s3;
+    a3 = 0.3 * s1 * s1 * s2 * s2;
+    double tw1 = 1.0 / (a1 + a2 + a3);
+    a1 = a1 * tw1, a2 = a2 * tw1, a3 = a3 * tw1;
+    s1 = a1 * (2.0 * v1 - 7.0 * v2 + 11.0 * v3);
+    s2 = a2 * (-v2 + 5.0 * v3 + 2.0 * v4);
+    s3 = a3 * (2.0 * v3 + 5.0 * v4 - v5);
+    return (s1 + s2 + s3);
+}
+// FP32 form: the same candidates and smoothness indicators; the weights use the division form
+// d_k / s_k^2 (equal to the product form) so that s^4 cannot overflow single precision.
+__device__ __forceinline__ float weno5_body(float v1, float v2, float v3, float v4, float v5) {
+    float a1;
+    a1 = v1 - 2.0f * v2 + v3;
+    float s1 = 13.0f * a1 * a1;
+    a1 = v1 - 4.0f * v2 + 3.0f * v3;
+    s1 += 3.0f * a1 * a1;
+    a1 = v2 - 2.0f * v3 + v4;
+    float s2 = 13.0f * a1 * a1;
+    a1 = v2 - v4;
+    s2 += 3.0f * a1 * a1;
+    a1 = v3 - 2.0f * v4 + v5;
+    float s3 = 13.0f * a1 * a1;
+    a1 = 3.0f * v3 - 4.0f * v4 + v5;
+    s3 += 3.0f * a1 * a1;
+    s1 += 1.0E-6f, s2 += 1.0E-6f, s3 += 1.0E-6f;
+    float w1 = 0.1f / (s1 * s1), w2 = 0.6f / (s2 * s2), w3 = 0.3f / (s3 * s3);
+    float tw = 1.0f / (w1 + w2 + w3);
+    return tw * (w1 * (2.0f * v1 - 7.0f * v2 + 11.0f * v3) + w2 * (-v2 + 5.0f * v3 + 2.0f * v4) +
+                 w3 * (2.0f * v3 + 5.0f * v4 - v5));
+}
+// weno5old_GPU :71-95 on 8-point stencil arrays indexed m+3
+template <class T>
+__device__ __forceinline__ T weno5(const T *pp, const T *mm) {
+    T temf = weno5_body(pp[1], pp[2], pp[3], pp[4], pp[5]);
+    T temm = weno5_body(mm[6], mm[5], mm[4], mm[3], mm[2]);
+    return (temf + temm) * T(kSix);
+}
+// weno7_P / weno7_M body, WENO7s_schemes.hpp:8-128
+template <class T>
+__device__ __forceinline__ T weno7_body(T v1, T v2, T v3, T v4, T v5, T v6, T v7) {
+    const T ep = T(1.0e-7);
+    const T C0 = T(1.0 / 35.0), C1 = T(12.0 / 35.0), C2 = T(18.0 / 35.0), C3 = T(4.0 / 35.0);
+    T S10 = T(-2.0 / 6.0) * v1 + T(9.0 / 6.0) * v2 - T(18.0 / 6.0) * v3 + T(11.0 / 6.0) * v4;
+    T S11 = T(1.0 / 6.0) * v2 - v3 + T(3.0 / 6.0) * v4 + T(2.0 / 6.0) * v5;
+    T S12 = T(-2.0 / 6.0) * v3 - T(3.0 / 6.0) * v4 + v5 - T(1.0 / 6.0) * v6;
+    T S13 = T(-11.0 / 6.0) * v4 + T(18.0 / 6.0) * v5 - T(9.0 / 6.0) * v6 + T(2.0 / 6.0) * v7;
+    T S20 = -v1 + T(4.0) * v2 - T(5.0) * v3 + T(2.0) * v4;
+    T S21 = v3 - T(2.0) * v4 + v5;
+    T S22 = v4 - T(2.0) * v5 + v6;
+    T S23 = T(2.0) * v4 - T(5.0) * v5 + T(4.0) * v6 - v7;
+    T S30 = -v1 + T(3.0) * v2 - T(3.0) * v3 + v4;
+    T S31 = -v2 + T(3.0) * v3 - T(3.0) * v4 + v5;
+    T S32 = -v3 + T(3.0) * v4 - T(3.0) * v5 + v6;
+    T S33 = -v4 + T(3.0) * v5 - T(3.0) * v6 + v7;
+    const T k13 = T(13.0 / 12.0), k1043 = T(1043.0 / 960.0), k112 = T(1.0 / 12.0);
+    T S0 = S10 * S10 + k13 * S20 * S20 + k1043 * S30 * S30 + k112 * S10 * S30;
+    T S1 = S11 * S11 + k13 * S21 * S21 + k1043 * S31 * S31 + k112 * S11 * S31;
+    T S2 = S12 * S12 + k13 * S22 * S22 + k1043 * S32 * S32 + k112 * S12 * S32;
+    T S3 = S13 * S13 + k13 * S23 * S23 + k1043 * S33 * S33 + k112 * S13 * S33;
+    T a0 = C0 / ((ep + S0) * (ep + S0));
+    T a1 = C1 / ((ep + S1) * (ep + S1));
+    T a2 = C2 / ((ep + S2) * (ep + S2));
+    T a3 = C3 / ((ep + S3) * (ep + S3));
+    T sum = a0 + a1 + a2 + a3;
+    T W0 = a0 / sum, W1 = a1 / sum, W2 = a2 / sum, W3 = a3 / sum;
+    T q0 = T(-3.0 / 12.0) * v1 + T(13.0 / 12.0) * v2 - T(23.0 / 12.0) * v3 + T(25.0 / 12.0) * v4;
+    T q1 = T(1.0 / 12.0) * v2 - T(5.0 / 12.0) * v3 + T(13.0 / 12.0) * v4 + T(3.0 / 12.0) * v5;
+    T q2 = T(-1.0 / 12.0) * v3 + T(7.0 / 12.0) * v4 + T(7.0 / 12.0) * v5 - T(1.0 / 12.0) * v6;
+    T q3 = T(3.0 / 12.0) * v4 + T(13.0 / 12.0) * v5 - T(5.0 / 12.0) * v6 + T(1.0 / 12.0) * v7;
+    return W0 * q0 + W1 * q1 + W2 * q2 + W3 * q3;
+}
+template <class T>
+__device__ __forceinline__ T weno7(const T *pp, const T *mm) {
+    T tp = weno7_body(pp[0], pp[1], pp[2], pp[3], pp[4], pp[5], pp[6]);
+    T tm = weno7_body(mm[7], mm[6], mm[5], mm[4], mm[3], mm[2], mm[1]);
+    return tp + tm;
+}
+
+// atomic max of a non-negative double through its bit pattern (monotone for x >= 0)
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, double v) {
+    if (!(v >= 0.0)) v = __longlong_as_double(0x7ff0000000000000LL);  // NaN -> +inf (flags the step)
+    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+}  // namespace xfg

@@ -1,0 +1,90 @@
+// xfg_inst.cuh - launchers of the kernels for one (COP, NS); included once per instantiation unit.
+#pragma once
+
+#include "xfg_kernels.cuh"
+#include "xfg_mixed.cuh"
+#include "xfg_ops.h"
+
+namespace xfg {
+
+template <bool COP, int NS>
+struct Inst {
+    static constexpr int E = Sys<COP, NS>::E;
+
+    static void bc(const LaunchCtx &c, double *U, const double *guard) {
+        const Geo &g = c.g;
+        if (g.dimx) {
+            long long n = (long long)g.Bx * g.Ymax * g.Zmax;
+            k_bc<0, E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, U, c.bc[0], c.bc[1], guard);
+        }
+        if (g.dimy) {
+            long long n = (long long)g.By * g.Xmax * g.Zmax;
+            k_bc<1, E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, U, c.bc[2], c.bc[3], guard);
+        }
+        if (g.dimz) {
+            long long n = (long long)g.Bz * g.Xmax * g.Ymax;
+            k_bc<2, E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, U, c.bc[4], c.bc[5], guard);
+        }
+    }
+    static void states(const LaunchCtx &c, double *UI, int want_lam, int guard) {
+        const long long n = c.g.ncell();
+        if (c.precision == XFG_MIXED)
+            k_states_mixed<COP, NS><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, c.th, UI, c.ghost, want_lam, guard);
+        else
+            k_states<COP, NS><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, c.th, UI, c.ghost, want_lam, guard);
+    }
+    template <int D, int ORDER>
+    static void faces_d(const LaunchCtx &c, const double *UI, int guard) {
+        const Geo &g = c.g;
+        long long n = (long long)(g.Xi + (D == 0)) * (g.Yi + (D == 1)) * (g.Zi + (D == 2));
+        const double *glf = c.glf ? c.glf + 3 * D : nullptr;
+        if (c.precision == XFG_MIXED)
+            k_faces_mixed<D, COP, NS, ORDER><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, c.artificial, glf, guard);
+        else
+            k_faces<D, COP, NS, ORDER><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, UI, c.artificial, glf, guard);
+    }
+    template <int ORDER>
+    static void faces(const LaunchCtx &c, int d, const double *UI, int guard) {
+        if (d == 0) faces_d<0, ORDER>(c, UI, guard);
+        else if (d == 1) faces_d<1, ORDER>(c, UI, guard);
+        else faces_d<2, ORDER>(c, UI, guard);
+    }
+    static void div_rk(const LaunchCtx &c, int flag, double dt, const double *dt_dev, int do_rk, int store_lu, int guard) {
+        const Geo &g = c.g;
+        long long n = (long long)g.Xi * g.Yi * g.Zi;
+        if (c.precision == XFG_MIXED)
+            k_div_rk_mixed<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, flag, dt, dt_dev, do_rk, store_lu, guard);
+        else
+            k_div_rk<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, flag, dt, dt_dev, do_rk, store_lu, guard);
+    }
+    static void glf(const LaunchCtx &c, unsigned long long *out, int guard) {
+        cudaMemsetAsync(out, 0, 9 * sizeof(unsigned long long), c.st);
+        k_glf<<<grid_for(c.g.ncell(), kThreads), kThreads, 0, c.st>>>(c.g, c.f, out, guard);
+    }
+
+    static void rk(const LaunchCtx &c, int flag, double dt) {
+        long long n = (long long)c.g.Xi * c.g.Yi * c.g.Zi;
+        k_rk<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, flag, dt);
+    }
+    static void estimate_nan(const LaunchCtx &c, const double *UI, int *pos) {
+        long long n = (long long)c.g.Xi * c.g.Yi * c.g.Zi;
+        k_estimate_nan<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, UI, c.f.LU, pos);
+    }
+
+    static const Ops *table(int order) {
+        static const Ops t5 = {COP ? 1 : 0, NS, 5, bc, states, faces<5>, div_rk, glf, rk, estimate_nan};
+        static const Ops t7 = {COP ? 1 : 0, NS, 7, bc, states, faces<7>, div_rk, glf, rk, estimate_nan};
+        return order == 7 ? &t7 : &t5;
+    }
+};
+
+// Registers the tables of one (COP, NS) at load time.
+template <bool COP, int NS>
+struct Registrar {
+    Registrar() {
+        register_ops(Inst<COP, NS>::table(5));
+        register_ops(Inst<COP, NS>::table(7));
+    }
+};
+
+}  // namespace xfg

@@ -1,0 +1,579 @@
+// xfg_kernels.cuh - CUDA kernels of the convective right-hand side (FP64 path).
+//
+// Stage pipeline per RK stage (the reference's kernels in brackets):
+//   k_bc          ghost fill, one launch per active direction   [FluidBCKernelX/Y/Z]
+//   k_states      rho, Y, primitives, T Newton, physical fluxes [Updaterhoyi + UpdateFuidStatesKernel]
+//                 + NaN/negativity check + GetDt wave-speed maxima (block reduce + atomicMax)
+//   k_faces<D>    characteristic WENO flux at every face of direction D
+//                 [GetLocalEigen + ReconstructFlux{X,Y,Z}], one thread per face
+//   k_div_rk      flux divergence and the SSP-RK3 stage combination, fused, with the NaN check
+//                 [UpdateFluidLU + EstimateFluidNANKernel + UpdateURK3rdKernel]
+// and once per step k_dt_step [GetDt host arithmetic + the time clip of XFLUIDS::Evolution].
+#pragma once
+
+#include "xfg_device.cuh"
+
+namespace xfg {
+
+constexpr int kThreads = 128;
+
+// error words in DevFields::err
+enum { ERR_STATE = 0, ERR_PRIM = 1, ERR_I = 2, ERR_J = 3, ERR_K = 4, ERR_NWORDS = 8 };
+
+__device__ __forceinline__ bool bad(double x) {  // NaN or Inf through the exponent bits
+    return ((__double2hiint(x) & 0x7ff00000) == 0x7ff00000);
+}
+
+__device__ __forceinline__ bool step_done(const DevFields &f) { return f.dtbuf && f.dtbuf[4] != 0.0; }
+
+// ---------------------------------------------------------------------------------------------
+// Boundary conditions, BCs_kernels.hpp:9-258 with the launch arguments of BCs_block.cpp:4-218.
+// One thread per (ghost layer, transverse cell) covering both faces of direction D.
+// ---------------------------------------------------------------------------------------------
+template <int D, int E>
+__global__ void __launch_bounds__(kThreads) k_bc(Geo g, double *__restrict__ U, int bc_lo, int bc_hi,
+                                                 const double *__restrict__ guard_dtbuf) {
+    if (guard_dtbuf && guard_dtbuf[4] != 0.0) return;
+    const int bw = D == 0 ? g.Bx : (D == 1 ? g.By : g.Bz);
+    const int inner = D == 0 ? g.Xi : (D == 1 ? g.Yi : g.Zi);
+    const int nmax = D == 0 ? g.Xmax : (D == 1 ? g.Ymax : g.Zmax);
+    // transverse extents (full, ghosts included)
+    const int ta = D == 0 ? g.Ymax : g.Xmax;
+    const int tb = D == 2 ? g.Ymax : g.Zmax;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long total = (long long)bw * ta * tb;
+    if (t >= total) return;
+    int gl = (int)(t % bw);
+    long long r = t / bw;
+    int a = (int)(r % ta), b = (int)(r / ta);
+    const long long P = g.pitch;
+    auto cell = [&](int cn) -> long long {
+        int i = D == 0 ? cn : a;
+        int j = D == 0 ? a : (D == 1 ? cn : b);
+        int k = D == 2 ? cn : b;
+        return (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    };
+    for (int side = 0; side < 2; side++) {
+        const int BC = side == 0 ? bc_lo : bc_hi;
+        const int cn = side == 0 ? gl : gl + nmax - bw;
+        const int mirror_offset = side == 0 ? 0 : inner;
+        const int index_inner = side == 0 ? bw : nmax - bw - 1;
+        const int sign = side == 0 ? 1 : -1;
+        const long long id = cell(cn);
+        long long src;
+        switch (BC) {
+        case XFG_SYMMETRY:
+            src = cell(2 * (bw + mirror_offset) - 1 - cn);
+#pragma unroll
+            for (int n = 0; n < E; n++) U[n * P + id] = (n == 1 + D) ? -U[n * P + src] : U[n * P + src];
+            break;
+        case XFG_PERIODIC:
+            src = cell(cn + sign * inner);
+#pragma unroll
+            for (int n = 0; n < E; n++) U[n * P + id] = U[n * P + src];
+            break;
+        case XFG_OUTFLOW:
+            src = cell(index_inner);
+#pragma unroll
+            for (int n = 0; n < E; n++) U[n * P + id] = U[n * P + src];
+            break;
+        case XFG_NSLIPWALL:
+        case XFG_VISCWALL:
+        case XFG_SLIPWALL:
+            src = cell(2 * (bw + mirror_offset) - 1 - cn);
+#pragma unroll
+            for (int n = 0; n < E; n++) U[n * P + id] = (n >= 1 && n <= 3) ? -U[n * P + src] : U[n * P + src];
+            break;
+        default:
+            break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Primitive recovery and physical fluxes on all cells: Getrhoyi (Update_device.hpp:7-29),
+// GetStates (:33-54), GetPhysFlux (:81-110); the inner-cell checks of EstimateYiKernel /
+// EstimatePrimitiveVarKernel (Estimate_kernels.hpp); the GetDt maxima of |u_d| + sqrt(1.4 p/rho)
+// over all cells (GlobalDt_block.hpp:31-66) when want_lam.
+// ---------------------------------------------------------------------------------------------
+template <bool COP, int NS>
+__global__ void __launch_bounds__(kThreads) k_states(Geo g, DevFields f, DevThermo th, double *__restrict__ UI,
+                                                     int ghost, int want_lam, int guard) {
+    using S = Sys<COP, NS>;
+    constexpr int E = S::E, NCOP = S::NCOP;
+    if (guard && step_done(f)) return;
+    const long long P = g.pitch, N = g.ncell();
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double lamx = 0.0, lamy = 0.0, lamz = 0.0;
+    if (id < N) {
+        double U[E];
+#pragma unroll
+        for (int n = 0; n < E; n++) U[n] = UI[n * P + id];
+        const double rho = U[0];
+        const double rho1 = 1.0 / rho;
+        double yi[NS];
+        if (COP) {
+            if (ghost) {
+                yi[NCOP] = 0.0;
+                double sum = 0.0;
+#pragma unroll
+                for (int s = 0; s < NCOP; s++) yi[s] = U[s + 5] * rho1, sum += yi[s];
+                sum = 1.0 / sum;
+#pragma unroll
+                for (int s = 0; s < NCOP; s++) {
+                    yi[s] *= sum;
+                    U[s + 5] = rho * yi[s];
+                    UI[(s + 5) * P + id] = U[s + 5];
+                }
+            } else {
+                yi[NCOP] = 1.0;
+#pragma unroll
+                for (int s = 0; s < NCOP; s++) yi[s] = U[s + 5] * rho1, yi[NCOP] += -yi[s];
+            }
+        }
+        const double u = U[1] * rho1, v = U[2] * rho1, w = U[3] * rho1;
+        const double tme = U[4] * rho1 - 0.5 * (u * u + v * v + w * w);
+        double p, gamma, T = 0.0, Cp = 0.0, Rm = 0.0;
+        if (COP) {
+            Rm = mix_R<NS>(th, yi);
+            T = newton_T<NS>(th, yi, tme, f.T[id]);
+            p = rho * Rm * T;
+            Cp = mix_Cp<NS>(th, yi, T);
+            const double CopW = 1.0 / mix_W_inv<NS>(th, yi);
+            const double gm = Cp / (Cp - kRu / CopW);
+            gamma = gm > 1.0 ? gm : -1.0;
+        } else {
+            gamma = th.ncop_gamma;
+            p = (th.ncop_gamma - 1.0) * rho * tme;
+        }
+        const double H = (U[4] + p) * rho1;
+        const double c = sqrt(gamma * p * rho1);
+        f.rho[id] = rho, f.u[id] = u, f.v[id] = v, f.w[id] = w, f.p[id] = p, f.H[id] = H, f.c[id] = c;
+        f.e[id] = tme, f.gamma[id] = gamma;
+        if (COP) {
+            f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
+#pragma unroll
+            for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s];
+        }
+        // physical fluxes of the active directions
+        const double Ep = U[4] + p;
+        if (g.dimx) {
+            double *F = f.F[0];
+            F[0 * P + id] = U[1];
+            F[1 * P + id] = U[1] * u + p;
+            F[2 * P + id] = U[1] * v;
+            F[3 * P + id] = U[1] * w;
+            F[4 * P + id] = Ep * u;
+#pragma unroll
+            for (int n = 5; n < E; n++) F[n * P + id] = U[1] * yi[n - 5];
+        }
+        if (g.dimy) {
+            double *F = f.F[1];
+            F[0 * P + id] = U[2];
+            F[1 * P + id] = U[2] * u;
+            F[2 * P + id] = U[2] * v + p;
+            F[3 * P + id] = U[2] * w;
+            F[4 * P + id] = Ep * v;
+#pragma unroll
+            for (int n = 5; n < E; n++) F[n * P + id] = U[2] * yi[n - 5];
+        }
+        if (g.dimz) {
+            double *F = f.F[2];
+            F[0 * P + id] = U[3];
+            F[1 * P + id] = U[3] * u;
+            F[2 * P + id] = U[3] * v;
+            F[3 * P + id] = U[3] * w + p;
+            F[4 * P + id] = Ep * w;
+#pragma unroll
+            for (int n = 5; n < E; n++) F[n * P + id] = U[3] * yi[n - 5];
+        }
+        // inner-cell checks (rho, p, T negative / NaN / Inf; Y NaN / Inf)
+        const int i = (int)(id % g.Xmax);
+        const long long r = id / g.Xmax;
+        const int j = (int)(r % g.Ymax), k = (int)(r / g.Ymax);
+        const bool inner = i >= g.Bx && i < g.Xmax - g.Bx && j >= g.By && j < g.Ymax - g.By && k >= g.Bz && k < g.Zmax - g.Bz;
+        if (inner) {
+            bool e1 = rho < 0.0 || bad(rho) || p < 0.0 || bad(p) || (COP && (T < 0.0 || bad(T)));
+            if (COP)
+#pragma unroll
+                for (int s = 0; s < NS; s++) e1 = e1 || bad(yi[s]);
+            if (e1) {
+                atomicOr(&f.err[ERR_PRIM], 1);
+                f.err[ERR_I] = i, f.err[ERR_J] = j, f.err[ERR_K] = k;
+            }
+        }
+        if (want_lam) {
+            const double c_local = sqrt(1.4 * p / rho);
+            lamx = fabs(u) + c_local, lamy = fabs(v) + c_local, lamz = fabs(w) + c_local;
+            if (!(lamx >= 0.0)) lamx = __longlong_as_double(0x7ff0000000000000LL);
+            if (!(lamy >= 0.0)) lamy = __longlong_as_double(0x7ff0000000000000LL);
+            if (!(lamz >= 0.0)) lamz = __longlong_as_double(0x7ff0000000000000LL);
+        }
+    }
+    if (want_lam) {  // warp then block max, one atomic per block and direction
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lamx = fmax(lamx, __shfl_xor_sync(0xffffffffu, lamx, o));
+            lamy = fmax(lamy, __shfl_xor_sync(0xffffffffu, lamy, o));
+            lamz = fmax(lamz, __shfl_xor_sync(0xffffffffu, lamz, o));
+        }
+        __shared__ double red[3][kThreads / 32];
+        const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0) red[0][wid] = lamx, red[1][wid] = lamy, red[2][wid] = lamz;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double a = red[0][0], b = red[1][0], c = red[2][0];
+            for (int q = 1; q < kThreads / 32; q++) a = fmax(a, red[0][q]), b = fmax(b, red[1][q]), c = fmax(c, red[2][q]);
+            if (g.dimx) atomic_max_nonneg(&f.lam[0], a);
+            if (g.dimy) atomic_max_nonneg(&f.lam[1], b);
+            if (g.dimz) atomic_max_nonneg(&f.lam[2], c);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Global LF maxima eigen_block[d][n] = max over all cells |lambda_n| (ConVenction_block.hpp:115-215)
+// for WENO5 (u_d - c, u_d, u_d + c); WENO7 local eigenvalues are zero. Written as bit patterns
+// into glf[d*3 + {0,1,2}].
+// ---------------------------------------------------------------------------------------------
+static __global__ void __launch_bounds__(kThreads) k_glf(Geo g, DevFields f, unsigned long long *glf, int guard) {
+    if (guard && step_done(f)) return;
+    const long long N = g.ncell();
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double m[9];
+    for (int q = 0; q < 9; q++) m[q] = 0.0;
+    if (id < N) {
+        const double c = f.c[id];
+        const double vel[3] = {f.u[id], f.v[id], f.w[id]};
+        for (int d = 0; d < 3; d++) {
+            m[3 * d + 0] = fabs(vel[d] - c);
+            m[3 * d + 1] = fabs(vel[d]);
+            m[3 * d + 2] = fabs(vel[d] + c);
+        }
+    }
+    for (int q = 0; q < 9; q++) {
+        double x = m[q];
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&glf[q], x);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Characteristic WENO flux at face (i+1/2) of direction D, one thread per face:
+// ReconstructFlux{X,Y,Z} (Reconstruction_kernels.hpp:8-199) with MARCO_ROE, MARCO_NOCOPC2 /
+// MARCO_COPC2 (ReconstructSoundSpeed, Utils_device.hpp:102-140), RoeAverageLeft/Right
+// (Eigen_matrix.hpp:7-455) and MARCO_FLUXWALL_WENO5 / _WENO7 (Eigen_callback.h:127-230).
+// Local eigenvalues (GetLocalEigen) are formed on the fly from u_d and c of the window cells.
+// ---------------------------------------------------------------------------------------------
+template <bool COP, int NS>
+__device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, const DevThermo &th, long long l,
+                                           long long r, FaceState<NS> &F, double &Gamma0) {
+    const long long P = g.pitch;
+    const double rl = f.rho[l], rr = f.rho[r];
+    const double ul = f.u[l], ur = f.u[r], vl = f.v[l], vr = f.v[r], wl = f.w[l], wr = f.w[r];
+    const double Hl = f.H[l], Hr = f.H[r], pl = f.p[l], pr = f.p[r];
+    const double D = sqrt(rr / rl);
+    const double D1 = 1.0 / (D + 1.0);
+    F.D = D, F.D1 = D1;
+    F._u = (ul + D * ur) * D1;
+    F._v = (vl + D * vr) * D1;
+    F._w = (wl + D * wr) * D1;
+    F._H = (Hl + D * Hr) * D1;
+    F._P = (pl + D * pr) * D1;
+    F._rho = sqrt(rr * rl);
+    if (!COP) {
+        Gamma0 = th.ncop_gamma;
+        F.c2 = Gamma0 * F._P / F._rho;
+        F.b1 = (Gamma0 - 1.0) / F.c2;
+        F.b3 = 0.0;
+        F._yi[0] = 1.0;
+    } else {
+        constexpr int NCOP = NS - 1;
+        double yl[NS], yr[NS], hl[NS], hr[NS];
+        const double Tl = f.T[l], Tr = f.T[r];
+#pragma unroll
+        for (int n = 0; n < NS; n++) {
+            yl[n] = f.y[n * P + l];
+            yr[n] = f.y[n * P + r];
+            hl[n] = enthalpy(th, Tl, n);
+            hr[n] = enthalpy(th, Tr, n);
+            F._yi[n] = (yl[n] + D * yr[n]) * D1;
+        }
+        const double Cpl = mix_Cp<NS>(th, yl, Tl), Cpr = mix_Cp<NS>(th, yr, Tr);
+        const double wl_ = mix_W_inv<NS>(th, yl), wr_ = mix_W_inv<NS>(th, yr);
+        const double gl = Cpl / (Cpl - kRu * wl_), gr = Cpr / (Cpr - kRu * wr_);  // get_CopGamma(yi, T)
+        Gamma0 = (gl + D * gr) * D1;
+        const double q2l = ul * ul + vl * vl + wl * wl, q2r = ur * ur + vr * vr + wr * wr;
+        const double Rl = wl_ * kRu, Rr = wr_ * kRu;
+        const double el = Hl - 0.5 * q2l - pl / rl, er = Hr - 0.5 * q2r - pr / rr;
+        const double RN = th.Ri[NCOP];
+        auto dpdrho = [&](double hN, double q2, double Cp, double Rm, double T, double gm) {
+            double RNT = RN * T;
+            return (gm - 1.0) * (0.5 * q2 - hN + Cp * RNT / Rm);
+        };
+        const double _dpdrho = (dpdrho(hl[NCOP], q2l, Cpl, Rl, Tl, gl) + D * dpdrho(hr[NCOP], q2r, Cpr, Rr, Tr, gr)) * D1;
+        double dpdrhoi[NCOP > 0 ? NCOP : 1], drhoi[NCOP > 0 ? NCOP : 1];
+#pragma unroll
+        for (int n = 0; n < NCOP; n++) {
+            const double Rin_RN = th.Ri[n] - RN;
+            const double a = (gl - 1.0) * ((-hl[n] + hl[NCOP]) + Cpl * Rin_RN * Tl / Rl);
+            const double b = (gr - 1.0) * ((-hr[n] + hr[NCOP]) + Cpr * Rin_RN * Tr / Rr);
+            dpdrhoi[n] = (a + D * b) * D1;
+            drhoi[n] = rr * yr[n] - rl * yl[n];
+        }
+        const double _prho = (pl / rl + D * (pr / rr)) * D1 +
+                             0.5 * D * D1 * D1 * ((ur - ul) * (ur - ul) + (vr - vl) * (vr - vl) + (wr - wl) * (wr - wl));
+        const double _dpdE = ((gl - 1.0) + D * (gr - 1.0)) * D1;
+        const double _dpde = ((gl - 1.0) * rl + D * ((gr - 1.0) * rr)) * D1;
+        const double dp = pr - pl, drho = rr - rl, de = er - el;
+        double S1 = 0.0, S2 = 0.0, SY = 0.0;
+#pragma unroll
+        for (int n = 0; n < NCOP; n++) {
+            S1 += dpdrhoi[n] * drhoi[n];
+            S2 += dpdrhoi[n] * drhoi[n] * dpdrhoi[n] * drhoi[n];
+        }
+        const double temp1 = dp - (_dpdrho * drho + _dpde * de + S1);
+        const double temp = temp1 / (_dpdrho * _dpdrho * drho * drho + _dpde * de * _dpde * de + S2 + 1e-19);
+#pragma unroll
+        for (int n = 0; n < NCOP; n++) SY += F._yi[n] * dpdrhoi[n];
+        const double _dpdE_new = _dpdE + _dpdE * _dpdE * de * F._rho * temp;
+        const double _dpdrho_new = _dpdrho + _dpdrho * _dpdrho * drho * temp;
+        const double csqr = _dpdrho_new + _dpdE_new * _prho + SY;
+        F.b1 = _dpdE_new / csqr;
+        double b3 = 0.0;
+#pragma unroll
+        for (int n = 0; n < NCOP; n++) {
+            const double dn = dpdrhoi[n] + dpdrhoi[n] * dpdrhoi[n] * drhoi[n] * temp;
+            F.z[n] = -dn / _dpdE_new;
+            b3 += F._yi[n] * F.z[n];
+        }
+        F.b3 = b3 * F.b1;
+        const double c2w = (0.0 < csqr) ? 0.0 : 1.0;
+        F.c2 = Gamma0 * F._P * F._rho * c2w + (1.0 - c2w) * csqr;
+    }
+    F.q2 = F._u * F._u + F._v * F._v + F._w * F._w;
+    F._c = sqrt(F.c2);
+    F.b2 = 1.0 + F.b1 * F.q2 - F.b1 * F._H;
+    F._c1 = 1.0 / F._c;
+}
+
+// Projection of the E components of cell q onto row n of L (kinds fold at compile time).
+template <int D, int E>
+__device__ __forceinline__ double project(const double *lrow, int n, const double *__restrict__ A, long long P,
+                                          long long q) {
+    double acc = 0.0;
+    bool first = true;
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+        const int kind = left_kind(D, E, n, k);
+        if (kind == 0) continue;
+        const double x = __ldg(A + k * P + q);
+        double t = kind == 1 ? x : (kind == 2 ? -x : x * lrow[k]);
+        acc = first ? t : acc + t;
+        first = false;
+    }
+    return acc;
+}
+
+template <int D, bool COP, int NS, int ORDER>
+__global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevThermo th, const double *__restrict__ UI,
+                                                    int artificial, const double *__restrict__ glf_d, int guard) {
+    using S = Sys<COP, NS>;
+    constexpr int E = S::E;
+    if (guard && step_done(f)) return;
+    const long long P = g.pitch;
+    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nfx * nfy * nfz) return;
+    const int i = (int)(t % nfx) + g.Bx - (D == 0 ? 1 : 0);
+    const long long r = t / nfx;
+    const int j = (int)(r % nfy) + g.By - (D == 1 ? 1 : 0);
+    const int k = (int)(r / nfy) + g.Bz - (D == 2 ? 1 : 0);
+    const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
+    const long long idl = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    const long long idr = idl + stride;
+
+    FaceState<NS> F;
+    double Gamma0;
+    face_state<COP, NS>(g, f, th, idl, idr, F, Gamma0);
+    const double un = D == 0 ? F._u : (D == 1 ? F._v : F._w);
+    const double *__restrict__ Fl = f.F[D];
+    const double *__restrict__ vd = D == 0 ? f.u : (D == 1 ? f.v : f.w);
+
+    // LLF window maxima of |u_d - c|, |u_d|, |u_d + c| over m = -2..3 (WENO5)
+    double lm0 = 0.0, lm1 = 0.0, lm2 = 0.0;
+    if (ORDER == 5 && artificial == XFG_LLF) {
+#pragma unroll
+        for (int m = -2; m <= 3; m++) {
+            const long long q = idl + m * stride;
+            const double ud = __ldg(vd + q), cc = __ldg(f.c + q);
+            lm0 = fmax(lm0, fabs(ud - cc));
+            lm1 = fmax(lm1, fabs(ud));
+            lm2 = fmax(lm2, fabs(ud + cc));
+        }
+    }
+    constexpr int M0 = ORDER == 7 ? -3 : -2, M1 = ORDER == 7 ? 4 : 3;
+    double acc[E];
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        const double ev = n == 0 ? fabs(un - F._c) : (n == E - 1 ? fabs(un + F._c) : fabs(un));
+        double av;
+        if (artificial == XFG_ROE || ORDER == 7) {
+            av = ev;  // WENO7: local eigenvalues are zero, so LLF reduces to |lambda_n| of the Roe state
+            if (ORDER == 7 && artificial == XFG_GLF) av = 0.0;
+        } else if (artificial == XFG_LLF) {
+            av = n == 0 ? lm0 : (n == E - 1 ? lm2 : lm1);
+        } else {
+            av = glf_d[n == 0 ? 0 : (n == E - 1 ? 2 : 1)];
+        }
+        double lrow[E];
+#pragma unroll
+        for (int kk = 0; kk < E; kk++) lrow[kk] = left_kind(D, E, n, kk) == 3 ? left_val<D, E>(F, n, kk) : 0.0;
+        double pp[8], mm[8];
+#pragma unroll
+        for (int m = M0; m <= M1; m++) {
+            const long long q = idl + m * stride;
+            const double uf = project<D, E>(lrow, n, UI, P, q);
+            const double ff = project<D, E>(lrow, n, Fl, P, q);
+            pp[m + 3] = 0.5 * (ff + av * uf);
+            mm[m + 3] = 0.5 * (ff - av * uf);
+        }
+        const double fl = ORDER == 7 ? weno7(pp, mm) : weno5(pp, mm);
+#pragma unroll
+        for (int kk = 0; kk < E; kk++) {
+            const int kind = right_kind(D, E, n, kk);
+            if (kind == 0) continue;
+            const double tv = kind == 1 ? fl : (kind == 2 ? -fl : fl * right_val<D, E>(F, n, kk));
+            acc[kk] = (n == 0) ? tv : acc[kk] + tv;  // column 0 of R has no structural zero
+        }
+    }
+    double *Fw = f.Fw[D];
+#pragma unroll
+    for (int n = 0; n < E; n++) Fw[n * P + idl] = acc[n];
+}
+
+// ---------------------------------------------------------------------------------------------
+// Flux divergence (UpdateFluidLU, Reconstruction_kernels.hpp:201-234) fused with the SSP-RK3
+// stage (UpdateURK3rdKernel, Update_kernels.hpp:64-94) and the NaN / Inf / negative density check
+// of EstimateFluidNANKernel (src/Fluids.cpp:43-86), on inner cells. store_lu keeps LU in memory.
+// dt_dev != nullptr reads dt from the device (graph replay), else dt is the argument.
+// ---------------------------------------------------------------------------------------------
+template <int E>
+__global__ void __launch_bounds__(kThreads) k_div_rk(Geo g, DevFields f, int flag, double dt_arg,
+                                                     const double *__restrict__ dt_dev, int do_rk, int store_lu,
+                                                     int guard) {
+    if (guard && step_done(f)) return;
+    const long long P = g.pitch;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
+    const int i = (int)(t % g.Xi) + g.Bx;
+    const long long r = t / g.Xi;
+    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    const long long sy = g.Xmax, sz = (long long)g.Xmax * g.Ymax;
+    const double dt = dt_dev ? dt_dev[0] : dt_arg;
+    int code = 0;
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        double LU0 = 0.0;
+        bool first = true;
+        if (g.dimx) { double tt = (f.Fw[0][n * P + id - 1] - f.Fw[0][n * P + id]) * g._dx; LU0 = tt; first = false; }
+        if (g.dimy) { double tt = (f.Fw[1][n * P + id - sy] - f.Fw[1][n * P + id]) * g._dy; LU0 = first ? tt : LU0 + tt; first = false; }
+        if (g.dimz) { double tt = (f.Fw[2][n * P + id - sz] - f.Fw[2][n * P + id]) * g._dz; LU0 = first ? tt : LU0 + tt; first = false; }
+        if (store_lu) f.LU[n * P + id] = LU0;
+        if (bad(LU0)) code = 1;
+        if (do_rk) {
+            const long long q = n * P + id;
+            double out;
+            if (flag == 1) {
+                out = f.U[q] + dt * LU0;
+                f.U1[q] = out;
+            } else if (flag == 2) {
+                out = 0.75 * f.U[q] + 0.25 * f.U1[q] + 0.25 * dt * LU0;
+                f.U1[q] = out;
+            } else {
+                out = (f.U[q] + 2.0 * f.U1[q] + 2.0 * dt * LU0) * kOT;
+                f.U[q] = out;
+            }
+            if (bad(out) || (n == 0 && out < 0.0)) code = 1;
+        }
+    }
+    if (code) {
+        atomicOr(&f.err[ERR_STATE], 1);
+        f.err[ERR_I] = i, f.err[ERR_J] = j, f.err[ERR_K] = k;
+    }
+}
+
+// SSP-RK3 stage from a stored LU (UpdateURK3rdKernel, Update_kernels.hpp:64-94), inner cells.
+template <int E>
+__global__ void __launch_bounds__(kThreads) k_rk(Geo g, DevFields f, int flag, double dt) {
+    const long long P = g.pitch;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
+    const int i = (int)(t % g.Xi) + g.Bx;
+    const long long r = t / g.Xi;
+    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        const long long q = n * P + id;
+        if (flag == 1) f.U1[q] = f.U[q] + dt * f.LU[q];
+        else if (flag == 2) f.U1[q] = 0.75 * f.U[q] + 0.25 * f.U1[q] + 0.25 * dt * f.LU[q];
+        else f.U[q] = (f.U[q] + 2.0 * f.U1[q] + 2.0 * dt * f.LU[q]) * kOT;
+    }
+}
+
+// EstimateFluidNANKernel (src/Fluids.cpp:43-86) on inner cells of UI and LU: per component
+// 10000 (negative density, component 0), 1100 / 1200 (NaN / Inf state), 21 / 22 (NaN / Inf LU),
+// accumulated over cells; pos[E+1..E+3] the (i, j, k) of a failing cell; pos[E] the flag.
+template <int E>
+__global__ void __launch_bounds__(kThreads) k_estimate_nan(Geo g, const double *__restrict__ UI,
+                                                           const double *__restrict__ LU, int *pos) {
+    const long long P = g.pitch;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
+    const int i = (int)(t % g.Xi) + g.Bx;
+    const long long r = t / g.Xi;
+    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    bool e = UI[id] < 0.0;
+    if (e) atomicAdd(&pos[0], 10000);
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        const double a = UI[n * P + id], b = LU[n * P + id];
+        if (isnan(a)) atomicAdd(&pos[n], 1100), e = true;
+        if (isinf(a)) atomicAdd(&pos[n], 1200), e = true;
+        if (isnan(b)) atomicAdd(&pos[n], 21), e = true;
+        if (isinf(b)) atomicAdd(&pos[n], 22), e = true;
+    }
+    if (e) {
+        pos[E] = 1;
+        pos[E + 1] = i, pos[E + 2] = j, pos[E + 3] = k;
+    }
+}
+
+// One-thread kernel: dt = CFL / sum(lambda_d / delta_d) from the maxima of the last k_states,
+// clipped to the target time as XFLUIDS::Evolution does (src/XFLUIDS.cpp:196-200); resets the
+// maxima; marks the step done when the target time is reached.
+static __global__ void k_dt_step(Geo g, DevFields f, double cfl) {
+    double *b = f.dtbuf;
+    if (b[4] != 0.0) return;
+    const double t = b[1], target = b[2];
+    if (!(t < target)) {
+        b[4] = 1.0;
+        b[0] = 0.0;
+        return;
+    }
+    const double lx = __longlong_as_double((long long)f.lam[0]);
+    const double ly = __longlong_as_double((long long)f.lam[1]);
+    const double lz = __longlong_as_double((long long)f.lam[2]);
+    const double dtref = lx * g._dx + ly * g._dy + lz * g._dz;
+    double dt = cfl / dtref;
+    if (t + dt > target) dt = target - t;
+    b[0] = dt;
+    b[1] = t + dt;
+    b[3] += 1.0;
+    f.lam[0] = f.lam[1] = f.lam[2] = 0ull;
+}
+
+}  // namespace xfg

@@ -1,0 +1,313 @@
+// xfg_mixed.cuh - mixed-precision form of the stage kernels.
+//
+// The conserved state U and the RK stage combination stay FP64; the characteristic projection,
+// the flux splitting, the WENO smoothness indicators and weights run in FP32 on FP32 copies of
+// U, of the physical fluxes and of the face primitives written by k_states_mixed. The FP32 right-
+// hand side is accumulated into the FP64 state by the RK stage. The multi-component temperature
+// Newton iteration and the multi-component Roe sound speed (the near-degenerate mixture
+// eigensystem) stay FP64.
+#pragma once
+
+#include "xfg_kernels.cuh"
+
+namespace xfg {
+
+// Primitive recovery of the mixed form. Single gas: from the FP64 state converted once to FP32.
+// Mixture: the FP64 recovery of k_states (Newton in FP64), followed by the FP32 copies.
+template <bool COP, int NS>
+__global__ void __launch_bounds__(kThreads) k_states_mixed(Geo g, DevFields f, DevThermo th, double *__restrict__ UI,
+                                                           int ghost, int want_lam, int guard) {
+    using S = Sys<COP, NS>;
+    constexpr int E = S::E, NCOP = S::NCOP;
+    if (guard && step_done(f)) return;
+    const long long P = g.pitch, N = g.ncell();
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    float lamx = 0.f, lamy = 0.f, lamz = 0.f;
+    if (id < N) {
+        float Uf[E];
+        float rho, u, v, w, p, H, c;
+        float yf[NS];
+        if (!COP) {
+#pragma unroll
+            for (int n = 0; n < E; n++) Uf[n] = (float)UI[n * P + id];
+            rho = Uf[0];
+            const float rho1 = 1.0f / rho;
+            u = Uf[1] * rho1, v = Uf[2] * rho1, w = Uf[3] * rho1;
+            const float tme = Uf[4] * rho1 - 0.5f * (u * u + v * v + w * w);
+            const float gm = (float)th.ncop_gamma;
+            p = (gm - 1.0f) * rho * tme;
+            H = (Uf[4] + p) * rho1;
+            c = sqrtf(gm * p * rho1);
+            yf[0] = 1.0f;
+        } else {
+            double U[E];
+#pragma unroll
+            for (int n = 0; n < E; n++) U[n] = UI[n * P + id];
+            const double rhod = U[0], rho1 = 1.0 / rhod;
+            double yi[NS];
+            if (ghost) {
+                yi[NCOP] = 0.0;
+                double sum = 0.0;
+#pragma unroll
+                for (int s = 0; s < NCOP; s++) yi[s] = U[s + 5] * rho1, sum += yi[s];
+                sum = 1.0 / sum;
+#pragma unroll
+                for (int s = 0; s < NCOP; s++) {
+                    yi[s] *= sum;
+                    U[s + 5] = rhod * yi[s];
+                    UI[(s + 5) * P + id] = U[s + 5];
+                }
+            } else {
+                yi[NCOP] = 1.0;
+#pragma unroll
+                for (int s = 0; s < NCOP; s++) yi[s] = U[s + 5] * rho1, yi[NCOP] += -yi[s];
+            }
+            const double ud = U[1] * rho1, vd = U[2] * rho1, wd = U[3] * rho1;
+            const double tme = U[4] * rho1 - 0.5 * (ud * ud + vd * vd + wd * wd);
+            const double Rm = mix_R<NS>(th, yi);
+            const double T = newton_T<NS>(th, yi, tme, f.T[id]);
+            const double pd = rhod * Rm * T;
+            const double Cp = mix_Cp<NS>(th, yi, T);
+            const double CopW = 1.0 / mix_W_inv<NS>(th, yi);
+            const double gmx = Cp / (Cp - kRu / CopW);
+            const double gamma = gmx > 1.0 ? gmx : -1.0;
+            const double Hd = (U[4] + pd) * rho1;
+            const double cd = sqrt(gamma * pd * rho1);
+            f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd, f.c[id] = cd;
+            f.e[id] = tme, f.gamma[id] = gamma, f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
+#pragma unroll
+            for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = (float)yi[s];
+#pragma unroll
+            for (int n = 0; n < E; n++) Uf[n] = (float)U[n];
+            rho = (float)rhod, u = (float)ud, v = (float)vd, w = (float)wd, p = (float)pd, H = (float)Hd, c = (float)cd;
+        }
+#pragma unroll
+        for (int n = 0; n < E; n++) f.Uf[n * P + id] = Uf[n];
+        float *pf = f.primf;
+        pf[0 * P + id] = rho, pf[1 * P + id] = u, pf[2 * P + id] = v, pf[3 * P + id] = w;
+        pf[4 * P + id] = H, pf[5 * P + id] = p, pf[6 * P + id] = c;
+        const float Ep = Uf[4] + p;
+        const float mom[3] = {Uf[1], Uf[2], Uf[3]}, vel[3] = {u, v, w};
+        const int dims[3] = {g.dimx, g.dimy, g.dimz};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            if (!dims[d]) continue;
+            float *F = f.Ff[d];
+            F[0 * P + id] = mom[d];
+            F[1 * P + id] = mom[d] * u + (d == 0 ? p : 0.f);
+            F[2 * P + id] = mom[d] * v + (d == 1 ? p : 0.f);
+            F[3 * P + id] = mom[d] * w + (d == 2 ? p : 0.f);
+            F[4 * P + id] = Ep * vel[d];
+#pragma unroll
+            for (int n = 5; n < E; n++) F[n * P + id] = mom[d] * yf[n - 5];
+        }
+        const int i = (int)(id % g.Xmax);
+        const long long r = id / g.Xmax;
+        const int j = (int)(r % g.Ymax), k = (int)(r / g.Ymax);
+        const bool inner = i >= g.Bx && i < g.Xmax - g.Bx && j >= g.By && j < g.Ymax - g.By && k >= g.Bz && k < g.Zmax - g.Bz;
+        if (inner && (!(rho >= 0.f) || !(p >= 0.f) || isinf(rho) || isinf(p))) {
+            atomicOr(&f.err[ERR_PRIM], 1);
+            f.err[ERR_I] = i, f.err[ERR_J] = j, f.err[ERR_K] = k;
+        }
+        if (want_lam) {
+            const float c_local = sqrtf(1.4f * p / rho);
+            lamx = fabsf(u) + c_local, lamy = fabsf(v) + c_local, lamz = fabsf(w) + c_local;
+            if (!(lamx >= 0.f)) lamx = __int_as_float(0x7f800000);
+            if (!(lamy >= 0.f)) lamy = __int_as_float(0x7f800000);
+            if (!(lamz >= 0.f)) lamz = __int_as_float(0x7f800000);
+        }
+    }
+    if (want_lam) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lamx = fmaxf(lamx, __shfl_xor_sync(0xffffffffu, lamx, o));
+            lamy = fmaxf(lamy, __shfl_xor_sync(0xffffffffu, lamy, o));
+            lamz = fmaxf(lamz, __shfl_xor_sync(0xffffffffu, lamz, o));
+        }
+        __shared__ float red[3][kThreads / 32];
+        const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (lane == 0) red[0][wid] = lamx, red[1][wid] = lamy, red[2][wid] = lamz;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float a = red[0][0], b = red[1][0], c = red[2][0];
+            for (int q = 1; q < kThreads / 32; q++) a = fmaxf(a, red[0][q]), b = fmaxf(b, red[1][q]), c = fmaxf(c, red[2][q]);
+            if (g.dimx) atomic_max_nonneg(&f.lam[0], (double)a);
+            if (g.dimy) atomic_max_nonneg(&f.lam[1], (double)b);
+            if (g.dimz) atomic_max_nonneg(&f.lam[2], (double)c);
+        }
+    }
+}
+
+template <int D, int E>
+__device__ __forceinline__ float project_f(const float *lrow, int n, const float *__restrict__ A, long long P, long long q) {
+    float acc = 0.f;
+    bool first = true;
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+        const int kind = left_kind(D, E, n, k);
+        if (kind == 0) continue;
+        const float x = __ldg(A + k * P + q);
+        float t = kind == 1 ? x : (kind == 2 ? -x : x * lrow[k]);
+        acc = first ? t : acc + t;
+        first = false;
+    }
+    return acc;
+}
+
+// FP32 characteristic WENO flux at face (i+1/2) of direction D (same structure as k_faces).
+template <int D, bool COP, int NS, int ORDER>
+__global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, DevThermo th, int artificial,
+                                                          const double *__restrict__ glf_d, int guard) {
+    using S = Sys<COP, NS>;
+    constexpr int E = S::E;
+    if (guard && step_done(f)) return;
+    const long long P = g.pitch;
+    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nfx * nfy * nfz) return;
+    const int i = (int)(t % nfx) + g.Bx - (D == 0 ? 1 : 0);
+    const long long r = t / nfx;
+    const int j = (int)(r % nfy) + g.By - (D == 1 ? 1 : 0);
+    const int k = (int)(r / nfy) + g.Bz - (D == 2 ? 1 : 0);
+    const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
+    const long long idl = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    const long long idr = idl + stride;
+    const float *__restrict__ pf = f.primf;
+
+    FaceStateT<float, NS> F;
+    if (!COP) {
+        const float rl = pf[idl], rr = pf[idr];
+        const float Dd = sqrtf(rr / rl);
+        const float D1 = 1.0f / (Dd + 1.0f);
+        F._u = (pf[1 * P + idl] + Dd * pf[1 * P + idr]) * D1;
+        F._v = (pf[2 * P + idl] + Dd * pf[2 * P + idr]) * D1;
+        F._w = (pf[3 * P + idl] + Dd * pf[3 * P + idr]) * D1;
+        F._H = (pf[4 * P + idl] + Dd * pf[4 * P + idr]) * D1;
+        F._P = (pf[5 * P + idl] + Dd * pf[5 * P + idr]) * D1;
+        F._rho = sqrtf(rr * rl);
+        const float gm = (float)th.ncop_gamma;
+        F.c2 = gm * F._P / F._rho;
+        F.b1 = (gm - 1.0f) / F.c2;
+        F.b3 = 0.f;
+        F._yi[0] = 1.f;
+        F.q2 = F._u * F._u + F._v * F._v + F._w * F._w;
+        F._c = sqrtf(F.c2);
+        F.b2 = 1.0f + F.b1 * F.q2 - F.b1 * F._H;
+        F._c1 = 1.0f / F._c;
+    } else {
+        FaceState<NS> Fd;
+        double G0;
+        face_state<COP, NS>(g, f, th, idl, idr, Fd, G0);
+        F._u = (float)Fd._u, F._v = (float)Fd._v, F._w = (float)Fd._w, F._H = (float)Fd._H;
+        F._P = (float)Fd._P, F._rho = (float)Fd._rho, F.c2 = (float)Fd.c2, F.b1 = (float)Fd.b1;
+        F.b3 = (float)Fd.b3, F.q2 = (float)Fd.q2, F._c = (float)Fd._c, F.b2 = (float)Fd.b2, F._c1 = (float)Fd._c1;
+#pragma unroll
+        for (int s = 0; s < NS; s++) F._yi[s] = (float)Fd._yi[s];
+#pragma unroll
+        for (int s = 0; s < (NS > 1 ? NS - 1 : 1); s++) F.z[s] = (float)Fd.z[s];
+    }
+    const float un = D == 0 ? F._u : (D == 1 ? F._v : F._w);
+    const float *__restrict__ Fl = f.Ff[D];
+    const float *__restrict__ Ua = f.Uf;
+    const float *__restrict__ vd = pf + (1 + D) * P;
+    const float *__restrict__ cf = pf + 6 * P;
+    float lm0 = 0.f, lm1 = 0.f, lm2 = 0.f;
+    if (ORDER == 5 && artificial == XFG_LLF) {
+#pragma unroll
+        for (int m = -2; m <= 3; m++) {
+            const long long q = idl + m * stride;
+            const float ud = __ldg(vd + q), cc = __ldg(cf + q);
+            lm0 = fmaxf(lm0, fabsf(ud - cc));
+            lm1 = fmaxf(lm1, fabsf(ud));
+            lm2 = fmaxf(lm2, fabsf(ud + cc));
+        }
+    }
+    constexpr int M0 = ORDER == 7 ? -3 : -2, M1 = ORDER == 7 ? 4 : 3;
+    float acc[E];
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        const float ev = n == 0 ? fabsf(un - F._c) : (n == E - 1 ? fabsf(un + F._c) : fabsf(un));
+        float av;
+        if (artificial == XFG_ROE || ORDER == 7) {
+            av = ev;
+            if (ORDER == 7 && artificial == XFG_GLF) av = 0.f;
+        } else if (artificial == XFG_LLF) {
+            av = n == 0 ? lm0 : (n == E - 1 ? lm2 : lm1);
+        } else {
+            av = (float)glf_d[n == 0 ? 0 : (n == E - 1 ? 2 : 1)];
+        }
+        float lrow[E];
+#pragma unroll
+        for (int kk = 0; kk < E; kk++) lrow[kk] = left_kind(D, E, n, kk) == 3 ? left_val<D, E>(F, n, kk) : 0.f;
+        float pp[8], mm[8];
+#pragma unroll
+        for (int m = M0; m <= M1; m++) {
+            const long long q = idl + m * stride;
+            const float uf = project_f<D, E>(lrow, n, Ua, P, q);
+            const float ff = project_f<D, E>(lrow, n, Fl, P, q);
+            pp[m + 3] = 0.5f * (ff + av * uf);
+            mm[m + 3] = 0.5f * (ff - av * uf);
+        }
+        const float fl = ORDER == 7 ? weno7(pp, mm) : weno5(pp, mm);
+#pragma unroll
+        for (int kk = 0; kk < E; kk++) {
+            const int kind = right_kind(D, E, n, kk);
+            if (kind == 0) continue;
+            const float tv = kind == 1 ? fl : (kind == 2 ? -fl : fl * right_val<D, E>(F, n, kk));
+            acc[kk] = (n == 0) ? tv : acc[kk] + tv;
+        }
+    }
+    float *Fw = f.Fwf[D];
+#pragma unroll
+    for (int n = 0; n < E; n++) Fw[n * P + idl] = acc[n];
+}
+
+// Divergence of the FP32 face fluxes, accumulated into the FP64 state by the RK stage.
+template <int E>
+__global__ void __launch_bounds__(kThreads) k_div_rk_mixed(Geo g, DevFields f, int flag, double dt_arg,
+                                                           const double *__restrict__ dt_dev, int do_rk, int store_lu,
+                                                           int guard) {
+    if (guard && step_done(f)) return;
+    const long long P = g.pitch;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
+    const int i = (int)(t % g.Xi) + g.Bx;
+    const long long r = t / g.Xi;
+    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    const long long sy = g.Xmax, sz = (long long)g.Xmax * g.Ymax;
+    const double dt = dt_dev ? dt_dev[0] : dt_arg;
+    const float fdx = (float)g._dx, fdy = (float)g._dy, fdz = (float)g._dz;
+    int code = 0;
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        float L = 0.f;
+        if (g.dimx) L += (f.Fwf[0][n * P + id - 1] - f.Fwf[0][n * P + id]) * fdx;
+        if (g.dimy) L += (f.Fwf[1][n * P + id - sy] - f.Fwf[1][n * P + id]) * fdy;
+        if (g.dimz) L += (f.Fwf[2][n * P + id - sz] - f.Fwf[2][n * P + id]) * fdz;
+        const double LU0 = (double)L;
+        if (store_lu) f.LU[n * P + id] = LU0;
+        if (!isfinite(L)) code = 1;
+        if (do_rk) {
+            const long long q = n * P + id;
+            double out;
+            if (flag == 1) {
+                out = f.U[q] + dt * LU0;
+                f.U1[q] = out;
+            } else if (flag == 2) {
+                out = 0.75 * f.U[q] + 0.25 * f.U1[q] + 0.25 * dt * LU0;
+                f.U1[q] = out;
+            } else {
+                out = (f.U[q] + 2.0 * f.U1[q] + 2.0 * dt * LU0) * kOT;
+                f.U[q] = out;
+            }
+            if (bad(out) || (n == 0 && out < 0.0)) code = 1;
+        }
+    }
+    if (code) {
+        atomicOr(&f.err[ERR_STATE], 1);
+        f.err[ERR_I] = i, f.err[ERR_J] = j, f.err[ERR_K] = k;
+    }
+}
+
+}  // namespace xfg

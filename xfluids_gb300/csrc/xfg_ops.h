@@ -1,0 +1,41 @@
+// xfg_ops.h - host-side table of kernel launchers, one table per compiled (COP, NS, order).
+// The API (xfg_api.cu) picks the table for a handle at creation; each instantiation unit
+// (xfg_inst_*.cu) fills the tables of its species count.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "xfg_device.cuh"
+
+namespace xfg {
+
+struct LaunchCtx {
+    Geo g;
+    DevFields f;
+    DevThermo th;
+    cudaStream_t st;
+    int artificial;                    // Artificial_type
+    int ghost;                         // GhostSpecies
+    int bc[6];
+    const double *glf;                 // GLF maxima per direction (9 doubles) or nullptr
+    int precision;                     // xfg_precision
+};
+
+struct Ops {
+    int cop, ns, order;
+    void (*bc)(const LaunchCtx &, double *U, const double *guard);
+    void (*states)(const LaunchCtx &, double *UI, int want_lam, int guard);
+    void (*faces)(const LaunchCtx &, int d, const double *UI, int guard);
+    void (*div_rk)(const LaunchCtx &, int flag, double dt, const double *dt_dev, int do_rk, int store_lu, int guard);
+    void (*glf)(const LaunchCtx &, unsigned long long *out, int guard);
+    void (*rk)(const LaunchCtx &, int flag, double dt);
+    void (*estimate_nan)(const LaunchCtx &, const double *UI, int *pos);
+};
+
+// Registry filled by the instantiation units.
+const Ops *find_ops(int cop, int ns, int order);
+void register_ops(const Ops *ops);
+
+inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+}  // namespace xfg
