@@ -242,6 +242,9 @@ void bc_cell(const Config &cf, R *U, int d, int BC, int i, int j, int k, int mir
     case XFG_NSLIPWALL:
     case XFG_VISCWALL:
     case XFG_SLIPWALL: {
+        // the Y and Z kernels mirror only nslipWall; viscWall and slipWall are no-ops there
+        // (BCs_kernels.hpp FluidBCKernelY/Z), the X kernel mirrors all three walls
+        if (d != 0 && BC != XFG_NSLIPWALL) break;
         src = 2 * (bw + mirror_offset) - 1 - c;
         size_t t = at(src);
         U[E * id + 0] = U[E * t + 0];
@@ -789,8 +792,11 @@ void lu_eigen(const Config &cf, Fields<R> &f) {
     for (int d = 0; d < 3; d++) {
         if (!dims[d]) continue;
         local_eigen(cf, f, d);
-        for (int n = 0; n < E; n++) {  // ConVenction_block.hpp:115-215
-            R mx = R(0.0);
+        // ConVenction_block.hpp:115-215: the SYCL max reduction folds in the previous value of
+        // eigen_block (zeroed once at allocation, src/Fluids.cpp:421-429), so the GLF maxima are
+        // running maxima over every GetLU call of the run
+        for (int n = 0; n < E; n++) {
+            R mx = f.eigen_block[d][n];
             for (long id = 0; id < ncell; id++) mx = fmax(mx, fabs(f.eig[d][E * id + n]));
             f.eigen_block[d][n] = mx;
         }

@@ -16,6 +16,10 @@ THERMO_JSON = os.path.join(GOLDEN, "thermo_tables.json")
 PARITY_TOL = 1e-12
 
 
+def parity_tol(scheme):
+    return PARITY_TOL
+
+
 def thermal(species, th=1):
     return thermo.load_thermal(species, th, tables_json=THERMO_JSON)
 

@@ -1,0 +1,77 @@
+"""Known-answer tests against fixtures generated from the reference's own build
+(tests/golden/make_golden.py): the oracle must reproduce them bit for bit on CPU; the CUDA path
+to the per-stage parity bound on the GPU."""
+import ast
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import helpers as H
+from oracle.xfo import Oracle
+from xfluids_gb300.abi import Block, Scheme
+from xfluids_gb300.mesh import empty_thermal
+
+FILES = sorted(glob.glob(os.path.join(H.GOLDEN, "*.npz")))
+
+
+def load(path):
+    z = np.load(path, allow_pickle=False)
+    b = Block()
+    for k, v in ast.literal_eval(str(z["block"])).items():
+        if k == "Boundarys":
+            for q in range(6):
+                b.Boundarys[q] = v[q]
+        else:
+            setattr(b, k, v)
+    s = Scheme()
+    for k, v in ast.literal_eval(str(z["scheme"])).items():
+        setattr(s, k, v)
+    th = H.thermal([str(x) for x in z["species"]], s.thermo) if s.cop else empty_thermal()
+    T0 = z["T0"] if z["T0"].size else None
+    return z, b, s, th, z["U0"], T0
+
+
+def test_fixtures_present():
+    assert len(FILES) >= 9
+
+
+@pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[:-4] for f in FILES])
+def test_oracle_reproduces_reference_bitwise(path):
+    z, b, s, th, U0, T0 = load(path)
+    o = Oracle(b, s, th, U0, T0)
+    o.initialize()
+    E = s.Emax
+    for q in range(len(z["dt"])):
+        if z["flag"][q] == 1:
+            assert o.get_dt() == z["dt"][q]
+        o.stage(int(z["flag"][q]), float(z["dt"][q]))
+        assert np.array_equal(H.inner_aos(b, o.get("U"), E), z["U"][q]), f"U stage {q}"
+        assert np.array_equal(H.inner_aos(b, o.get("LU"), E), z["LU"][q]), f"LU stage {q}"
+    for nm in ("rho", "p", "u", "v", "w", "c", "H"):
+        assert np.array_equal(o.get(nm), z["last_" + nm]), nm
+    if s.cop:
+        assert np.array_equal(o.get("T"), z["last_T"])
+        assert np.array_equal(o.get("y"), z["last_y"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[:-4] for f in FILES])
+def test_cuda_matches_reference_fixture(path, cuda_lib):
+    from xfluids_gb300.fluid import Fluid
+    z, b, s, th, U0, T0 = load(path)
+    f = Fluid(b, s, th)
+    f.InitialU(U0, T0)
+    f.initialize()
+    E = s.Emax
+    tol = H.parity_tol(s)
+    for q in range(len(z["dt"])):
+        if z["flag"][q] == 1:
+            dt = f.GetFluidDt()
+            assert abs(dt - z["dt"][q]) <= tol * z["dt"][q]
+        f.stage(int(z["flag"][q]), float(z["dt"][q]))
+        for nm, ref in (("U", z["U"][q]), ("LU", z["LU"][q])):
+            r = H.normwise(H.inner_aos(b, f.get(nm), E), ref, E)
+            assert np.all(r <= tol), f"{nm} stage {q}: {r} > {tol}"
+    f.close()

@@ -43,7 +43,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(unit):
         obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
-        cmd = [nvcc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, unit), "-o", obj]
+        extra = os.environ.get("XFG_NVCC_EXTRA", "").split()
+        cmd = [nvcc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, unit), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {unit}:\n{r.stderr[-4000:]}")

@@ -80,6 +80,9 @@ __global__ void __launch_bounds__(kThreads) k_bc(Geo g, double *__restrict__ U, 
         case XFG_NSLIPWALL:
         case XFG_VISCWALL:
         case XFG_SLIPWALL:
+            // FluidBCKernelY/Z mirror nslipWall only (viscWall / slipWall are no-ops there);
+            // FluidBCKernelX mirrors all three walls
+            if (D != 0 && BC != XFG_NSLIPWALL) break;
             src = cell(2 * (bw + mirror_offset) - 1 - cn);
 #pragma unroll
             for (int n = 0; n < E; n++) U[n * P + id] = (n >= 1 && n <= 3) ? -U[n * P + src] : U[n * P + src];
@@ -233,8 +236,8 @@ __global__ void __launch_bounds__(kThreads) k_states(Geo g, DevFields f, DevTher
 
 // ---------------------------------------------------------------------------------------------
 // Global LF maxima eigen_block[d][n] = max over all cells |lambda_n| (ConVenction_block.hpp:115-215)
-// for WENO5 (u_d - c, u_d, u_d + c); WENO7 local eigenvalues are zero. Written as bit patterns
-// into glf[d*3 + {0,1,2}].
+// for WENO5 (u_d - c, u_d, u_d + c); WENO7 local eigenvalues are zero. Folded by atomicMax into
+// the bit patterns glf[d*3 + {0,1,2}], which keep the maxima of all earlier calls.
 // ---------------------------------------------------------------------------------------------
 static __global__ void __launch_bounds__(kThreads) k_glf(Geo g, DevFields f, unsigned long long *glf, int guard) {
     if (guard && step_done(f)) return;
