@@ -1,0 +1,327 @@
+#!/usr/bin/env python3
+"""Benchmark of the convective right-hand side: cell-updates/s of the 2D isentropic Euler vortex
+(periodic [0,10]^2, 4096^2 cells, WENO5-JS + LLF, SSP-RK3, CFL 0.5), plain FP64 path (the headline
+`value`) and the mixed-precision form (FP32 reconstruction, FP64 state) beside it.
+
+One step = one full SSP-RK3 time step (3 stages, dt included) of the whole grid; one cell-update =
+one inner cell advanced one step. The state (670 MB) is larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--size 4096]
+
+--impl reference times the reference algorithm's CPU implementation (the oracle restatement,
+OpenMP over all host threads) on the same workload. Under torchrun every rank advances its own
+replica of the grid (replicas only: no data exchange); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+# DRAM bytes per face of the FP64 x-face kernel measured by ncu on a small case, scaled per face
+# (profiles/k_faces_fp64_vortex.md); None until a capture exists.
+NCU_FACE_BYTES_FP64 = None
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Dist:
+    """Barrier + max-over-ranks for torchrun launches (no data-path collective)."""
+
+    def __init__(self, world, local):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as td
+            torch.cuda.set_device(local)
+            td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+            self.td, self.torch = td, torch
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device="cuda")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device="cuda")
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in self.rows for q in range(4) if len(r) > 5 + q and r[5 + q] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def flops_per_face(size=64):
+    """Algorithmic flops of one x face of the vortex workload, counted on the oracle restatement
+    with a counting scalar (+,-,*,/,sqrt,exp,log = 1), per face and per cell-update."""
+    from oracle import xfo
+    from xfluids_gb300 import cases
+    b, s, th, U, T = cases.isentropic_vortex(size)
+    c = xfo.count_flops(b, s, th, U, T, 1)
+    nfx = (size + 1) * size
+    return c["faces_x"] / 3.0 / nfx, sum(c.values()) / float(size * size)
+
+
+def cpu_baseline(size, threads, min_seconds=10.0):
+    """Oracle (restatement) on the host cores: steps of the size^2 vortex until min_seconds."""
+    from oracle import xfo
+    from xfluids_gb300 import cases
+    xfo.set_threads(threads)
+    b, s, th, U, T = cases.isentropic_vortex(size)
+    o = xfo.Oracle(b, s, th, U, T)
+    o.initialize()
+    o.step()  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.step()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= min_seconds:
+            break
+    return size * size * n / el, n, el
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return 0
+    from oracle import xfo
+    threads = os.cpu_count() or 1
+    xfo.set_threads(threads)
+    from xfluids_gb300 import cases
+    # size the per-step sample so that warmup + steps ends within ~3 minutes
+    probe_n = 1024
+    rate, _, _ = cpu_baseline(probe_n, threads, min_seconds=2.0)
+    n = args.size
+    while n > 256 and (args.steps + args.warmup) * n * n / rate > 150.0:
+        n //= 2
+    b, s, th, U, T = cases.isentropic_vortex(n)
+    o = xfo.Oracle(b, s, th, U, T)
+    o.initialize()
+    for _ in range(args.warmup):
+        o.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step()
+    el = time.perf_counter() - t0
+    value = n * n * args.steps / el
+    line = {
+        "impl": "reference", "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"2D isentropic Euler vortex {args.size}^2 (sample {n}^2 per step), WENO5-JS LLF, SSP-RK3, CFL 0.5",
+                   "precision": "fp64", "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steps of the {n}^2 vortex after {args.warmup} warm-up steps"},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu_arm(args, world, rank, local):
+    from xfluids_gb300 import cases
+    from xfluids_gb300.abi import MIXED
+    from xfluids_gb300.fluid import Fluid, PinnedArray, measure_pipe_peaks, build_info
+    d = Dist(world, local)
+    n = args.size
+    peaks = measure_pipe_peaks(local)
+    fpf, flops_per_cu = flops_per_face()
+
+    def setup(precision):
+        b, s, th, U, T = cases.isentropic_vortex(n, precision=precision)
+        f = Fluid(b, s, th, device=local)
+        f.InitialU(U, T)
+        f.initialize()
+        return f, b, U
+
+    def reset(fl, U):
+        fl.InitialU(U)
+        fl.initialize()
+        fl.time = 0.0
+
+    # ---- plain FP64 path: device-timed value --------------------------------------------------
+    f, b, U0 = setup(0)
+    f.advance(args.warmup)          # warm-up (also captures the step graph)
+    reset(f, U0)
+    d.barrier()
+    f.synchronize()
+    with ClockSampler(local) as clk:
+        st, t_end, k, ms = f.advance_timed(args.steps)
+    d.barrier()
+    ms = d.max(ms)
+    cells_all = d.sum(n * n * k)
+    value = cells_all / (ms * 1e-3)
+    launches = f.launches_per_step * k
+    phases = [f.time_phases() for _ in range(2)]
+    ph = {key: float(np.mean([p[key] for p in phases])) for key in phases[0]}
+    face_launch_ms = ph["faces_x"] / 3.0
+    faces_per_launch = (n + 1) * n
+    achieved = fpf * faces_per_launch / (face_launch_ms * 1e-3)
+    U_fp64 = f.get("U")
+    t_fp64 = f.time
+    ms_total_fp64 = ms / k
+
+    # ---- end to end through the public API with host buffers -----------------------------------
+    E = 5
+    host = PinnedArray(U0.size)
+    host.array[:] = U0
+    e2e_steps = max(1, min(args.steps, 3))
+    f2, _, _ = setup(0)
+    f2.advance(1)
+    f2.synchronize()
+    d.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        f2.InitialU(host.array)            # H2D of the step's input state
+        f2.initialize()
+        f2.advance(1)
+        host.array[:] = f2.get("U")        # D2H of the step's result
+    el = time.perf_counter() - t0
+    el = d.max(el)
+    e2e_value = d.sum(n * n * e2e_steps) / el
+    bytes_state = U0.size * 8
+    f2.close()
+    host.close()
+
+    # ---- mixed precision form, from the same initial state to the same final time ---------------
+    fm, _, _ = setup(MIXED)
+    fm.advance(args.warmup)
+    reset(fm, U0)
+    d.barrier()
+    st_m, tm, km, ms_m = fm.advance_timed(args.steps + 16, t_fp64)
+    ms_m = d.max(ms_m)
+    value_mixed = d.sum(n * n * km) / (ms_m * 1e-3)
+    Um = fm.get("U")
+    Ui = U_fp64.reshape(b.Zmax, b.Ymax, b.Xmax, E)[b.inner_slices()]
+    Umi = Um.reshape(b.Zmax, b.Ymax, b.Xmax, E)[b.inner_slices()]
+    l1 = float(np.abs(Umi - Ui).mean())
+    linf = float(np.abs(Umi - Ui).max())
+    phases_m = fm.time_phases()
+    mixed_face_ms = phases_m["faces_x"] / 3.0
+    fm.close()
+    f.close()
+    d.close()
+    if rank != 0:
+        return 0
+
+    fp64_peak = peaks["fp64_flops"] / 1e12
+    traffic = None if NCU_FACE_BYTES_FP64 is None else NCU_FACE_BYTES_FP64 * faces_per_launch
+    cpu_threads = os.cpu_count() or 1
+    cpu_val, cpu_steps, cpu_el = cpu_baseline(1024, cpu_threads, min_seconds=10.0)
+    line = {
+        "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+        "steps": k, "warmup": args.warmup, "ms_per_step": ms_total_fp64, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"2D isentropic Euler vortex {n}^2, periodic [0,10]^2, WENO5-JS LLF, SSP-RK3, CFL 0.5",
+                   "precision": "fp64 (plain path)", "cells": n * n, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (state 670 MB)"},
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_state,
+                "d2h_bytes_per_step": bytes_state, "steps": e2e_steps,
+                "path": "xfg_set_state(pinned host U) + BoundaryCondition + UpdateFluidStates + xfg_advance(1) + xfg_get_array(U)"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp64", "kernel": "k_faces<x> (FP64 characteristic WENO5 face flux)",
+                     "achieved": achieved / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": achieved / 1e12 / fp64_peak, "traffic": traffic,
+                     "algorithmic_flops_per_face": fpf, "faces_per_launch": faces_per_launch,
+                     "launch_ms": face_launch_ms,
+                     "peak_source": "measured FP64 FMA chain on this GPU (xfg_measure_pipe_peaks); MEASURED_PEAKS.json has no FP64 figure"},
+        "phases_ms_per_step": ph,
+        "mixed": {"value": value_mixed, "unit": "cell-updates/s", "speedup_vs_fp64": value_mixed / value,
+                  "steps": km, "l1_vs_fp64": l1, "linf_vs_fp64": linf, "t": tm,
+                  "faces_x_launch_ms": mixed_face_ms, "phases_ms_per_step": phases_m,
+                  "fp32_peak_tflops": peaks["fp32_flops"] / 1e12},
+        "cpu_baseline": {"value": cpu_val, "unit": "cell-updates/s", "cores": cpu_threads, "kind": "port",
+                         "sample": f"{cpu_steps} steps of the 1024^2 vortex ({cpu_el:.1f} s) on the oracle restatement"},
+        "clocks": clk.summary(),
+        "flops_per_cell_update": flops_per_cu,
+        "build": build_info(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=4096)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference_arm(args, world, rank)
+    return run_gpu_arm(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

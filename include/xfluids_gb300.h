@@ -68,7 +68,12 @@ typedef struct xfg_thermal {
 /* Scheme selection: the reference's compile-time switches (cmake/init_options.cmake:23-90,
  * cmake/init_sample.cmake:216-282) as run-time values. */
 enum xfg_artificial { XFG_ROE = 1, XFG_LLF = 2, XFG_GLF = 3 };  /* Artificial_type */
-enum xfg_precision { XFG_FP64 = 0, XFG_MIXED = 1 };
+/* XFG_FP64: FP64 path; single-gas kernels use fused multiply-add, mixture kernels are compiled
+ *           without contraction (their characteristic system amplifies rounding differences).
+ * XFG_MIXED: FP32 reconstruction / splitting / WENO with the FP64 state and RK stage sum.
+ * XFG_FP64_STRICT: FP64 without contraction anywhere: the operation sequence of the reference's
+ *           CPU build, bit-identical to it where the math library calls agree. */
+enum xfg_precision { XFG_FP64 = 0, XFG_MIXED = 1, XFG_FP64_STRICT = 2 };
 
 typedef struct xfg_scheme {
     int cop;               /* COP: multi-component (Emax = NUM_SPECIES + 4) or single gas (Emax = 5) */
@@ -78,7 +83,7 @@ typedef struct xfg_scheme {
     int thermo;            /* Thermo: 1 NASA-9, 0 JANAF / NASA-7 */
     int ghost_species;     /* GhostSpecies: renormalise Y and write it back into U */
     double ncop_gamma;     /* NCOP_Gamma, ratio of specific heats without COP */
-    int precision;         /* xfg_precision: FP64 path or FP32 reconstruction with FP64 state */
+    int precision;         /* xfg_precision */
 } xfg_scheme;
 
 /* Arrays a caller can read back (xfg_get_array). */
@@ -156,6 +161,17 @@ int xfg_step(xfg_handle *h, double target_t, double *t, double *dt);
  * device and the launches replayed from a captured CUDA graph. Stops early once target_t is
  * reached. *t and *steps_done report the result; the call synchronises once at the end. */
 int xfg_advance(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done);
+
+/* xfg_advance with the device time of the replayed steps (CUDA events on the handle's stream
+ * around the graph launches) written to *device_ms. */
+int xfg_advance_timed(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done, float *device_ms);
+
+/* Number of kernel launches of one fused step (xfg_step / one xfg_advance replay). */
+int xfg_launches_per_step(xfg_handle *h, int *n);
+
+/* Page-locked host buffers for callers that stream states to and from the device. */
+int xfg_pinned_alloc(size_t bytes, void **ptr);
+int xfg_pinned_free(void *ptr);
 
 /* One fused step like xfg_step with CUDA events between the launches: ms_out[7] receives the
  * device time of each phase summed over the three stages: [0] dt, [1] boundary, [2] primitive

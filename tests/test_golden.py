@@ -57,10 +57,12 @@ def test_oracle_reproduces_reference_bitwise(path):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 2], ids=["fp64", "strict"])
 @pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[:-4] for f in FILES])
-def test_cuda_matches_reference_fixture(path, cuda_lib):
+def test_cuda_matches_reference_fixture(path, precision, cuda_lib):
     from xfluids_gb300.fluid import Fluid
     z, b, s, th, U0, T0 = load(path)
+    s.precision = precision
     f = Fluid(b, s, th)
     f.InitialU(U0, T0)
     f.initialize()

@@ -9,7 +9,7 @@ import pytest
 
 import helpers as H
 from oracle.xfo import Oracle
-from xfluids_gb300.abi import ROE, LLF, GLF, MIXED
+from xfluids_gb300.abi import ROE, LLF, GLF, MIXED, FP64, FP64_STRICT
 
 pytestmark = pytest.mark.gpu
 
@@ -38,8 +38,9 @@ def _compare_stage(block, f, o, E, tag, cop):
     return worst
 
 
-def run_stagewise(case, steps=2):
+def run_stagewise(case, steps=2, precision=FP64):
     b, s, th, U, T = case
+    s.precision = precision
     E = s.Emax
     f = _fluid(b, s, th, U, T)
     o = Oracle(b, s, th, U, T)
@@ -74,10 +75,19 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("precision", [FP64, FP64_STRICT], ids=["fp64", "strict"])
 @pytest.mark.parametrize("name", list(CASES))
-def test_stagewise_parity(name, cuda_lib):
-    worst = run_stagewise(CASES[name](), steps=2)
+def test_stagewise_parity(name, precision, cuda_lib):
+    worst = run_stagewise(CASES[name](), steps=2, precision=precision)
     print(f"{name}: worst normwise relative difference {worst:.3e}")
+
+
+@pytest.mark.parametrize("name", ["vortex64", "blast3d_weno7_glf", "riemann2d_weno7_sym", "mixing5_weno7_janaf"])
+def test_strict_is_bitwise(name, cuda_lib):
+    """Without contraction the CUDA path performs the reference's operation sequence: every array
+    of every stage is bit-identical to the oracle (no log/exp on these cases)."""
+    worst = run_stagewise(CASES[name](), steps=2, precision=FP64_STRICT)
+    assert worst == 0.0
 
 
 @pytest.mark.parametrize("name", ["vortex64", "sod_weno5_llf", "mixing5_weno7_janaf", "blast3d_weno5"])
@@ -123,6 +133,25 @@ def test_advance_stops_at_target(cuda_lib):
     f.close()
 
 
+def test_mixed_mixture_close_to_fp64(cuda_lib):
+    """Mixed form on the 5-species mixing layer: FP32 projection / WENO with the FP64 Roe sound
+    speed of the mixture and the FP64 Newton temperature."""
+    b, s, th, U, T = H.mixing_small((24, 16, 8))
+    f64 = _fluid(b, s, th, U, T)
+    s2 = H.mixing_small((24, 16, 8))[1]
+    s2.precision = MIXED
+    fmx = _fluid(b, s2, th, U, T)
+    f64.initialize(), fmx.initialize()
+    st1, t1, n1 = f64.advance(5)
+    st2, t2, n2 = fmx.advance(50, t1)
+    assert st1 == 0 and st2 == 0 and t1 == t2
+    a, r = H.inner_aos(b, fmx.get("U"), 9), H.inner_aos(b, f64.get("U"), 9)
+    rel = np.abs(a - r).mean(axis=0) / np.abs(r).mean(axis=0)
+    print("mixed mixture L1 relative per component", rel)
+    assert np.all(rel < 1e-4), rel
+    f64.close(), fmx.close()
+
+
 def test_mixed_precision_close_to_fp64(cuda_lib):
     from xfluids_gb300 import cases
     b, s, th, U, T = cases.isentropic_vortex(128)
@@ -140,7 +169,7 @@ def test_mixed_precision_close_to_fp64(cuda_lib):
 
 def test_nan_detection(cuda_lib):
     b, s, th, U, T = H.sod_like(64)
-    U = U.copy()
+    U = U.copy().reshape(-1)
     U[5 * 40 + 4] = np.nan     # energy of one inner cell
     f = _fluid(b, s, th, U, T)
     err = f.initialize()

@@ -19,7 +19,7 @@ INFLOW, OUTFLOW, SYMMETRY, PERIODIC, NSLIPWALL, VISCWALL, SLIPWALL, INNERBLOCK =
 # enum xfg_artificial (Artificial_type)
 ROE, LLF, GLF = 1, 2, 3
 # enum xfg_precision
-FP64, MIXED = 0, 1
+FP64, MIXED, FP64_STRICT = 0, 1, 2
 
 # enum xfg_array
 ARRAYS = {
@@ -129,6 +129,10 @@ def lib():
         "xfg_device_array": [P, I, C.POINTER(P), C.POINTER(C.c_size_t)],
         "xfg_measure_pipe_peaks": [I, pd],
         "xfg_time_phases": [P, D, C.POINTER(C.c_float)],
+        "xfg_advance_timed": [P, I, D, pd, pi, C.POINTER(C.c_float)],
+        "xfg_launches_per_step": [P, pi],
+        "xfg_pinned_alloc": [C.c_size_t, C.POINTER(P)],
+        "xfg_pinned_free": [P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

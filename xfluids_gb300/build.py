@@ -12,8 +12,12 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libxfluids_gb300.so")
 
-UNITS = ["xfg_api.cu", "xfg_inst_ncop.cu", "xfg_inst_cop2.cu", "xfg_inst_cop3.cu", "xfg_inst_cop4.cu",
-         "xfg_inst_cop5.cu", "xfg_inst_cop6.cu"]
+# (unit, extra nvcc flags): FP64 mixture kernels and the strict single-gas kernels are compiled
+# without floating-point contraction.
+NOFMA = ["--fmad=false"]
+UNITS = [("xfg_api.cu", []), ("xfg_inst_ncop.cu", []), ("xfg_inst_ncop_strict.cu", NOFMA)]
+UNITS += [(f"xfg_inst_cop{n}.cu", NOFMA) for n in (2, 3, 4, 5, 6)]
+UNITS += [(f"xfg_inst_cop{n}_mixed.cu", []) for n in (2, 3, 4, 5, 6)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
@@ -41,10 +45,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     nvcc = _nvcc()
 
-    def compile_one(unit):
+    def compile_one(item):
+        unit, unit_flags = item
         obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
         extra = os.environ.get("XFG_NVCC_EXTRA", "").split()
-        cmd = [nvcc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, unit), "-o", obj]
+        cmd = [nvcc, *ARCH, *FLAGS, *unit_flags, *extra, "-c", os.path.join(CSRC, unit), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {unit}:\n{r.stderr[-4000:]}")

@@ -12,10 +12,12 @@
 #include <vector>
 
 #include "../../include/xfluids_gb300.h"
+#define XFG_KNS api
 #include "xfg_kernels.cuh"
 #include "xfg_ops.h"
 
 using namespace xfg;
+using namespace xfg::api;
 
 // ---------------------------------------------------------------------------------------------
 // errors
@@ -46,9 +48,9 @@ static std::vector<const Ops *> &registry() {
     return r;
 }
 void register_ops(const Ops *ops) { registry().push_back(ops); }
-const Ops *find_ops(int cop, int ns, int order) {
+const Ops *find_ops(int cop, int ns, int order, int precision) {
     for (const Ops *o : registry())
-        if (o->cop == cop && o->ns == ns && o->order == order) return o;
+        if (o->cop == cop && o->ns == ns && o->order == order && o->precision == precision) return o;
     return nullptr;
 }
 }  // namespace xfg
@@ -106,6 +108,7 @@ static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *
     if (!b || !s || !t) return fail(-1, "null argument");
     if (s->scheme_order != 5 && s->scheme_order != 7) return fail(-1, "scheme_order must be 5 or 7 (got %d)", s->scheme_order);
     if (s->artificial_type < 1 || s->artificial_type > 3) return fail(-1, "artificial_type must be 1..3");
+    if (s->precision < 0 || s->precision > 2) return fail(-1, "precision must be 0 (fp64), 1 (mixed) or 2 (fp64 strict)");
     if (s->cop && (s->num_species < 2 || s->num_species > XFG_MAX_SPECIES))
         return fail(-1, "num_species %d out of range for COP", s->num_species);
     if (!s->cop && s->num_species != 1) return fail(-1, "num_species must be 1 without COP");
@@ -138,7 +141,8 @@ const char *xfg_build_info(void) {
         info = "xfluids_gb300 sm_103a; kernels:";
         for (const Ops *o : registry()) {
             char b[64];
-            snprintf(b, sizeof b, " %s%d/weno%d", o->cop ? "cop" : "ncop", o->ns, o->order);
+            static const char *pn[3] = {"fp64", "mixed", "fp64strict"};
+            snprintf(b, sizeof b, " %s%d/weno%d/%s", o->cop ? "cop" : "ncop", o->ns, o->order, pn[o->precision]);
             info += b;
         }
     }
@@ -151,8 +155,11 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     *out = nullptr;
     int v = validate(block, scheme, thermal);
     if (v) return v;
-    const Ops *ops = find_ops(scheme->cop ? 1 : 0, scheme->cop ? scheme->num_species : 1, scheme->scheme_order);
-    if (!ops) return fail(-1, "no kernels built for cop=%d num_species=%d order=%d", scheme->cop, scheme->num_species, scheme->scheme_order);
+    const Ops *ops = find_ops(scheme->cop ? 1 : 0, scheme->cop ? scheme->num_species : 1, scheme->scheme_order,
+                              scheme->precision);
+    if (!ops)
+        return fail(-1, "no kernels built for cop=%d num_species=%d order=%d precision=%d", scheme->cop,
+                    scheme->num_species, scheme->scheme_order, scheme->precision);
     CK(cudaSetDevice(device));
     xfg_handle *h = new xfg_handle();
     h->device = device;
@@ -164,7 +171,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     h->N = (long long)block->Xmax * block->Ymax * block->Zmax;
     h->P = (long long)align_up((size_t)h->N, 64);
     const int E = h->E, NS = h->NS;
-    const bool mixed = scheme->precision == XFG_MIXED;
+    const bool mixed = scheme->precision == XFG_MIXED;  // FP32 copies instead of FP64 fluxes
     const int dims[3] = {block->DimX, block->DimY, block->DimZ};
     const size_t arr8 = (size_t)h->P * 8, arr4 = align_up((size_t)h->P * 4, 256);
     // layout of the pool
@@ -458,7 +465,17 @@ int xfg_step(xfg_handle *h, double target_t, double *t, double *dt) {
     return finish(h, t, dt, nullptr);
 }
 
+static int advance_impl(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done, float *device_ms);
+
 int xfg_advance(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done) {
+    return advance_impl(h, nsteps, target_t, t, steps_done, nullptr);
+}
+
+int xfg_advance_timed(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done, float *device_ms) {
+    return advance_impl(h, nsteps, target_t, t, steps_done, device_ms);
+}
+
+static int advance_impl(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done, float *device_ms) {
     if (!h) return fail(-1, "null handle");
     if (!h->states_ready) return fail(-1, "xfg_advance needs a preceding xfg_update_states (main.cpp:45-47)");
     CK(cudaSetDevice(h->device));
@@ -474,8 +491,31 @@ int xfg_advance(xfg_handle *h, int nsteps, double target_t, double *t, int *step
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return fail(-2, "graph instantiate failed: %s", cudaGetErrorString(e));
     }
+    if (device_ms) CK(cudaEventRecord(h->ev[2], h->st));
     for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(h->graph, h->st));
-    return finish(h, t, nullptr, steps_done);
+    if (device_ms) CK(cudaEventRecord(h->ev[3], h->st));
+    int rc = finish(h, t, nullptr, steps_done);
+    if (device_ms) cudaEventElapsedTime(device_ms, h->ev[2], h->ev[3]);
+    return rc;
+}
+
+int xfg_pinned_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return fail(-1, "null argument");
+    CK(cudaMallocHost(ptr, bytes));
+    return 0;
+}
+
+int xfg_pinned_free(void *ptr) {
+    CK(cudaFreeHost(ptr));
+    return 0;
+}
+
+int xfg_launches_per_step(xfg_handle *h, int *n) {
+    if (!h || !n) return fail(-1, "null argument");
+    const int dims = h->bl.DimX + h->bl.DimY + h->bl.DimZ;
+    const int glf = h->sc.artificial_type == XFG_GLF ? 1 : 0;
+    *n = 1 + 3 * (dims + 1 + glf + dims + 1);  // dt, then per stage: bc per dim, states, [glf], faces per dim, div+rk
+    return 0;
 }
 
 // Per-phase device times of one fused step (ms, summed over the 3 stages): [0] dt, [1] boundary,

@@ -14,6 +14,10 @@
 
 #include "../../include/xfluids_gb300.h"
 
+#ifndef XFG_KNS
+#define XFG_KNS fast
+#endif
+
 namespace xfg {
 
 constexpr double kRu = 6.02214076e26 * 1.380649e-23 * 1.0E-3;  // global_setup.h:48-54
@@ -61,6 +65,21 @@ struct DevFields {
     double *dtbuf;             // [0] dt of the step, [1] time, [2] target time, [3] steps done
     int *err;                  // error words: [0] state NaN code, [1] primitive error, [2] i, [3] j, [4] k
 };
+
+// Roe state of a face: MARCO_ROE (global_marco.h:26-37), c^2 and MARCO_PREEIGEN.
+template <class T, int NS>
+struct FaceStateT {
+    T _u, _v, _w, _H, _P, _rho, D, D1;
+    T c2, b1, b3, q2, _c, b2, _c1;
+    T z[NS > 1 ? NS - 1 : 1];
+    T _yi[NS];
+};
+template <int NS>
+using FaceState = FaceStateT<double, NS>;
+
+// Device code lives in a namespace per translation unit (XFG_KNS) so that the same template
+// compiled with different floating-point contraction flags in two units stays two kernels.
+namespace XFG_KNS {
 
 // ---------------------------------------------------------------------------------------------
 // Thermodynamics, src/solver_Ini/Thermo_device.h
@@ -186,17 +205,6 @@ __host__ __device__ constexpr int right_kind(int D, int E, int n, int k) {
     if (k == 4) return 3;
     return (k == 5 + (n - 4)) ? 1 : 0;
 }
-
-// Roe state of a face: MARCO_ROE (global_marco.h:26-37), c^2 and MARCO_PREEIGEN.
-template <class T, int NS>
-struct FaceStateT {
-    T _u, _v, _w, _H, _P, _rho, D, D1;
-    T c2, b1, b3, q2, _c, b2, _c1;
-    T z[NS > 1 ? NS - 1 : 1];
-    T _yi[NS];
-};
-template <int NS>
-using FaceState = FaceStateT<double, NS>;
 
 // General entry (kind 3) of row n of L for direction D, component k (RoeAverageLeft_*).
 template <int D, int E, class T, int NS>
@@ -361,4 +369,5 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, doub
     atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
+}  // namespace XFG_KNS
 }  // namespace xfg

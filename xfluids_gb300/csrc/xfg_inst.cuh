@@ -1,4 +1,10 @@
-// xfg_inst.cuh - launchers of the kernels for one (COP, NS); included once per instantiation unit.
+// xfg_inst.cuh - launchers of the kernels for one (COP, NS, arithmetic form); included by the
+// instantiation units. Each unit defines XFG_KNS (its own kernel namespace) before the include and
+// registers the tables it compiles:
+//   xfg_inst_ncop.cu          single gas, FP64 with FMA contraction + mixed form
+//   xfg_inst_ncop_strict.cu   single gas, FP64 without contraction (--fmad=false)
+//   xfg_inst_cop<N>.cu        N-species mixture, FP64 without contraction (--fmad=false)
+//   xfg_inst_cop<N>_mixed.cu  N-species mixture, mixed form
 #pragma once
 
 #include "xfg_kernels.cuh"
@@ -6,8 +12,9 @@
 #include "xfg_ops.h"
 
 namespace xfg {
+namespace XFG_KNS {
 
-template <bool COP, int NS>
+template <bool COP, int NS, bool MIXED>
 struct Inst {
     static constexpr int E = Sys<COP, NS>::E;
 
@@ -28,7 +35,7 @@ struct Inst {
     }
     static void states(const LaunchCtx &c, double *UI, int want_lam, int guard) {
         const long long n = c.g.ncell();
-        if (c.precision == XFG_MIXED)
+        if (MIXED)
             k_states_mixed<COP, NS><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, c.th, UI, c.ghost, want_lam, guard);
         else
             k_states<COP, NS><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, c.th, UI, c.ghost, want_lam, guard);
@@ -38,7 +45,7 @@ struct Inst {
         const Geo &g = c.g;
         long long n = (long long)(g.Xi + (D == 0)) * (g.Yi + (D == 1)) * (g.Zi + (D == 2));
         const double *glf = c.glf ? c.glf + 3 * D : nullptr;
-        if (c.precision == XFG_MIXED)
+        if (MIXED)
             k_faces_mixed<D, COP, NS, ORDER><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, c.artificial, glf, guard);
         else
             k_faces<D, COP, NS, ORDER><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, UI, c.artificial, glf, guard);
@@ -52,7 +59,7 @@ struct Inst {
     static void div_rk(const LaunchCtx &c, int flag, double dt, const double *dt_dev, int do_rk, int store_lu, int guard) {
         const Geo &g = c.g;
         long long n = (long long)g.Xi * g.Yi * g.Zi;
-        if (c.precision == XFG_MIXED)
+        if (MIXED)
             k_div_rk_mixed<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, flag, dt, dt_dev, do_rk, store_lu, guard);
         else
             k_div_rk<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, flag, dt, dt_dev, do_rk, store_lu, guard);
@@ -62,7 +69,6 @@ struct Inst {
         // reference's reductions fold in the previous eigen_block values
         k_glf<<<grid_for(c.g.ncell(), kThreads), kThreads, 0, c.st>>>(c.g, c.f, out, guard);
     }
-
     static void rk(const LaunchCtx &c, int flag, double dt) {
         long long n = (long long)c.g.Xi * c.g.Yi * c.g.Zi;
         k_rk<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, flag, dt);
@@ -72,20 +78,25 @@ struct Inst {
         k_estimate_nan<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, UI, c.f.LU, pos);
     }
 
-    static const Ops *table(int order) {
-        static const Ops t5 = {COP ? 1 : 0, NS, 5, bc, states, faces<5>, div_rk, glf, rk, estimate_nan};
-        static const Ops t7 = {COP ? 1 : 0, NS, 7, bc, states, faces<7>, div_rk, glf, rk, estimate_nan};
-        return order == 7 ? &t7 : &t5;
+    // tables for scheme order 5 and 7, registered under precision id `prec`
+    static const Ops *table(int order, int prec) {
+        static Ops t[2][3];
+        Ops &o = t[order == 7][prec];
+        o = Ops{COP ? 1 : 0, NS, order, prec, bc, states, order == 7 ? faces<7> : faces<5>, div_rk, glf, rk, estimate_nan};
+        return &o;
     }
 };
 
-// Registers the tables of one (COP, NS) at load time.
-template <bool COP, int NS>
+// Registers, at load time, the tables of one (COP, NS, form) under the given precision ids.
+template <bool COP, int NS, bool MIXED>
 struct Registrar {
-    Registrar() {
-        register_ops(Inst<COP, NS>::table(5));
-        register_ops(Inst<COP, NS>::table(7));
+    explicit Registrar(std::initializer_list<int> precisions) {
+        for (int prec : precisions) {
+            register_ops(Inst<COP, NS, MIXED>::table(5, prec));
+            register_ops(Inst<COP, NS, MIXED>::table(7, prec));
+        }
     }
 };
 
+}  // namespace XFG_KNS
 }  // namespace xfg

@@ -20,6 +20,8 @@ constexpr int kThreads = 128;
 // error words in DevFields::err
 enum { ERR_STATE = 0, ERR_PRIM = 1, ERR_I = 2, ERR_J = 3, ERR_K = 4, ERR_NWORDS = 8 };
 
+namespace XFG_KNS {
+
 __device__ __forceinline__ bool bad(double x) {  // NaN or Inf through the exponent bits
     return ((__double2hiint(x) & 0x7ff00000) == 0x7ff00000);
 }
@@ -579,4 +581,5 @@ static __global__ void k_dt_step(Geo g, DevFields f, double cfl) {
     f.lam[0] = f.lam[1] = f.lam[2] = 0ull;
 }
 
+}  // namespace XFG_KNS
 }  // namespace xfg

@@ -11,6 +11,7 @@
 #include "xfg_kernels.cuh"
 
 namespace xfg {
+namespace XFG_KNS {
 
 // Primitive recovery of the mixed form. Single gas: from the FP64 state converted once to FP32.
 // Mixture: the FP64 recovery of k_states (Newton in FP64), followed by the FP32 copies.
@@ -310,4 +311,5 @@ __global__ void __launch_bounds__(kThreads) k_div_rk_mixed(Geo g, DevFields f, i
     }
 }
 
+}  // namespace XFG_KNS
 }  // namespace xfg

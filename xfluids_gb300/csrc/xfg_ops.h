@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include <initializer_list>
+
 #include "xfg_device.cuh"
 
 namespace xfg {
@@ -23,6 +25,7 @@ struct LaunchCtx {
 
 struct Ops {
     int cop, ns, order;
+    int precision;                     // xfg_precision the table serves
     void (*bc)(const LaunchCtx &, double *U, const double *guard);
     void (*states)(const LaunchCtx &, double *UI, int want_lam, int guard);
     void (*faces)(const LaunchCtx &, int d, const double *UI, int guard);
@@ -33,7 +36,7 @@ struct Ops {
 };
 
 // Registry filled by the instantiation units.
-const Ops *find_ops(int cop, int ns, int order);
+const Ops *find_ops(int cop, int ns, int order, int precision);
 void register_ops(const Ops *ops);
 
 inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }

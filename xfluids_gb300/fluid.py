@@ -119,6 +119,18 @@ class Fluid:
         st = check(lib().xfg_advance(self._h, nsteps, target_t, C.byref(t), C.byref(n)))
         return st, t.value, n.value
 
+    def advance_timed(self, nsteps: int, target_t: float = 1e300):
+        """advance() plus the device time (ms, CUDA events on the handle's stream)."""
+        t, n, ms = C.c_double(), C.c_int(), C.c_float()
+        st = check(lib().xfg_advance_timed(self._h, nsteps, target_t, C.byref(t), C.byref(n), C.byref(ms)))
+        return st, t.value, n.value, ms.value
+
+    @property
+    def launches_per_step(self) -> int:
+        n = C.c_int()
+        check(lib().xfg_launches_per_step(self._h, C.byref(n)))
+        return n.value
+
     def time_phases(self, target_t: float = 1e300):
         """One fused step with per-phase device times (ms): dt, boundary, states, faces x/y/z, rk."""
         ms = (C.c_float * 7)()
@@ -144,6 +156,29 @@ def measure_pipe_peaks(device: int = 0):
     out = (C.c_double * 3)()
     check(lib().xfg_measure_pipe_peaks(device, out))
     return {"fp64_flops": out[0], "fp32_flops": out[1], "sm_clock_mhz": out[2]}
+
+
+class PinnedArray:
+    """A numpy view of page-locked host memory (xfg_pinned_alloc)."""
+
+    def __init__(self, n: int, dtype=np.float64):
+        self.nbytes = int(n) * np.dtype(dtype).itemsize
+        self._p = C.c_void_p()
+        check(lib().xfg_pinned_alloc(self.nbytes, C.byref(self._p)))
+        buf = (C.c_char * self.nbytes).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=int(n))
+
+    def close(self):
+        if self._p.value:
+            self.array = None
+            lib().xfg_pinned_free(self._p)
+            self._p = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def build_info() -> str:
