@@ -232,7 +232,7 @@ def run_gpu_arm(args, world, rank, local):
     # ---- end to end through the public API with host buffers -----------------------------------
     E = 5
     host = PinnedArray(U0.size)
-    host.array[:] = U0
+    host.array[:] = U0.reshape(-1)
     e2e_steps = max(1, min(args.steps, 3))
     f2, _, _ = setup(0)
     f2.advance(1)
