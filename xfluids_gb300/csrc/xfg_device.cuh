@@ -18,6 +18,14 @@
 #define XFG_KNS fast
 #endif
 
+// Units compiled with -DXFG_STRICT (and --fmad=false) keep the reference's operation sequence
+// everywhere; the others may use the rearranged single-gas FP64 fast path.
+#ifdef XFG_STRICT
+#define XFG_STRICT_BUILD 1
+#else
+#define XFG_STRICT_BUILD 0
+#endif
+
 namespace xfg {
 
 constexpr double kRu = 6.02214076e26 * 1.380649e-23 * 1.0E-3;  // global_setup.h:48-54
@@ -61,6 +69,8 @@ struct DevFields {
     float *Uf, *Ff[3];         // FP32 copies of U and of the physical fluxes (mixed form)
     float *primf;              // FP32 rho, u, v, w, H, p, c (7 components, mixed form)
     float *Fwf[3];             // FP32 face fluxes (mixed form)
+    double *sr, *isr;          // sqrt(rho) and 1/sqrt(rho) per cell (single-gas FP64 fast path)
+    double *eab[3];            // |u_d - c|, |u_d|, |u_d + c| per cell and direction (same path)
     unsigned long long *lam;   // dt wave-speed maxima (3 x bit patterns of non-negative doubles)
     double *dtbuf;             // [0] dt of the step, [1] time, [2] target time, [3] steps done
     int *err;                  // error words: [0] state NaN code, [1] primitive error, [2] i, [3] j, [4] k
@@ -71,6 +81,7 @@ template <class T, int NS>
 struct FaceStateT {
     T _u, _v, _w, _H, _P, _rho, D, D1;
     T c2, b1, b3, q2, _c, b2, _c1;
+    T ent0;  // (1 - b2 - b3) / b1, column 0 of the entropy row of L
     T z[NS > 1 ? NS - 1 : 1];
     T _yi[NS];
 };
@@ -80,6 +91,27 @@ using FaceState = FaceStateT<double, NS>;
 // Device code lives in a namespace per translation unit (XFG_KNS) so that the same template
 // compiled with different floating-point contraction flags in two units stays two kernels.
 namespace XFG_KNS {
+
+// Reciprocal and inverse square root for the single-gas FP64 fast path: the hardware
+// approximation refined by two Newton-Raphson steps (r <- r (2 - x r); y <- y (1.5 - x y^2 / 2)),
+// within a few ulp of the correctly rounded value for normal finite x.
+__device__ __forceinline__ double rcp_nr(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    double e = fma(-x, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-x, r, 1.0);
+    return fma(r, e, r);
+}
+__device__ __forceinline__ double rsqrt_nr(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double h = 0.5 * x;
+    double e = fma(-h * y, y, 0.5);
+    y = fma(y, e, y);
+    e = fma(-h * y, y, 0.5);
+    return fma(y, e, y);
+}
 
 // ---------------------------------------------------------------------------------------------
 // Thermodynamics, src/solver_Ini/Thermo_device.h
@@ -227,7 +259,7 @@ __device__ __forceinline__ T left_val(const FaceStateT<T, NS> &F, int n, int k) 
     }
     if (n >= 1 && n <= 3) {
         if (n == D + 1) {
-            if (k == 0) return (T(1.0) - b2 - b3) / b1;
+            if (k == 0) return F.ent0;
             if (k >= 1 && k <= 3) return vel[k - 1];
             return F.z[k - 5];
         }
@@ -293,6 +325,35 @@ __device__ __forceinline__ double weno5_body(double v1, double v2, double v3, do
     s3 = a3 * (2.0 * v3 + 5.0 * v4 - v5);
     return (s1 + s2 + s3);
 }
+// FP64 fast form of the body: the same smoothness indicators, weights and candidates arranged for
+// fused multiply-adds; returns the weighted candidate sum and the weight sum separately (the
+// caller normalises both sides of a face with one reciprocal each).
+__device__ __forceinline__ void weno5_body_nd(double v1, double v2, double v3, double v4, double v5, double &num,
+                                              double &den) {
+    double a = fma(-2.0, v2, v1) + v3;
+    double b = fma(3.0, v3, fma(-4.0, v2, v1));
+    const double s1 = fma(13.0 * a, a, fma(3.0 * b, b, 1.0E-6));
+    a = fma(-2.0, v3, v2) + v4;
+    b = v2 - v4;
+    const double s2 = fma(13.0 * a, a, fma(3.0 * b, b, 1.0E-6));
+    a = fma(-2.0, v4, v3) + v5;
+    b = fma(-4.0, v4, 3.0 * v3) + v5;
+    const double s3 = fma(13.0 * a, a, fma(3.0 * b, b, 1.0E-6));
+    const double p23 = s2 * s3, p13 = s1 * s3, p12 = s1 * s2;
+    const double a1 = 0.1 * p23 * p23, a2 = 0.6 * p13 * p13, a3 = 0.3 * p12 * p12;
+    const double q1 = fma(11.0, v3, fma(-7.0, v2, 2.0 * v1));
+    const double q2 = fma(2.0, v4, fma(5.0, v3, -v2));
+    const double q3 = fma(5.0, v4, fma(2.0, v3, -v5));
+    num = fma(a3, q3, fma(a2, q2, a1 * q1));
+    den = a1 + a2 + a3;
+}
+__device__ __forceinline__ double weno5_fast(const double *pp, const double *mm) {
+    double nf, df, nm, dm;
+    weno5_body_nd(pp[1], pp[2], pp[3], pp[4], pp[5], nf, df);
+    weno5_body_nd(mm[6], mm[5], mm[4], mm[3], mm[2], nm, dm);
+    return fma(nf, rcp_nr(df), nm * rcp_nr(dm)) * kSix;
+}
+
 // FP32 form: the same candidates and smoothness indicators; the weights use the division form
 // d_k / s_k^2 (equal to the product form) so that s^4 cannot overflow single precision.
 __device__ __forceinline__ float weno5_body(float v1, float v2, float v3, float v4, float v5) {

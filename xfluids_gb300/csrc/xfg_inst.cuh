@@ -45,10 +45,12 @@ struct Inst {
         const Geo &g = c.g;
         long long n = (long long)(g.Xi + (D == 0)) * (g.Yi + (D == 1)) * (g.Zi + (D == 2));
         const double *glf = c.glf ? c.glf + 3 * D : nullptr;
+        (void)n;
+        const dim3 grid = face_grid<D>(g), block(32, 4, 1);
         if (MIXED)
-            k_faces_mixed<D, COP, NS, ORDER><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, c.artificial, glf, guard);
+            k_faces_mixed<D, COP, NS, ORDER><<<grid, block, 0, c.st>>>(g, c.f, c.th, c.artificial, glf, guard);
         else
-            k_faces<D, COP, NS, ORDER><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, UI, c.artificial, glf, guard);
+            k_faces<D, COP, NS, ORDER><<<grid, block, 0, c.st>>>(g, c.f, c.th, UI, c.artificial, glf, guard);
     }
     template <int ORDER>
     static void faces(const LaunchCtx &c, int d, const double *UI, int guard) {

@@ -155,6 +155,20 @@ __global__ void __launch_bounds__(kThreads) k_states(Geo g, DevFields f, DevTher
         const double c = sqrt(gamma * p * rho1);
         f.rho[id] = rho, f.u[id] = u, f.v[id] = v, f.w[id] = w, f.p[id] = p, f.H[id] = H, f.c[id] = c;
         f.e[id] = tme, f.gamma[id] = gamma;
+        if (!COP && !XFG_STRICT_BUILD && f.sr) {  // inputs of the single-gas fast face kernel
+            const double isr = rsqrt_nr(rho);
+            f.isr[id] = isr;
+            f.sr[id] = rho * isr;
+            const double vel[3] = {u, v, w};
+            const int dims[3] = {g.dimx, g.dimy, g.dimz};
+#pragma unroll
+            for (int d = 0; d < 3; d++)
+                if (dims[d]) {
+                    f.eab[d][id] = fabs(vel[d] - c);
+                    f.eab[d][P + id] = fabs(vel[d]);
+                    f.eab[d][2 * P + id] = fabs(vel[d] + c);
+                }
+        }
         if (COP) {
             f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
 #pragma unroll
@@ -360,6 +374,35 @@ __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, con
     F._c = sqrt(F.c2);
     F.b2 = 1.0 + F.b1 * F.q2 - F.b1 * F._H;
     F._c1 = 1.0 / F._c;
+    F.ent0 = (1.0 - F.b2 - F.b3) / F.b1;
+}
+
+// Single-gas Roe state of the FP64 fast path from the per-cell sqrt(rho) and 1/sqrt(rho):
+// D = sqrt(rho_r/rho_l), the Roe weights, sqrt(rho_r rho_l), c^2 = gamma P/rho and the
+// MARCO_PREEIGEN quantities with reciprocals instead of divisions (mathematically the same state).
+__device__ __forceinline__ void face_state_fast(const DevFields &f, const DevThermo &th, long long l, long long r,
+                                                FaceState<1> &F) {
+    const double srl = __ldg(f.sr + l), srr = __ldg(f.sr + r);
+    const double iS = rcp_nr(srl + srr);
+    const double wl = srl * iS, wr = srr * iS;
+    F._u = fma(wl, __ldg(f.u + l), wr * __ldg(f.u + r));
+    F._v = fma(wl, __ldg(f.v + l), wr * __ldg(f.v + r));
+    F._w = fma(wl, __ldg(f.w + l), wr * __ldg(f.w + r));
+    F._H = fma(wl, __ldg(f.H + l), wr * __ldg(f.H + r));
+    F._P = fma(wl, __ldg(f.p + l), wr * __ldg(f.p + r));
+    F._rho = srl * srr;
+    const double irho = __ldg(f.isr + l) * __ldg(f.isr + r);
+    const double g = th.ncop_gamma;
+    const double gP = g * F._P;
+    F.c2 = gP * irho;
+    F.b1 = ((g - 1.0) * F._rho) * rcp_nr(gP);
+    F.b3 = 0.0;
+    F._yi[0] = 1.0;
+    F.q2 = fma(F._u, F._u, fma(F._v, F._v, F._w * F._w));
+    F._c1 = rsqrt_nr(F.c2);
+    F._c = F.c2 * F._c1;
+    F.b2 = fma(F.b1, F.q2 - F._H, 1.0);
+    F.ent0 = (1.0 - F.b2) * (F.c2 * (1.0 / (g - 1.0)));
 }
 
 // Projection of the E components of cell q onto row n of L (kinds fold at compile time).
@@ -380,6 +423,28 @@ __device__ __forceinline__ double project(const double *lrow, int n, const doubl
     return acc;
 }
 
+// Face (i+1/2) of direction D handled by this thread. Blocks are 32 x 4 threads: 32 faces along x
+// and 4 along y (D = 0, 1) or z (D = 2), so the rows of a y or z stencil are shared in L1 by the
+// warps of a block. Returns false outside the face range.
+template <int D>
+__device__ __forceinline__ bool face_of_thread(const Geo &g, int &i, int &j, int &k) {
+    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
+    const int fi = blockIdx.x * 32 + threadIdx.x;
+    const int fj = D == 2 ? (int)blockIdx.y : (int)(blockIdx.y * 4 + threadIdx.y);
+    const int fk = D == 2 ? (int)(blockIdx.z * 4 + threadIdx.y) : (int)blockIdx.z;
+    if (fi >= nfx || fj >= nfy || fk >= nfz) return false;
+    i = fi + g.Bx - (D == 0 ? 1 : 0);
+    j = fj + g.By - (D == 1 ? 1 : 0);
+    k = fk + g.Bz - (D == 2 ? 1 : 0);
+    return true;
+}
+template <int D>
+inline dim3 face_grid(const Geo &g) {
+    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
+    if (D == 2) return dim3((nfx + 31) / 32, nfy, (nfz + 3) / 4);
+    return dim3((nfx + 31) / 32, (nfy + 3) / 4, nfz);
+}
+
 template <int D, bool COP, int NS, int ORDER>
 __global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevThermo th, const double *__restrict__ UI,
                                                     int artificial, const double *__restrict__ glf_d, int guard) {
@@ -387,20 +452,24 @@ __global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevTherm
     constexpr int E = S::E;
     if (guard && step_done(f)) return;
     const long long P = g.pitch;
-    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)nfx * nfy * nfz) return;
-    const int i = (int)(t % nfx) + g.Bx - (D == 0 ? 1 : 0);
-    const long long r = t / nfx;
-    const int j = (int)(r % nfy) + g.By - (D == 1 ? 1 : 0);
-    const int k = (int)(r / nfy) + g.Bz - (D == 2 ? 1 : 0);
+    int i, j, k;
+    if (!face_of_thread<D>(g, i, j, k)) return;
     const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
     const long long idl = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long idr = idl + stride;
 
+    // single-gas FP64 fast path (not in the strict units): per-cell sqrt(rho), 1/sqrt(rho) and
+    // |lambda| arrays written by k_states, reciprocal-based Roe state, FMA-form WENO5
+    // (a handle without those arrays gets the general form)
+    constexpr bool FAST_BUILD = !COP && !XFG_STRICT_BUILD;
+    const bool FAST = FAST_BUILD && f.sr && f.isr && f.eab[D];
     FaceState<NS> F;
     double Gamma0;
-    face_state<COP, NS>(g, f, th, idl, idr, F, Gamma0);
+    if (FAST_BUILD && FAST) {
+        face_state_fast(f, th, idl, idr, *reinterpret_cast<FaceState<1> *>(&F));
+    } else {
+        face_state<COP, NS>(g, f, th, idl, idr, F, Gamma0);
+    }
     const double un = D == 0 ? F._u : (D == 1 ? F._v : F._w);
     const double *__restrict__ Fl = f.F[D];
     const double *__restrict__ vd = D == 0 ? f.u : (D == 1 ? f.v : f.w);
@@ -408,13 +477,24 @@ __global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevTherm
     // LLF window maxima of |u_d - c|, |u_d|, |u_d + c| over m = -2..3 (WENO5)
     double lm0 = 0.0, lm1 = 0.0, lm2 = 0.0;
     if (ORDER == 5 && artificial == XFG_LLF) {
+        if (FAST_BUILD && FAST) {
+            const double *__restrict__ ea = f.eab[D];
 #pragma unroll
-        for (int m = -2; m <= 3; m++) {
-            const long long q = idl + m * stride;
-            const double ud = __ldg(vd + q), cc = __ldg(f.c + q);
-            lm0 = fmax(lm0, fabs(ud - cc));
-            lm1 = fmax(lm1, fabs(ud));
-            lm2 = fmax(lm2, fabs(ud + cc));
+            for (int m = -2; m <= 3; m++) {
+                const long long q = idl + m * stride;
+                lm0 = fmax(lm0, __ldg(ea + q));
+                lm1 = fmax(lm1, __ldg(ea + P + q));
+                lm2 = fmax(lm2, __ldg(ea + 2 * P + q));
+            }
+        } else {
+#pragma unroll
+            for (int m = -2; m <= 3; m++) {
+                const long long q = idl + m * stride;
+                const double ud = __ldg(vd + q), cc = __ldg(f.c + q);
+                lm0 = fmax(lm0, fabs(ud - cc));
+                lm1 = fmax(lm1, fabs(ud));
+                lm2 = fmax(lm2, fabs(ud + cc));
+            }
         }
     }
     constexpr int M0 = ORDER == 7 ? -3 : -2, M1 = ORDER == 7 ? 4 : 3;
@@ -443,7 +523,7 @@ __global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevTherm
             pp[m + 3] = 0.5 * (ff + av * uf);
             mm[m + 3] = 0.5 * (ff - av * uf);
         }
-        const double fl = ORDER == 7 ? weno7(pp, mm) : weno5(pp, mm);
+        const double fl = ORDER == 7 ? weno7(pp, mm) : (FAST_BUILD ? weno5_fast(pp, mm) : weno5(pp, mm));
 #pragma unroll
         for (int kk = 0; kk < E; kk++) {
             const int kind = right_kind(D, E, n, kk);

@@ -155,6 +155,21 @@ __device__ __forceinline__ float project_f(const float *lrow, int n, const float
     return acc;
 }
 
+template <int D, int E>
+__device__ __forceinline__ float project_r(const float *lrow, int n, const float *x) {
+    float acc = 0.f;
+    bool first = true;
+#pragma unroll
+    for (int k = 0; k < E; k++) {
+        const int kind = left_kind(D, E, n, k);
+        if (kind == 0) continue;
+        float t = kind == 1 ? x[k] : (kind == 2 ? -x[k] : x[k] * lrow[k]);
+        acc = first ? t : acc + t;
+        first = false;
+    }
+    return acc;
+}
+
 // FP32 characteristic WENO flux at face (i+1/2) of direction D (same structure as k_faces).
 template <int D, bool COP, int NS, int ORDER>
 __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, DevThermo th, int artificial,
@@ -163,13 +178,8 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
     constexpr int E = S::E;
     if (guard && step_done(f)) return;
     const long long P = g.pitch;
-    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (long long)nfx * nfy * nfz) return;
-    const int i = (int)(t % nfx) + g.Bx - (D == 0 ? 1 : 0);
-    const long long r = t / nfx;
-    const int j = (int)(r % nfy) + g.By - (D == 1 ? 1 : 0);
-    const int k = (int)(r / nfy) + g.Bz - (D == 2 ? 1 : 0);
+    int i, j, k;
+    if (!face_of_thread<D>(g, i, j, k)) return;
     const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
     const long long idl = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long idr = idl + stride;
@@ -195,6 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
         F._c = sqrtf(F.c2);
         F.b2 = 1.0f + F.b1 * F.q2 - F.b1 * F._H;
         F._c1 = 1.0f / F._c;
+        F.ent0 = (1.0f - F.b2 - F.b3) / F.b1;
     } else {
         FaceState<NS> Fd;
         double G0;
@@ -202,6 +213,7 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
         F._u = (float)Fd._u, F._v = (float)Fd._v, F._w = (float)Fd._w, F._H = (float)Fd._H;
         F._P = (float)Fd._P, F._rho = (float)Fd._rho, F.c2 = (float)Fd.c2, F.b1 = (float)Fd.b1;
         F.b3 = (float)Fd.b3, F.q2 = (float)Fd.q2, F._c = (float)Fd._c, F.b2 = (float)Fd.b2, F._c1 = (float)Fd._c1;
+        F.ent0 = (float)Fd.ent0;
 #pragma unroll
         for (int s = 0; s < NS; s++) F._yi[s] = (float)Fd._yi[s];
 #pragma unroll
@@ -224,6 +236,19 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
         }
     }
     constexpr int M0 = ORDER == 7 ? -3 : -2, M1 = ORDER == 7 ? 4 : 3;
+    constexpr int NP = M1 - M0 + 1;
+    // single gas: every stencil value is loaded once into registers and projected on all fields;
+    // mixtures (larger E) re-read the stencil from L1 per field to bound register use
+    constexpr bool PRELOAD = E <= 6;
+    float Us[PRELOAD ? NP : 1][PRELOAD ? E : 1], Fs[PRELOAD ? NP : 1][PRELOAD ? E : 1];
+    if constexpr (PRELOAD) {
+#pragma unroll
+        for (int m = 0; m < NP; m++) {
+            const long long q = idl + (m + M0) * stride;
+#pragma unroll
+            for (int kk = 0; kk < E; kk++) Us[m][kk] = __ldg(Ua + kk * P + q), Fs[m][kk] = __ldg(Fl + kk * P + q);
+        }
+    }
     float acc[E];
 #pragma unroll
     for (int n = 0; n < E; n++) {
@@ -243,9 +268,15 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
         float pp[8], mm[8];
 #pragma unroll
         for (int m = M0; m <= M1; m++) {
-            const long long q = idl + m * stride;
-            const float uf = project_f<D, E>(lrow, n, Ua, P, q);
-            const float ff = project_f<D, E>(lrow, n, Fl, P, q);
+            float uf, ff;
+            if constexpr (PRELOAD) {
+                uf = project_r<D, E>(lrow, n, Us[m - M0]);
+                ff = project_r<D, E>(lrow, n, Fs[m - M0]);
+            } else {
+                const long long q = idl + m * stride;
+                uf = project_f<D, E>(lrow, n, Ua, P, q);
+                ff = project_f<D, E>(lrow, n, Fl, P, q);
+            }
             pp[m + 3] = 0.5f * (ff + av * uf);
             mm[m + 3] = 0.5f * (ff - av * uf);
         }
