@@ -194,6 +194,29 @@ int xfg_device_array(xfg_handle *h, int which, double **ptr, size_t *pitch);
  * out[1] = FP32, out[2] = SM clock (MHz) reported by the driver during the run (0 if unknown). */
 int xfg_measure_pipe_peaks(int device, double *out);
 
+/* Right-hand side of one state without any device allocation.
+ *
+ * No counterpart in the reference. For callers that cannot allocate device memory (a host
+ * application or plugin host that owns every allocation or forbids the driver allocator, a
+ * real-time loop where an allocation and its implicit synchronisation are not allowed): the caller
+ * passes device pointers to the state U (reference AoS layout, all cells), to the temperature T
+ * (Newton warm start, Xmax*Ymax*Zmax doubles; required for a mixture, may be NULL otherwise) and to
+ * the output LU (AoS, Emax per cell; inner cells are written, ghost cells are 0). The function
+ * applies the boundary conditions to its own copy of U, recovers the primitives and computes LU
+ * as xfg_boundary + xfg_update_states + xfg_compute_lu do, on `stream` (a cudaStream_t, 0 = legacy
+ * default stream), without synchronising. FP64 forms only (precision XFG_FP64 or XFG_FP64_STRICT).
+ *
+ * Every intermediate array lives in one file-scope device array of XFG_NOALLOC_MAX_SCRATCH_BYTES,
+ * which every GPU that loads the library holds until the process exits; blocks that need more are
+ * rejected with a status < 0 and a message in xfg_last_error(). The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress) with that device current: make it before
+ * any stream capture. All calls share the array, which keeps the previous call's contents (the
+ * words that must start at zero are cleared by each call): calls that overlap on the GPU, on
+ * different streams or from different host threads, race and must be serialised by the caller. */
+#define XFG_NOALLOC_MAX_SCRATCH_BYTES (64u << 20)
+int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *scheme, const xfg_thermal *thermal,
+                           const double *U_aos, const double *T, double *LU_aos, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -133,6 +133,7 @@ def lib():
         "xfg_launches_per_step": [P, pi],
         "xfg_pinned_alloc": [C.c_size_t, C.POINTER(P)],
         "xfg_pinned_free": [P],
+        "xfg_compute_lu_noalloc": [C.POINTER(Block), C.POINTER(Scheme), C.POINTER(Thermal), P, P, P, P],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

@@ -43,6 +43,7 @@ static int fail(int code, const char *fmt, ...) {
 // launcher registry
 // ---------------------------------------------------------------------------------------------
 namespace xfg {
+void set_last_error(const char *msg) { g_err = msg; }
 static std::vector<const Ops *> &registry() {
     static std::vector<const Ops *> r;
     return r;

@@ -35,6 +35,9 @@ struct Ops {
     void (*estimate_nan)(const LaunchCtx &, const double *UI, int *pos);
 };
 
+// Message returned by xfg_last_error() on this host thread.
+void set_last_error(const char *msg);
+
 // Registry filled by the instantiation units.
 const Ops *find_ops(int cop, int ns, int order, int precision);
 void register_ops(const Ops *ops);
