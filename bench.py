@@ -186,6 +186,82 @@ def run_reference_arm(args, world, rank):
     return 0
 
 
+TUNE_PAD_STEPS = 12  # steps of the schedule search, padded (the full search has 11 trials)
+
+
+def bench_ensemble(args, local, members, scheme, precision):
+    """Batched ensemble (256 independent 2D four-quadrant Riemann problems, N per side
+    round(2^U[7,10]), WENO5 LLF, CFL 0.45): warm-up steps (graph capture), then args.steps fused
+    steps of all members timed with CUDA events on the ensemble's stream."""
+    from xfluids_gb300 import autotune
+    from xfluids_gb300.ensemble import Ensemble
+    scheme.precision = precision
+    pool = sum(Ensemble.member_bytes(b, precision) for b, _ in members) + 4096 * len(members)
+    e = Ensemble(scheme, capacity=len(members), pool_bytes=pool, device=local)
+    try:
+        slots = [e.add(b, U, 0.25) for b, U in members]
+        assert None not in slots
+        e.advance(args.warmup)
+        # schedule search on the live ensemble (bit-identical results under every schedule); the
+        # FP64 search is shorter, its steps cost ~15x more
+        space = None if precision else [("tile_2d_large", [5, 6, 7]), ("tile_2d_small", [5, 6, 4]),
+                                         ("fused_faces", [0, 1])]
+        sched, rep = autotune.tune(e, steps=1, space=space, use_cache=False)
+        if len(rep["trials"]) < TUNE_PAD_STEPS:  # both precisions reach the same step count
+            e.advance(TUNE_PAD_STEPS - len(rep["trials"]))
+        before = [e.status(q)["steps"] for q in slots]
+        st, ms = e.advance(args.steps)
+        info = [e.status(q) for q in slots]
+        states = [e.get_state(q) for q in slots]
+    finally:
+        e.close()
+    # cell-updates actually performed: a member stopped by a numerical error (no positivity
+    # limiter on these states) does no further steps
+    work = sum(b.X_inner * b.Y_inner * (i["steps"] - s0) for (b, _), i, s0 in zip(members, info, before))
+    failed = [q for q, i in enumerate(info) if i["error"]]
+    return {"value": work / (ms * 1e-3), "ms": ms, "cell_updates": work, "status": st,
+            "failed_members": failed, "schedule": sched, "tuning_trials": len(rep["trials"]),
+            "tuned_ms_per_step": [round(t[1], 3) for t in rep["trials"]]}, states
+
+
+def bench_serving(local, count, precision, fp64_check_work=3e8):
+    """Continuous-batching server on the first `count` requests of the seeded Poisson trace
+    (mean 200 req/s, 1D and 2D Riemann solves, N per side round(2^U[8,11]), t_end U[0.1,0.3]);
+    the smaller results are re-solved alone in FP64 for the error of the served precision."""
+    from xfluids_gb300.fluid import Fluid
+    from xfluids_gb300.mesh import empty_thermal
+    from xfluids_gb300.serve import Server, poisson_trace, serving_scheme, summary
+    warm = poisson_trace(2, seed=99, lo=6.0, hi=7.0, t_lo=0.01, t_hi=0.02)
+    trace = poisson_trace(count, seed=0)
+    srv = Server(precision, hbm_budget=48 << 30, capacity=64, chunk=16, device=local)
+    try:
+        srv.run(warm, realtime=False)
+        srv.device_ms = 0.0
+        srv.run(trace, realtime=True)
+        out = summary(trace, device_ms=srv.device_ms)
+    finally:
+        srv.close()
+    l1 = []
+    sc = serving_scheme(0)
+    for r in trace:
+        if r.cells * r.steps > fp64_check_work:
+            continue
+        f = Fluid(r.block, sc, empty_thermal(), device=local)
+        f.InitialU(r.U)
+        f.initialize()
+        t = 0.0
+        while t < r.t_end:
+            _, t, _ = f.advance(256, r.t_end)
+        ref = f.get("U").reshape(r.block.Zmax, r.block.Ymax, r.block.Xmax, 5)[r.block.inner_slices()]
+        got = r.result.reshape(r.block.Zmax, r.block.Ymax, r.block.Xmax, 5)[r.block.inner_slices()]
+        l1.append(float(np.abs(got - ref).mean()))
+        f.close()
+    out.update({"requests_checked_vs_fp64": len(l1), "l1_vs_fp64_max": max(l1) if l1 else None,
+                "trace": f"first {count} requests, Poisson mean 200 req/s, seed 0",
+                "sizes": [f"{r.kind}:{r.n}" for r in trace]})
+    return out
+
+
 def run_gpu_arm(args, world, rank, local):
     from xfluids_gb300 import cases
     from xfluids_gb300.abi import MIXED
@@ -268,6 +344,28 @@ def run_gpu_arm(args, world, rank, local):
     mixed_face_ms = phases_m["faces_x"] / 3.0
     fm.close()
     f.close()
+
+    # ---- batched ensemble, FP64 and mixed, and the serving trace -----------------------------
+    ens = {}
+    if args.ensemble:
+        scheme_e, members = cases.riemann_ensemble(256, seed=0)
+        e64, s64 = bench_ensemble(args, local, members, scheme_e, 0)
+        emx, smx = bench_ensemble(args, local, members, scheme_e, MIXED)
+        bad = set(e64["failed_members"]) | set(emx["failed_members"])
+        diff = [np.abs(a - b_).reshape(members[q][0].Zmax, members[q][0].Ymax, members[q][0].Xmax, 5)[
+                    members[q][0].inner_slices()].reshape(-1, 5)
+                for q, (a, b_) in enumerate(zip(smx, s64)) if q not in bad]
+        ncell_all = sum(x.shape[0] for x in diff)
+        ens = {"workload": "256 independent 2D four-quadrant Riemann problems, N per side round(2^U[7,10]) (seed 0), "
+                           "WENO5-JS LLF, SSP-RK3, CFL 0.45, one batched launch per phase, CUDA-graph replay",
+               "cells": sum(b.X_inner * b.Y_inner for b, _ in members), "steps": args.steps,
+               "fp64": e64, "mixed": emx, "members_compared": len(diff),
+               "mixed_speedup_vs_fp64": emx["value"] / e64["value"],
+               "mixed_speedup_vs_plain_fp64_vortex": emx["value"] / value,
+               "l1_mixed_vs_fp64": float(sum(x.sum() for x in diff) / (ncell_all * 5)),
+               "linf_mixed_vs_fp64": float(max(x.max() for x in diff))}
+        del s64, smx, diff
+    serving = bench_serving(local, args.serve_requests, MIXED) if args.serve_requests > 0 else None
     d.close()
     if rank != 0:
         return 0
@@ -298,6 +396,8 @@ def run_gpu_arm(args, world, rank, local):
                   "steps": km, "l1_vs_fp64": l1, "linf_vs_fp64": linf, "t": tm,
                   "faces_x_launch_ms": mixed_face_ms, "phases_ms_per_step": phases_m,
                   "fp32_peak_tflops": peaks["fp32_flops"] / 1e12},
+        "ensemble": ens or None,
+        "serving": serving,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-updates/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_steps} steps of the 1024^2 vortex ({cpu_el:.1f} s) on the oracle restatement"},
         "clocks": clk.summary(),
@@ -315,6 +415,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=4096)
+    ap.add_argument("--ensemble", type=int, default=1, help="run the 256-member batched ensemble (0 = skip)")
+    ap.add_argument("--serve-requests", type=int, default=8, help="requests of the serving trace (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()

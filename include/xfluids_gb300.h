@@ -194,6 +194,71 @@ int xfg_device_array(xfg_handle *h, int which, double **ptr, size_t *pitch);
  * out[1] = FP32, out[2] = SM clock (MHz) reported by the driver during the run (0 if unknown). */
 int xfg_measure_pipe_peaks(int device, double *out);
 
+/* ------------------------------------------------------------------------------------------
+ * Ensemble of independent single-gas grids (batched ensemble, request serving).
+ * No single counterpart in the reference, which advances one block per process: the members are
+ * XFLUIDS runs of the same scheme (each member's step is XFLUIDS::Evolution's loop body with its
+ * own dt and target time, src/XFLUIDS.cpp:172-214), advanced together by batched kernels.
+ * ------------------------------------------------------------------------------------------ */
+typedef struct xfg_ensemble xfg_ensemble;
+
+/* Create an ensemble with `capacity` member slots and a device pool of pool_bytes from which the
+ * members are sub-allocated (admission by HBM budget). scheme: single gas (cop = 0), ROE or LLF,
+ * WENO5/7, precision XFG_FP64 or XFG_MIXED. */
+int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *scheme, const xfg_thermal *thermal,
+                        int device, xfg_ensemble **out);
+int xfg_ensemble_destroy(xfg_ensemble *e);
+
+/* Device bytes one member of this block takes from the pool. */
+size_t xfg_ensemble_member_bytes(const xfg_block *block, int precision);
+
+/* Admit a member: state U (AoS, host or device), target time; runs BoundaryCondition(U) and
+ * UpdateStates(U) for it (main.cpp:45-47). Returns 0 and *slot, 1 when no slot is free, 2 when the
+ * pool has no room (the caller retries after members leave). */
+int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_aos, double target_t, int *slot);
+
+/* Release a member's slot and pool memory. */
+int xfg_ensemble_remove(xfg_ensemble *e, int slot);
+
+/* nsteps fused steps of every active member (members past their target time do nothing),
+ * replayed from a CUDA graph when use_graph (the graph is re-captured after membership changes).
+ * A member whose step produced an error (the codes of xfg_step) stops at that step; the others go
+ * on. Synchronises once; *device_ms (may be NULL) receives the device time of the steps. Returns
+ * 0, or the worst error code among the active members (10000 state NaN / negative density, 1
+ * primitive error), or < 0 on a CUDA or argument error. */
+int xfg_ensemble_advance(xfg_ensemble *e, int nsteps, int use_graph, float *device_ms);
+
+/* Time, step count and done flag (also set for a member stopped by an error) of a member as of
+ * the last advance; returns its error code (0, 1 or 10000 as xfg_step). */
+int xfg_ensemble_status(xfg_ensemble *e, int slot, double *t, int *steps, int *done);
+
+/* Copy a member's state U out (AoS, host or device pointer). */
+int xfg_ensemble_get_state(xfg_ensemble *e, int slot, double *U_aos);
+
+/* Launch schedule of the batched step (the autotuner's knobs). None changes the operations of a
+ * step: FP64 results are bit-identical under every schedule, mixed-precision results agree to FP32
+ * rounding (FMA contraction of FP32 expressions may differ between kernel forms).
+ *   XFG_ENS_LARGEST_FIRST  members in the launch tables largest first (1, default) or by slot (0)
+ *   XFG_ENS_FUSED_FACES    all face sweeps of a stage in one launch (1) or one launch each (0, default)
+ *   XFG_ENS_GRAPH_STEPS    fused steps per captured CUDA graph, 1..64 (default 1)
+ *   XFG_ENS_TILE_1D..3D    face tile of a size class (1D; 2D below 384 cells per side; 2D from 384;
+ *                          3D): log2 of its x extent, 3..7, the tile being 2^v x 128/2^v faces
+ *                          (defaults 7, 5, 5, 5) */
+enum {
+    XFG_ENS_LARGEST_FIRST = 0,
+    XFG_ENS_FUSED_FACES = 1,
+    XFG_ENS_GRAPH_STEPS = 2,
+    XFG_ENS_TILE_1D = 3,
+    XFG_ENS_TILE_2D_SMALL = 4,
+    XFG_ENS_TILE_2D_LARGE = 5,
+    XFG_ENS_TILE_3D = 6
+};
+int xfg_ensemble_set_option(xfg_ensemble *e, int option, int value);
+int xfg_ensemble_get_option(xfg_ensemble *e, int option, int *value);
+
+size_t xfg_ensemble_free_bytes(xfg_ensemble *e);
+int xfg_ensemble_active(xfg_ensemble *e);
+
 /* Right-hand side of one state without any device allocation.
  *
  * No counterpart in the reference. For callers that cannot allocate device memory (a host

@@ -74,3 +74,14 @@ def test_create_rejects_bad_arguments(cuda_lib):
     b.Bwidth_X = 2
     rc = cuda_lib.xfg_create(C.byref(b), C.byref(s), C.byref(th), 0, C.byref(h))
     assert rc == -1 and "Bwidth" in cuda_lib.xfg_last_error().decode()
+
+
+def test_ensemble_rejects_unsupported_schemes_before_touching_a_device(cuda_lib):
+    """xfg_ensemble_create checks the scheme first (no device call is made for these)."""
+    from xfluids_gb300.ensemble import Ensemble
+    from xfluids_gb300.mesh import make_scheme
+    for kw in (dict(cop=True, num_species=2), dict(artificial_type=abi.GLF), dict(precision=2),
+               dict(scheme_order=6)):
+        sc = make_scheme(**{"scheme_order": 5, "artificial_type": abi.LLF, **kw})
+        with pytest.raises(abi.XfgError):
+            Ensemble(sc, capacity=2, pool_bytes=1 << 20)

@@ -1,0 +1,226 @@
+"""Batched ensemble engine (xfg_ensemble_*, xfluids_gb300/ensemble.py).
+
+Every member advanced inside the ensemble must equal the same grid advanced alone through the
+single-grid path (Fluid.advance, itself parity-checked against the oracle): same number of steps,
+same time, same state within the FP64 parity bound. Also: graph replay equals direct launches
+bit for bit, members stop at their own target time, admission by slot and pool budget, slot reuse.
+"""
+import numpy as np
+import pytest
+
+from helpers import PARITY_TOL, blast3d, normwise, riemann_small, sod_like
+from xfluids_gb300 import cases
+from xfluids_gb300.abi import LLF, PERIODIC, ROE
+from xfluids_gb300.ensemble import Ensemble
+from xfluids_gb300.fluid import Fluid
+from xfluids_gb300.mesh import empty_thermal, make_scheme
+
+pytestmark = pytest.mark.gpu
+
+FP64, MIXED = 0, 1
+# mixed-precision members against the mixed single-grid path: the same FP32 expressions compiled
+# into other kernels may contract differently into FMAs, so the two agree to FP32 rounding only
+# (dt, and hence t, to about 1e-7 relative); bounds for state (normwise) and time:
+MIXED_TOL = 1e-5
+MIXED_T_TOL = 1e-6
+
+
+def members():
+    out = []
+    for mk in (lambda: sod_like(96), lambda: cases.isentropic_vortex(32), lambda: riemann_small(40),
+               lambda: blast3d(), lambda: riemann_small(24, seed=5, bc=PERIODIC)):
+        b, _, _, U, _ = mk()
+        out.append((b, np.ascontiguousarray(U, dtype=np.float64).reshape(-1)))
+    return out
+
+
+def alone(b, U, scheme, nsteps, target=1e300):
+    f = Fluid(b, scheme, empty_thermal())
+    try:
+        f.InitialU(U)
+        f.initialize()
+        st, t, n = f.advance(nsteps, target)
+        assert st == 0
+        return f.get("U").reshape(-1), t, n
+    finally:
+        f.close()
+
+
+def pool_for(blocks, precision, extra=0):
+    return sum(Ensemble.member_bytes(b, precision) for b in blocks) + 4096 * len(blocks) + extra
+
+
+@pytest.mark.parametrize("order,art,prec", [(5, LLF, FP64), (7, ROE, FP64), (5, ROE, FP64), (5, LLF, MIXED),
+                                            (7, LLF, MIXED)])
+def test_members_equal_single_grid_runs(cuda_lib, order, art, prec):
+    scheme = make_scheme(cop=False, scheme_order=order, artificial_type=art, precision=prec)
+    ms = members()
+    nsteps = 6
+    # member 1 stops half way through: its target is half the time the free run reaches
+    _, t_free, _ = alone(ms[1][0], ms[1][1], scheme, nsteps)
+    targets = [1e300] * len(ms)
+    targets[1] = 0.5 * t_free
+    e = Ensemble(scheme, capacity=8, pool_bytes=pool_for([b for b, _ in ms], prec))
+    try:
+        slots = [e.add(b, U, tg) for (b, U), tg in zip(ms, targets)]
+        assert None not in slots and e.active == len(ms)
+        st, dev_ms = e.advance(nsteps)
+        assert st == 0 and dev_ms > 0
+        for (b, U), tg, s in zip(ms, targets, slots):
+            ref, t_ref, n_ref = alone(b, U, scheme, nsteps, tg)
+            info = e.status(s)
+            got = e.get_state(s)
+            assert info["error"] == 0
+            assert info["steps"] == n_ref
+            assert info["t"] == pytest.approx(t_ref, rel=1e-13 if prec == FP64 else MIXED_T_TOL, abs=0)
+            err = normwise(got, ref, 5).max()
+            assert err <= (PARITY_TOL if prec == FP64 else MIXED_TOL), (s, err)
+        assert e.status(slots[1])["done"] and e.status(slots[1])["t"] == pytest.approx(targets[1], rel=1e-15)
+        assert not e.status(slots[0])["done"]
+    finally:
+        e.close()
+
+
+def run_ensemble(scheme, ms, nsteps, use_graph, largest_first=1, chunks=1, **sched):
+    e = Ensemble(scheme, capacity=len(ms), pool_bytes=pool_for([b for b, _ in ms], scheme.precision))
+    try:
+        e.set_option("largest_first", largest_first)
+        e.set_schedule(sched)
+        slots = [e.add(b, U, 1e300) for b, U in ms]
+        for _ in range(chunks):
+            assert e.advance(nsteps // chunks, use_graph=use_graph)[0] == 0
+        return [e.get_state(s) for s in slots], [e.status(s)["t"] for s in slots]
+    finally:
+        e.close()
+
+
+def test_graph_replay_and_launch_order_are_bitwise_neutral(cuda_lib):
+    scheme = make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=FP64)
+    ms = members()
+    direct, t_direct = run_ensemble(scheme, ms, 4, use_graph=False)
+    graph, t_graph = run_ensemble(scheme, ms, 4, use_graph=True, chunks=2)
+    slot_order, t_slot = run_ensemble(scheme, ms, 4, use_graph=True, largest_first=0)
+    for a, b, c in zip(direct, graph, slot_order):
+        assert np.array_equal(a, b) and np.array_equal(a, c)
+    assert t_direct == t_graph == t_slot
+    # face tiles, the fused face launch and multi-step graphs (4 steps = one 3-step graph + 1)
+    for sched in (dict(fused_faces=1), dict(tile_1d=5, tile_2d_small=7, tile_3d=6), dict(tile_2d_small=3, tile_3d=4),
+                  dict(graph_steps=3, fused_faces=1, tile_1d=6, tile_2d_small=4)):
+        other, t_other = run_ensemble(scheme, ms, 4, use_graph=True, **sched)
+        for a, b in zip(direct, other):
+            assert np.array_equal(a, b), sched
+        assert t_other == t_direct
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED])
+def test_autotuner_picks_and_caches_a_schedule(cuda_lib, tmp_path, monkeypatch, prec):
+    from xfluids_gb300 import autotune
+    monkeypatch.setenv("XFG_TUNE_CACHE", str(tmp_path / "sched.json"))
+    scheme = make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=prec)
+    ms = members()
+    e = Ensemble(scheme, capacity=len(ms), pool_bytes=pool_for([b for b, _ in ms], prec))
+    try:
+        slots = [e.add(b, U, 1e300) for b, U in ms]
+        best, rep = autotune.tune(e, steps=1)
+        assert rep["source"] == "search" and len(rep["trials"]) >= 8
+        assert e.schedule() == best
+        steps_tuning = e.status(slots[0])["steps"]
+        assert steps_tuning == len(rep["trials"])      # trials advanced the live ensemble
+        best2, rep2 = autotune.tune(e, steps=1)
+        assert rep2["source"] == "cache" and best2 == best
+        # the tuned run equals the single-grid runs over the same number of steps
+        e.advance(2)
+        for (b, U), s in zip(ms, slots):
+            ref, _, _ = alone(b, U, scheme, steps_tuning + 2)
+            assert normwise(e.get_state(s), ref, 5).max() <= (PARITY_TOL if prec == FP64 else MIXED_TOL)
+    finally:
+        e.close()
+
+
+def test_admission_by_slot_and_pool_budget(cuda_lib):
+    scheme = make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=FP64)
+    ms = members()
+    b0, U0 = ms[2]
+    need = Ensemble.member_bytes(b0, FP64)
+    # pool for one member only
+    e = Ensemble(scheme, capacity=4, pool_bytes=need + 1024)
+    try:
+        s0 = e.add(b0, U0, 1e300)
+        assert s0 is not None
+        assert e.add(b0, U0, 1e300) is None          # no pool memory: admission waits
+        e.remove(s0)
+        assert e.free_bytes == need + 1024
+        s1 = e.add(b0, U0, 1e300)                     # the slot and the memory are reused
+        assert s1 is not None
+        assert e.advance(2)[0] == 0
+        ref, t_ref, _ = alone(b0, U0, scheme, 2)
+        assert normwise(e.get_state(s1), ref, 5).max() <= PARITY_TOL
+    finally:
+        e.close()
+    # capacity: two slots
+    e = Ensemble(scheme, capacity=2, pool_bytes=pool_for([b0] * 3, FP64))
+    try:
+        assert e.add(b0, U0, 1e300) is not None and e.add(b0, U0, 1e300) is not None
+        assert e.add(b0, U0, 1e300) is None           # no free slot
+    finally:
+        e.close()
+
+
+def test_members_join_and_leave_between_advances(cuda_lib):
+    """A member added after others have run equals its own run alone; removing a member does not
+    disturb the others."""
+    scheme = make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=FP64)
+    ms = members()
+    e = Ensemble(scheme, capacity=8, pool_bytes=pool_for([b for b, _ in ms], FP64))
+    try:
+        s = [e.add(*ms[q], 1e300) for q in range(3)]
+        assert e.advance(3)[0] == 0
+        e.remove(s[1])
+        s3 = e.add(*ms[3], 1e300)
+        assert e.advance(2)[0] == 0
+        for slot, q, n in ((s[0], 0, 5), (s[2], 2, 5), (s3, 3, 2)):
+            ref, t_ref, _ = alone(*ms[q], scheme, n)
+            assert e.status(slot)["steps"] == n
+            assert normwise(e.get_state(slot), ref, 5).max() <= PARITY_TOL
+    finally:
+        e.close()
+
+
+
+def failing_member(n=32):
+    """Member 88 of the seeded 256-member Riemann ensemble: the first RK stage of the unlimited
+    characteristic WENO5 drives the density negative (the oracle shows the same at step 0)."""
+    _, rng = cases.ensemble_sizes(256, 0)
+    for _ in range(88):
+        cases.riemann_states(rng)
+    b, _, _, U, _ = cases.riemann2d(n, cases.riemann_states(rng))
+    return b, np.ascontiguousarray(U).reshape(-1)
+
+
+def test_member_with_numerical_error_stops_and_others_go_on(cuda_lib):
+    scheme = make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=FP64)
+    ms = members()[:3]
+    bad = failing_member()
+    e = Ensemble(scheme, capacity=4, pool_bytes=pool_for([b for b, _ in ms] + [bad[0]], FP64))
+    try:
+        slots = [e.add(b, U, 1e300) for b, U in ms]
+        sb = e.add(*bad, 1e300)
+        st, _ = e.advance(4)
+        assert st != 0                                   # worst member code is reported
+        info = e.status(sb)
+        assert info["error"] != 0 and info["done"] and info["steps"] == 1
+        for (b, U), s in zip(ms, slots):
+            ref, _, n_ref = alone(b, U, scheme, 4)
+            assert e.status(s)["error"] == 0 and e.status(s)["steps"] == n_ref == 4
+            assert normwise(e.get_state(s), ref, 5).max() <= PARITY_TOL
+    finally:
+        e.close()
+    # the same grid alone reports the error too
+    f = Fluid(bad[0], scheme, empty_thermal())
+    try:
+        f.InitialU(bad[1])
+        f.initialize()
+        st, _, _ = f.advance(1)
+        assert st != 0
+    finally:
+        f.close()

@@ -135,10 +135,26 @@ def lib():
         "xfg_pinned_free": [P],
         "xfg_compute_lu_noalloc": [C.POINTER(Block), C.POINTER(Scheme), C.POINTER(Thermal), P, P, P, P],
     }
+    sig.update({
+        "xfg_ensemble_create": [I, C.c_size_t, C.POINTER(Scheme), C.POINTER(Thermal), I, C.POINTER(P)],
+        "xfg_ensemble_destroy": [P],
+        "xfg_ensemble_add": [P, C.POINTER(Block), P, D, pi],
+        "xfg_ensemble_remove": [P, I],
+        "xfg_ensemble_advance": [P, I, I, C.POINTER(C.c_float)],
+        "xfg_ensemble_status": [P, I, pd, pi, pi],
+        "xfg_ensemble_get_state": [P, I, P],
+        "xfg_ensemble_set_option": [P, I, I],
+        "xfg_ensemble_get_option": [P, I, pi],
+        "xfg_ensemble_active": [P],
+    })
     for name, args in sig.items():
         fn = getattr(L, name)
         fn.argtypes = args
         fn.restype = C.c_int
+    L.xfg_ensemble_member_bytes.argtypes = [C.POINTER(Block), I]
+    L.xfg_ensemble_member_bytes.restype = C.c_size_t
+    L.xfg_ensemble_free_bytes.argtypes = [P]
+    L.xfg_ensemble_free_bytes.restype = C.c_size_t
     _lib = L
     return L
 

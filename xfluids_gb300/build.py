@@ -15,7 +15,8 @@ LIB = os.path.join(BUILD, "libxfluids_gb300.so")
 # (unit, extra nvcc flags): FP64 mixture kernels and the strict single-gas kernels are compiled
 # without floating-point contraction.
 NOFMA = ["--fmad=false", "-DXFG_STRICT"]
-UNITS = [("xfg_api.cu", []), ("xfg_noalloc.cu", []), ("xfg_inst_ncop.cu", []), ("xfg_inst_ncop_strict.cu", NOFMA)]
+UNITS = [("xfg_api.cu", []), ("xfg_noalloc.cu", []), ("xfg_inst_ncop.cu", []), ("xfg_inst_ncop_strict.cu", NOFMA),
+         ("xfg_ensemble.cu", [])]
 UNITS += [(f"xfg_inst_cop{n}.cu", NOFMA) for n in (2, 3, 4, 5, 6)]
 UNITS += [(f"xfg_inst_cop{n}_mixed.cu", []) for n in (2, 3, 4, 5, 6)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

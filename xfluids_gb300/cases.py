@@ -85,10 +85,37 @@ def riemann2d(n, states, cfl=0.45, precision=0):
     return b, s, empty_thermal(), U, None
 
 
+def riemann1d(n, left, right, cfl=0.5, precision=0):
+    """1D two-state Riemann problem on [0,1] split at x = 0.5, transmissive ends (the Sod layout
+    with arbitrary states): left/right = (rho, u, p)."""
+    b = make_block((n, 0, 0), (1.0, 1.0, 1.0), [OUTFLOW] * 6, cfl=cfl)
+    s = make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=precision)
+    X, _, _ = cell_centres(b)
+    lft = X < 0.5
+    rho = np.where(lft, left[0], right[0])
+    u = np.where(lft, left[1], right[1])
+    p = np.where(lft, left[2], right[2])
+    z = np.zeros_like(rho)
+    U = conserved_ideal(rho, u, z, z, p)
+    return b, s, empty_thermal(), U, None
+
+
 def ensemble_sizes(count=256, seed=0, lo=7.0, hi=10.0):
     """Cells per side N = round(2^U[lo,hi]) for each ensemble member, seeded."""
     rng = np.random.default_rng(seed)
     return np.rint(2.0 ** rng.uniform(lo, hi, count)).astype(int), rng
+
+
+def riemann_ensemble(count=256, seed=0, lo=7.0, hi=10.0, precision=0):
+    """Batched ensemble of independent 2D four-quadrant Riemann problems: N per side
+    round(2^U[lo,hi]), quadrant states as riemann_states, CFL 0.45, outflow. Returns the scheme
+    and a list of (block, U)."""
+    sizes, rng = ensemble_sizes(count, seed, lo, hi)
+    members = []
+    for n in sizes:
+        b, s, _, U, _ = riemann2d(int(n), riemann_states(rng), precision=precision)
+        members.append((b, U))
+    return make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=precision), members
 
 
 # ---------------------------------------------------------------------------------------------

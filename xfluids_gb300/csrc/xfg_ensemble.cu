@@ -1,0 +1,623 @@
+// xfg_ensemble.cu - many independent single-gas grids advanced together (batched ensemble and the
+// device side of the request server).
+//
+// All members live in one device pool (allocated once; members are sub-allocated first-fit, so
+// admission is by HBM budget). One step of every active member is one sequence of batched kernels:
+// each launch covers the blocks of all members of that phase, a block finds its member through a
+// prefix table of block offsets and runs the same device bodies as the single-grid kernels
+// (xfg_kernels.cuh / xfg_mixed.cuh) on that member's arrays. Every member has its own dt, time,
+// target time and done flag on the device; members that reached their target skip all work. The
+// step is captured once in a CUDA graph and replayed until membership changes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/xfluids_gb300.h"
+#define XFG_KNS ens
+#include "xfg_kernels.cuh"
+#include "xfg_mixed.cuh"
+#include "xfg_ops.h"
+
+using namespace xfg;
+using namespace xfg::ens;
+
+namespace {
+
+// Device descriptor of one member.
+struct Member {
+    Geo g;
+    DevFields f;
+    double cfl;
+    int bc[6];
+    int active;
+    int ltx;  // face tile of this member: 2^ltx faces along x by kThreads >> ltx across
+};
+
+// phases with a block table; PH_FALL holds three entries per member (x, y, z face sweeps of the
+// fused face launch), the others one
+enum { PH_BC0, PH_BC1, PH_BC2, PH_STATES, PH_F0, PH_F1, PH_F2, PH_DIV, PH_FALL, PH_N };
+
+// size classes with their own face tile: 1D, 2D below 384 cells per side, 2D from 384, 3D
+enum { CL_1D, CL_2D_SMALL, CL_2D_LARGE, CL_3D, CL_N };
+
+__device__ __forceinline__ int member_of_block(const int *__restrict__ off, int n, int b) {
+    int lo = 0, hi = n;  // off[0] = 0 <= b < off[n]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ bool member_done(const Member &m) { return m.f.dtbuf[4] != 0.0; }
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) kb_bc(const Member *__restrict__ M, const int *__restrict__ off, int n, int flag) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    bc_body<D, 5>(m.g, flag == 1 || flag == 0 ? m.f.U : m.f.U1, m.bc[2 * D], m.bc[2 * D + 1], t);
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_states(const Member *__restrict__ M, const int *__restrict__ off, int n,
+                                                      DevThermo th, int flag, int want_lam) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    const long long id = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    double *UI = flag == 1 || flag == 0 ? m.f.U : m.f.U1;
+    if (MIXED) {
+        float lx = 0.f, ly = 0.f, lz = 0.f;
+        states_mixed_body<false, 1>(m.g, m.f, th, UI, 0, want_lam, id, lx, ly, lz);
+        if (want_lam) lam_block_reduce_f(m.g, m.f, lx, ly, lz);
+    } else {
+        double lx = 0.0, ly = 0.0, lz = 0.0;
+        states_body<false, 1>(m.g, m.f, th, UI, 0, want_lam, id, lx, ly, lz);
+        if (want_lam) lam_block_reduce(m.g, m.f, lx, ly, lz);
+    }
+}
+
+template <int D, int ORDER, bool MIXED>
+__device__ __forceinline__ void member_face(const Member &m, int lb, const DevThermo &th, int flag, int artificial) {
+    const dim3 gd = face_grid_tile<D>(m.g, m.ltx);
+    const int bx = lb % gd.x, by = (lb / gd.x) % gd.y, bz = lb / (gd.x * gd.y);
+    int i, j, k;
+    if (!face_of_tile<D>(m.g, bx, by, bz, m.ltx, i, j, k)) return;
+    if (MIXED)
+        faces_mixed_body<D, false, 1, ORDER>(m.g, m.f, th, artificial, nullptr, i, j, k);
+    else
+        faces_body<D, false, 1, ORDER>(m.g, m.f, th, flag == 1 || flag == 0 ? m.f.U : m.f.U1, artificial, nullptr, i, j, k);
+}
+
+// one face sweep (direction D) of every member
+template <int D, int ORDER, bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_faces(const Member *__restrict__ M, const int *__restrict__ off, int n,
+                                                     DevThermo th, int flag, int artificial) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    member_face<D, ORDER, MIXED>(m, blockIdx.x - off[mi], th, flag, artificial);
+}
+
+// all face sweeps of every member in one launch (entries 3 q + D of the table)
+template <int ORDER, bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_faces_all(const Member *__restrict__ M, const int *__restrict__ off,
+                                                         int n3, DevThermo th, int flag, int artificial) {
+    const int e = member_of_block(off, n3, blockIdx.x);
+    const Member &m = M[e / 3];
+    if (member_done(m)) return;
+    const int lb = blockIdx.x - off[e];
+    switch (e % 3) {
+    case 0: member_face<0, ORDER, MIXED>(m, lb, th, flag, artificial); break;
+    case 1: member_face<1, ORDER, MIXED>(m, lb, th, flag, artificial); break;
+    default: member_face<2, ORDER, MIXED>(m, lb, th, flag, artificial); break;
+    }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_div_rk(const Member *__restrict__ M, const int *__restrict__ off, int n, int flag) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    if (MIXED)
+        div_rk_mixed_body<5>(m.g, m.f, flag, m.f.dtbuf[0], 1, 0, t);
+    else
+        div_rk_body<5>(m.g, m.f, flag, m.f.dtbuf[0], 1, 0, t);
+}
+
+__global__ void kb_dt(const Member *__restrict__ M, int n) {
+    const int mi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (mi >= n) return;
+    const Member &m = M[mi];
+    if (!m.active) return;
+    // a member whose last step produced a NaN / Inf / negative density or pressure stops there,
+    // as the reference's run stops after EstimateFluidNAN / UpdateFluidStates report an error
+    if (m.f.err[ERR_STATE] | m.f.err[ERR_PRIM]) {
+        if (m.f.dtbuf[4] == 0.0) m.f.dtbuf[4] = 2.0, m.f.dtbuf[0] = 0.0;
+        return;
+    }
+    dt_step_body(m.g, m.f, m.cfl);
+}
+
+__global__ void kb_aos_to_soa(const double *__restrict__ aos, double *__restrict__ soa, int E, long long N, long long P) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * E) return;
+    soa[(t % E) * P + t / E] = aos[t];
+}
+__global__ void kb_soa_to_aos(const double *__restrict__ soa, double *__restrict__ aos, int E, long long N, long long P) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N * E) return;
+    aos[t] = soa[(t % E) * P + t / E];
+}
+
+size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+thread_local std::string g_eerr;
+int efail(int code, const char *fmt, const char *detail = "") {
+    char buf[512];
+    snprintf(buf, sizeof buf, fmt, detail);
+    set_last_error(buf);
+    return code;
+}
+#define ECK(call)                                                                            \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) return efail(-2, #call " failed: %s", cudaGetErrorString(e_)); \
+    } while (0)
+
+// First-fit allocator over the device pool (offsets in bytes).
+struct PoolAlloc {
+    size_t size = 0;
+    std::map<size_t, size_t> free_;  // offset -> length
+    void init(size_t n) { size = n, free_.clear(), free_[0] = n; }
+    bool alloc(size_t n, size_t *off) {
+        n = up(n, 256);
+        for (auto it = free_.begin(); it != free_.end(); ++it)
+            if (it->second >= n) {
+                *off = it->first;
+                size_t rest = it->second - n, o = it->first + n;
+                free_.erase(it);
+                if (rest) free_[o] = rest;
+                return true;
+            }
+        return false;
+    }
+    void release(size_t off, size_t n) {
+        n = up(n, 256);
+        auto it = free_.emplace(off, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) it->second += nx->second, free_.erase(nx);
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) pv->second += it->second, free_.erase(it);
+        }
+    }
+    size_t free_bytes() const {
+        size_t s = 0;
+        for (auto &kv : free_) s += kv.second;
+        return s;
+    }
+};
+
+}  // namespace
+
+struct xfg_ensemble {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    xfg_scheme sc;
+    DevThermo th;
+    int capacity = 0;
+    char *pool = nullptr;
+    size_t pool_bytes = 0;
+    PoolAlloc alloc;
+    std::vector<Member> hm;               // host mirror of the member table
+    std::vector<size_t> m_off, m_len;     // pool allocation of each slot
+    std::vector<xfg_block> blocks;
+    Member *dm = nullptr;                 // device member table
+    int *doff = nullptr;                  // device block tables, PH_N rows of 3 capacity + 1
+    double *ddt = nullptr;                // device dtbuf of all slots (8 doubles each)
+    double *hdt = nullptr;                // pinned mirror
+    int *derr = nullptr;                  // device error words (8 ints each)
+    int *herr = nullptr;
+    std::vector<int> order;               // active slots in launch order
+    int nblk[PH_N] = {0};
+    bool dirty = true;
+    cudaGraphExec_t graph = nullptr;
+    int graph_built_steps = 0;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    // launch schedule (xfg_ensemble_set_option)
+    int largest_first = 1;
+    int fused_faces = 0;                  // one launch for all face sweeps
+    int graph_steps = 1;                  // fused steps per captured graph
+    int ltx[CL_N] = {7, 5, 5, 5};         // face tile per size class
+};
+
+namespace {
+
+size_t row_len(const xfg_ensemble *e) { return 3 * (size_t)e->capacity + 1; }
+
+size_t member_bytes(const xfg_block &b, bool mixed) {
+    const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
+    const int dims = b.DimX + b.DimY + b.DimZ;
+    size_t nd = 3 * 5 + 12;                              // U, U1, LU, primitives
+    if (!mixed) nd += 2 * 5 * dims + 2 + 3 * dims;       // F, Fw, sqrt(rho), 1/sqrt(rho), |lambda|
+    size_t bytes = nd * P * 8;
+    if (mixed) bytes += (size_t)(5 + 7 + 2 * 5 * dims) * up(P * 4, 256);
+    return bytes + 1024;                                 // lam + small words
+}
+
+void carve(Member &m, char *base, const xfg_block &b, bool mixed) {
+    const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
+    const int dims[3] = {b.DimX, b.DimY, b.DimZ};
+    char *p = base;
+    auto t8 = [&](int c) { double *r = (double *)p; p += (size_t)c * P * 8; return r; };
+    auto t4 = [&](int c) { float *r = (float *)p; p += (size_t)c * up(P * 4, 256); return r; };
+    DevFields &f = m.f;
+    std::memset(&f, 0, sizeof f);
+    f.U = t8(5), f.U1 = t8(5), f.LU = t8(5);
+    f.rho = t8(1), f.u = t8(1), f.v = t8(1), f.w = t8(1), f.p = t8(1), f.H = t8(1);
+    f.c = t8(1), f.T = t8(1), f.gamma = t8(1), f.e = t8(1), f.Cp = t8(1), f.R = t8(1);
+    if (!mixed) {
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) f.F[d] = t8(5), f.Fw[d] = t8(5);
+        f.sr = t8(1), f.isr = t8(1);
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) f.eab[d] = t8(3);
+    } else {
+        f.Uf = t4(5), f.primf = t4(7);
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) f.Ff[d] = t4(5), f.Fwf[d] = t4(5);
+    }
+    f.lam = (unsigned long long *)p;
+    Geo &g = m.g;
+    g.Xmax = b.Xmax, g.Ymax = b.Ymax, g.Zmax = b.Zmax, g.Xi = b.X_inner, g.Yi = b.Y_inner, g.Zi = b.Z_inner;
+    g.Bx = b.Bwidth_X, g.By = b.Bwidth_Y, g.Bz = b.Bwidth_Z, g.dimx = b.DimX, g.dimy = b.DimY, g.dimz = b.DimZ;
+    g._dx = b._dx, g._dy = b._dy, g._dz = b._dz, g.pitch = (long long)P;
+    m.cfl = b.CFLnumber;
+    for (int q = 0; q < 6; q++) m.bc[q] = b.Boundarys[q];
+}
+
+int size_class(const Geo &g) {
+    const int dims = g.dimx + g.dimy + g.dimz;
+    if (dims == 1) return CL_1D;
+    if (dims == 3) return CL_3D;
+    return std::max(g.Xi, std::max(g.Yi, g.Zi)) < 384 ? CL_2D_SMALL : CL_2D_LARGE;
+}
+
+int face_blocks(const Geo &g, int d, int ltx) {
+    const int dims[3] = {g.dimx, g.dimy, g.dimz};
+    if (!dims[d]) return 0;
+    const dim3 b = d == 0 ? face_grid_tile<0>(g, ltx) : (d == 1 ? face_grid_tile<1>(g, ltx) : face_grid_tile<2>(g, ltx));
+    return (int)(b.x * b.y * b.z);
+}
+
+int blocks_of(const Geo &g, int ph, int ltx) {
+    const long long N = g.ncell(), inner = (long long)g.Xi * g.Yi * g.Zi;
+    auto gb = [](long long n) { return (int)((n + kThreads - 1) / kThreads); };
+    switch (ph) {
+    case PH_BC0: return g.dimx ? gb((long long)g.Bx * g.Ymax * g.Zmax) : 0;
+    case PH_BC1: return g.dimy ? gb((long long)g.By * g.Xmax * g.Zmax) : 0;
+    case PH_BC2: return g.dimz ? gb((long long)g.Bz * g.Xmax * g.Ymax) : 0;
+    case PH_STATES: return gb(N);
+    case PH_F0: return face_blocks(g, 0, ltx);
+    case PH_F1: return face_blocks(g, 1, ltx);
+    case PH_F2: return face_blocks(g, 2, ltx);
+    case PH_DIV: return gb(inner);
+    }
+    return 0;
+}
+
+// Rebuild the launch order, the block tables and the device member table.
+int rebuild(xfg_ensemble *e) {
+    e->order.clear();
+    for (int s = 0; s < e->capacity; s++)
+        if (e->hm[s].active) e->order.push_back(s);
+    if (e->largest_first)
+        std::stable_sort(e->order.begin(), e->order.end(), [e](int a, int b) { return e->hm[a].g.ncell() > e->hm[b].g.ncell(); });
+    const int n = (int)e->order.size();
+    std::vector<Member> ordered(std::max(n, 1));
+    for (int q = 0; q < n; q++) {
+        ordered[q] = e->hm[e->order[q]];
+        ordered[q].ltx = e->ltx[size_class(ordered[q].g)];
+    }
+    std::vector<int> tab((size_t)PH_N * row_len(e), 0);
+    for (int ph = 0; ph < PH_N; ph++) {
+        long long acc = 0;
+        int *t = &tab[(size_t)ph * row_len(e)];
+        if (ph == PH_FALL) {
+            for (int q = 0; q < n; q++)
+                for (int d = 0; d < 3; d++) t[3 * q + d] = (int)acc, acc += face_blocks(ordered[q].g, d, ordered[q].ltx);
+            t[3 * n] = (int)acc;
+        } else {
+            for (int q = 0; q < n; q++) t[q] = (int)acc, acc += blocks_of(ordered[q].g, ph, ordered[q].ltx);
+            t[n] = (int)acc;
+        }
+        if (acc > 0x7fffffffLL) return efail(-1, "ensemble too large for one launch per phase%s");
+        e->nblk[ph] = (int)acc;
+    }
+    ECK(cudaMemcpyAsync(e->dm, ordered.data(), sizeof(Member) * std::max(n, 1), cudaMemcpyHostToDevice, e->st));
+    ECK(cudaMemcpyAsync(e->doff, tab.data(), sizeof(int) * tab.size(), cudaMemcpyHostToDevice, e->st));
+    ECK(cudaStreamSynchronize(e->st));
+    if (e->graph) cudaGraphExecDestroy(e->graph), e->graph = nullptr;
+    e->dirty = false;
+    return 0;
+}
+
+const int *tab(const xfg_ensemble *e, int ph) { return e->doff + (size_t)ph * row_len(e); }
+
+void launch_step(xfg_ensemble *e) {
+    const int n = (int)e->order.size();
+    if (!n) return;
+    const bool mixed = e->sc.precision == XFG_MIXED;
+    const int order5 = e->sc.scheme_order == 5;
+    cudaStream_t st = e->st;
+    kb_dt<<<(n + 127) / 128, 128, 0, st>>>(e->dm, n);
+    for (int flag = 1; flag <= 3; flag++) {
+        if (e->nblk[PH_BC0]) kb_bc<0><<<e->nblk[PH_BC0], kThreads, 0, st>>>(e->dm, tab(e, PH_BC0), n, flag);
+        if (e->nblk[PH_BC1]) kb_bc<1><<<e->nblk[PH_BC1], kThreads, 0, st>>>(e->dm, tab(e, PH_BC1), n, flag);
+        if (e->nblk[PH_BC2]) kb_bc<2><<<e->nblk[PH_BC2], kThreads, 0, st>>>(e->dm, tab(e, PH_BC2), n, flag);
+        if (mixed) kb_states<true><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
+        else kb_states<false><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
+        const int art = e->sc.artificial_type;
+        if (e->fused_faces) {
+            const int nb = e->nblk[PH_FALL];
+            const int *t = tab(e, PH_FALL);
+            if (nb) {
+                if (mixed) {
+                    if (order5) kb_faces_all<5, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                    else kb_faces_all<7, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                } else {
+                    if (order5) kb_faces_all<5, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                    else kb_faces_all<7, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                }
+            }
+        } else {
+#define XFG_FACES(D, PH)                                                                                           \
+            if (e->nblk[PH]) {                                                                                     \
+                const int *t = tab(e, PH);                                                                         \
+                if (mixed) {                                                                                       \
+                    if (order5) kb_faces<D, 5, true><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);  \
+                    else kb_faces<D, 7, true><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);         \
+                } else {                                                                                           \
+                    if (order5) kb_faces<D, 5, false><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art); \
+                    else kb_faces<D, 7, false><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);        \
+                }                                                                                                  \
+            }
+            XFG_FACES(0, PH_F0)
+            XFG_FACES(1, PH_F1)
+            XFG_FACES(2, PH_F2)
+#undef XFG_FACES
+        }
+        if (mixed) kb_div_rk<true><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
+        else kb_div_rk<false><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *scheme, const xfg_thermal *thermal,
+                        int device, xfg_ensemble **out) {
+    if (!out || !scheme || capacity <= 0) return efail(-1, "bad argument%s");
+    *out = nullptr;
+    if (scheme->cop) return efail(-1, "the ensemble engine serves single-gas members (cop = 0)%s");
+    if (scheme->precision != XFG_FP64 && scheme->precision != XFG_MIXED)
+        return efail(-1, "ensemble precision must be XFG_FP64 or XFG_MIXED%s");
+    if (scheme->artificial_type == XFG_GLF) return efail(-1, "the ensemble engine supports Roe and LLF splitting%s");
+    if (scheme->scheme_order != 5 && scheme->scheme_order != 7) return efail(-1, "scheme_order must be 5 or 7%s");
+    ECK(cudaSetDevice(device));
+    xfg_ensemble *e = new xfg_ensemble();
+    e->device = device, e->sc = *scheme, e->capacity = capacity;
+    std::memset(&e->th, 0, sizeof e->th);
+    e->th.ncop_gamma = scheme->ncop_gamma;
+    e->th.nasa = 1;
+    e->hm.assign(capacity, Member{});
+    for (auto &m : e->hm) std::memset(&m, 0, sizeof m);
+    e->m_off.assign(capacity, 0), e->m_len.assign(capacity, 0), e->blocks.assign(capacity, xfg_block{});
+    cudaError_t err = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking);
+    if (err == cudaSuccess) err = cudaMalloc(&e->pool, pool_bytes);
+    if (err == cudaSuccess) err = cudaMalloc(&e->dm, sizeof(Member) * capacity);
+    if (err == cudaSuccess) err = cudaMalloc(&e->doff, sizeof(int) * PH_N * (3 * (size_t)capacity + 1));
+    if (err == cudaSuccess) err = cudaMalloc(&e->ddt, sizeof(double) * 8 * capacity);
+    if (err == cudaSuccess) err = cudaMalloc(&e->derr, sizeof(int) * 8 * capacity);
+    if (err == cudaSuccess) err = cudaMallocHost(&e->hdt, sizeof(double) * 8 * capacity);
+    if (err == cudaSuccess) err = cudaMallocHost(&e->herr, sizeof(int) * 8 * capacity);
+    if (err == cudaSuccess) err = cudaEventCreate(&e->ev[0]);
+    if (err == cudaSuccess) err = cudaEventCreate(&e->ev[1]);
+    if (err == cudaSuccess) err = cudaMemsetAsync(e->ddt, 0, sizeof(double) * 8 * capacity, e->st);
+    if (err == cudaSuccess) err = cudaMemsetAsync(e->derr, 0, sizeof(int) * 8 * capacity, e->st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->st);
+    if (err != cudaSuccess) {
+        xfg_ensemble_destroy(e);
+        return efail(-3, "ensemble allocation failed: %s", cudaGetErrorString(err));
+    }
+    e->pool_bytes = pool_bytes;
+    e->alloc.init(pool_bytes);
+    *out = e;
+    return 0;
+}
+
+int xfg_ensemble_destroy(xfg_ensemble *e) {
+    if (!e) return 0;
+    cudaSetDevice(e->device);
+    if (e->st) cudaStreamSynchronize(e->st);
+    if (e->graph) cudaGraphExecDestroy(e->graph);
+    for (auto &v : e->ev)
+        if (v) cudaEventDestroy(v);
+    cudaFree(e->pool), cudaFree(e->dm), cudaFree(e->doff), cudaFree(e->ddt), cudaFree(e->derr);
+    if (e->hdt) cudaFreeHost(e->hdt);
+    if (e->herr) cudaFreeHost(e->herr);
+    if (e->st) cudaStreamDestroy(e->st);
+    delete e;
+    return 0;
+}
+
+size_t xfg_ensemble_member_bytes(const xfg_block *block, int precision) {
+    return block ? member_bytes(*block, precision == XFG_MIXED) : 0;
+}
+
+int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_aos, double target_t, int *slot) {
+    if (!e || !block || !U_aos || !slot) return efail(-1, "null argument%s");
+    *slot = -1;
+    int s = -1;
+    for (int q = 0; q < e->capacity; q++)
+        if (!e->hm[q].active && e->m_len[q] == 0) { s = q; break; }
+    if (s < 0) return 1;  // no free slot
+    const bool mixed = e->sc.precision == XFG_MIXED;
+    const size_t need = member_bytes(*block, mixed);
+    size_t off = 0;
+    if (!e->alloc.alloc(need, &off)) return 2;  // no memory: admission waits
+    ECK(cudaSetDevice(e->device));
+    Member &m = e->hm[s];
+    std::memset(&m, 0, sizeof m);
+    carve(m, e->pool + off, *block, mixed);
+    m.f.dtbuf = e->ddt + 8 * s;
+    m.f.err = e->derr + 8 * s;
+    m.active = 1;
+    e->m_off[s] = off, e->m_len[s] = need, e->blocks[s] = *block;
+    const long long N = m.g.ncell(), P = m.g.pitch;
+    ECK(cudaMemsetAsync(e->pool + off, 0, need, e->st));
+    double *stage = m.f.LU;  // AoS staging in LU (5 * P >= 5 * N)
+    ECK(cudaMemcpyAsync(stage, U_aos, sizeof(double) * 5 * N, cudaMemcpyDefault, e->st));
+    kb_aos_to_soa<<<(unsigned)((5 * N + 255) / 256), 256, 0, e->st>>>(stage, m.f.U, 5, N, P);
+    ECK(cudaMemcpyAsync(m.f.U1, m.f.U, sizeof(double) * 5 * P, cudaMemcpyDeviceToDevice, e->st));
+    double dtb[8] = {0.0, 0.0, target_t, 0.0, 0.0, 0.0, 0.0, 0.0};
+    ECK(cudaMemcpyAsync(m.f.dtbuf, dtb, sizeof dtb, cudaMemcpyHostToDevice, e->st));
+    ECK(cudaMemsetAsync(m.f.err, 0, 8 * sizeof(int), e->st));
+    // main.cpp:45-47 for this member: BoundaryCondition(U) and UpdateStates(U) (dt maxima on)
+    LaunchCtx c;
+    std::memset(&c, 0, sizeof c);
+    c.g = m.g, c.f = m.f, c.th = e->th, c.st = e->st, c.artificial = e->sc.artificial_type;
+    for (int q = 0; q < 6; q++) c.bc[q] = m.bc[q];
+    c.precision = e->sc.precision;
+    const Ops *ops = find_ops(0, 1, e->sc.scheme_order, e->sc.precision);
+    if (!ops) return efail(-1, "no single-gas kernels for this scheme%s");
+    ops->bc(c, m.f.U, nullptr);
+    ops->states(c, m.f.U, 1, 0);
+    ECK(cudaGetLastError());
+    ECK(cudaStreamSynchronize(e->st));
+    e->dirty = true;
+    *slot = s;
+    return 0;
+}
+
+int xfg_ensemble_remove(xfg_ensemble *e, int slot) {
+    if (!e || slot < 0 || slot >= e->capacity || e->m_len[slot] == 0) return efail(-1, "bad slot%s");
+    ECK(cudaStreamSynchronize(e->st));
+    e->alloc.release(e->m_off[slot], e->m_len[slot]);
+    e->m_len[slot] = 0, e->m_off[slot] = 0;
+    std::memset(&e->hm[slot], 0, sizeof(Member));
+    e->dirty = true;
+    return 0;
+}
+
+int xfg_ensemble_advance(xfg_ensemble *e, int nsteps, int use_graph, float *device_ms) {
+    if (!e) return efail(-1, "null ensemble%s");
+    ECK(cudaSetDevice(e->device));
+    if (e->dirty) {
+        int rc = rebuild(e);
+        if (rc) return rc;
+    }
+    if (e->order.empty()) return 0;
+    const int G = use_graph ? e->graph_steps : 1;
+    if (use_graph && (!e->graph || e->graph_built_steps != G)) {
+        if (e->graph) cudaGraphExecDestroy(e->graph), e->graph = nullptr;
+        cudaGraph_t g;
+        ECK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+        for (int q = 0; q < G; q++) launch_step(e);
+        cudaError_t err = cudaStreamEndCapture(e->st, &g);
+        if (err != cudaSuccess) return efail(-2, "graph capture failed: %s", cudaGetErrorString(err));
+        err = cudaGraphInstantiate(&e->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (err != cudaSuccess) return efail(-2, "graph instantiate failed: %s", cudaGetErrorString(err));
+        e->graph_built_steps = G;
+    }
+    ECK(cudaEventRecord(e->ev[0], e->st));
+    int left = nsteps;
+    if (use_graph)
+        for (; left >= G; left -= G) ECK(cudaGraphLaunch(e->graph, e->st));
+    for (; left > 0; left--) launch_step(e);
+    ECK(cudaEventRecord(e->ev[1], e->st));
+    ECK(cudaMemcpyAsync(e->hdt, e->ddt, sizeof(double) * 8 * e->capacity, cudaMemcpyDeviceToHost, e->st));
+    ECK(cudaMemcpyAsync(e->herr, e->derr, sizeof(int) * 8 * e->capacity, cudaMemcpyDeviceToHost, e->st));
+    ECK(cudaStreamSynchronize(e->st));
+    ECK(cudaGetLastError());
+    if (device_ms) cudaEventElapsedTime(device_ms, e->ev[0], e->ev[1]);
+    int rc = 0;
+    for (int s : e->order)
+        if (e->herr[8 * s + ERR_STATE]) rc = 10000;
+        else if (e->herr[8 * s + ERR_PRIM] && !rc) rc = 1;
+    return rc;
+}
+
+// Time, steps, done flag and error of a member as of the last xfg_ensemble_advance.
+int xfg_ensemble_status(xfg_ensemble *e, int slot, double *t, int *steps, int *done) {
+    if (!e || slot < 0 || slot >= e->capacity) return efail(-1, "bad slot%s");
+    const double *b = e->hdt + 8 * slot;
+    if (t) *t = b[1];
+    if (steps) *steps = (int)b[3];
+    if (done) *done = b[4] != 0.0;
+    if (e->herr[8 * slot + ERR_STATE]) return 10000;
+    return e->herr[8 * slot + ERR_PRIM] ? 1 : 0;
+}
+
+int xfg_ensemble_get_state(xfg_ensemble *e, int slot, double *U_aos) {
+    if (!e || slot < 0 || slot >= e->capacity || e->m_len[slot] == 0 || !U_aos) return efail(-1, "bad slot%s");
+    ECK(cudaSetDevice(e->device));
+    const Member &m = e->hm[slot];
+    const long long N = m.g.ncell(), P = m.g.pitch;
+    kb_soa_to_aos<<<(unsigned)((5 * N + 255) / 256), 256, 0, e->st>>>(m.f.U, m.f.LU, 5, N, P);
+    ECK(cudaMemcpyAsync(U_aos, m.f.LU, sizeof(double) * 5 * N, cudaMemcpyDefault, e->st));
+    ECK(cudaStreamSynchronize(e->st));
+    return 0;
+}
+
+int xfg_ensemble_get_option(xfg_ensemble *e, int option, int *value) {
+    if (!e || !value) return efail(-1, "null argument%s");
+    if (option == XFG_ENS_LARGEST_FIRST) *value = e->largest_first;
+    else if (option == XFG_ENS_FUSED_FACES) *value = e->fused_faces;
+    else if (option == XFG_ENS_GRAPH_STEPS) *value = e->graph_steps;
+    else if (option >= XFG_ENS_TILE_1D && option <= XFG_ENS_TILE_3D) *value = e->ltx[option - XFG_ENS_TILE_1D];
+    else return efail(-1, "unknown option%s");
+    return 0;
+}
+
+int xfg_ensemble_set_option(xfg_ensemble *e, int option, int value) {
+    if (!e) return efail(-1, "null ensemble%s");
+    if (option == XFG_ENS_LARGEST_FIRST) e->largest_first = value ? 1 : 0;
+    else if (option == XFG_ENS_FUSED_FACES) e->fused_faces = value ? 1 : 0;
+    else if (option == XFG_ENS_GRAPH_STEPS) {
+        if (value < 1 || value > 64) return efail(-1, "graph steps must be in 1..64%s");
+        e->graph_steps = value;
+        return 0;  // the graph is re-captured at the next advance
+    } else if (option >= XFG_ENS_TILE_1D && option <= XFG_ENS_TILE_3D) {
+        if (value < 3 || value > 7) return efail(-1, "face tile: log2 of its x extent must be in 3..7%s");
+        e->ltx[option - XFG_ENS_TILE_1D] = value;
+    } else
+        return efail(-1, "unknown option%s");
+    e->dirty = true;
+    return 0;
+}
+
+size_t xfg_ensemble_free_bytes(xfg_ensemble *e) { return e ? e->alloc.free_bytes() : 0; }
+
+int xfg_ensemble_active(xfg_ensemble *e) {
+    if (!e) return 0;
+    int n = 0;
+    for (auto &m : e->hm) n += m.active ? 1 : 0;
+    return n;
+}
+
+}  // extern "C"

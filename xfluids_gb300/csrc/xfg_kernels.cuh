@@ -33,16 +33,13 @@ __device__ __forceinline__ bool step_done(const DevFields &f) { return f.dtbuf &
 // One thread per (ghost layer, transverse cell) covering both faces of direction D.
 // ---------------------------------------------------------------------------------------------
 template <int D, int E>
-__global__ void __launch_bounds__(kThreads) k_bc(Geo g, double *__restrict__ U, int bc_lo, int bc_hi,
-                                                 const double *__restrict__ guard_dtbuf) {
-    if (guard_dtbuf && guard_dtbuf[4] != 0.0) return;
+__device__ __forceinline__ void bc_body(const Geo &g, double *__restrict__ U, int bc_lo, int bc_hi, long long t) {
     const int bw = D == 0 ? g.Bx : (D == 1 ? g.By : g.Bz);
     const int inner = D == 0 ? g.Xi : (D == 1 ? g.Yi : g.Zi);
     const int nmax = D == 0 ? g.Xmax : (D == 1 ? g.Ymax : g.Zmax);
     // transverse extents (full, ghosts included)
     const int ta = D == 0 ? g.Ymax : g.Xmax;
     const int tb = D == 2 ? g.Ymax : g.Zmax;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long total = (long long)bw * ta * tb;
     if (t >= total) return;
     int gl = (int)(t % bw);
@@ -94,6 +91,12 @@ __global__ void __launch_bounds__(kThreads) k_bc(Geo g, double *__restrict__ U, 
         }
     }
 }
+template <int D, int E>
+__global__ void __launch_bounds__(kThreads) k_bc(Geo g, double *__restrict__ U, int bc_lo, int bc_hi,
+                                                 const double *__restrict__ guard_dtbuf) {
+    if (guard_dtbuf && guard_dtbuf[4] != 0.0) return;
+    bc_body<D, E>(g, U, bc_lo, bc_hi, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ---------------------------------------------------------------------------------------------
 // Primitive recovery and physical fluxes on all cells: Getrhoyi (Update_device.hpp:7-29),
@@ -102,14 +105,12 @@ __global__ void __launch_bounds__(kThreads) k_bc(Geo g, double *__restrict__ U, 
 // over all cells (GlobalDt_block.hpp:31-66) when want_lam.
 // ---------------------------------------------------------------------------------------------
 template <bool COP, int NS>
-__global__ void __launch_bounds__(kThreads) k_states(Geo g, DevFields f, DevThermo th, double *__restrict__ UI,
-                                                     int ghost, int want_lam, int guard) {
+__device__ __forceinline__ void states_body(const Geo &g, const DevFields &f, const DevThermo &th,
+                                            double *__restrict__ UI, int ghost, int want_lam, long long id,
+                                            double &lamx, double &lamy, double &lamz) {
     using S = Sys<COP, NS>;
     constexpr int E = S::E, NCOP = S::NCOP;
-    if (guard && step_done(f)) return;
     const long long P = g.pitch, N = g.ncell();
-    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    double lamx = 0.0, lamy = 0.0, lamz = 0.0;
     if (id < N) {
         double U[E];
 #pragma unroll
@@ -229,25 +230,38 @@ __global__ void __launch_bounds__(kThreads) k_states(Geo g, DevFields f, DevTher
             if (!(lamz >= 0.0)) lamz = __longlong_as_double(0x7ff0000000000000LL);
         }
     }
-    if (want_lam) {  // warp then block max, one atomic per block and direction
+}
+
+// Warp then block max of the GetDt wave speeds, one atomic per block and direction. Every thread
+// of the block calls it (a block never spans two grids).
+__device__ __forceinline__ void lam_block_reduce(const Geo &g, const DevFields &f, double lamx, double lamy, double lamz) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            lamx = fmax(lamx, __shfl_xor_sync(0xffffffffu, lamx, o));
-            lamy = fmax(lamy, __shfl_xor_sync(0xffffffffu, lamy, o));
-            lamz = fmax(lamz, __shfl_xor_sync(0xffffffffu, lamz, o));
-        }
-        __shared__ double red[3][kThreads / 32];
-        const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        if (lane == 0) red[0][wid] = lamx, red[1][wid] = lamy, red[2][wid] = lamz;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double a = red[0][0], b = red[1][0], c = red[2][0];
-            for (int q = 1; q < kThreads / 32; q++) a = fmax(a, red[0][q]), b = fmax(b, red[1][q]), c = fmax(c, red[2][q]);
-            if (g.dimx) atomic_max_nonneg(&f.lam[0], a);
-            if (g.dimy) atomic_max_nonneg(&f.lam[1], b);
-            if (g.dimz) atomic_max_nonneg(&f.lam[2], c);
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        lamx = fmax(lamx, __shfl_xor_sync(0xffffffffu, lamx, o));
+        lamy = fmax(lamy, __shfl_xor_sync(0xffffffffu, lamy, o));
+        lamz = fmax(lamz, __shfl_xor_sync(0xffffffffu, lamz, o));
     }
+    __shared__ double red[3][kThreads / 32];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[0][wid] = lamx, red[1][wid] = lamy, red[2][wid] = lamz;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = red[0][0], b = red[1][0], c = red[2][0];
+        for (int q = 1; q < (int)(blockDim.x >> 5); q++) a = fmax(a, red[0][q]), b = fmax(b, red[1][q]), c = fmax(c, red[2][q]);
+        if (g.dimx) atomic_max_nonneg(&f.lam[0], a);
+        if (g.dimy) atomic_max_nonneg(&f.lam[1], b);
+        if (g.dimz) atomic_max_nonneg(&f.lam[2], c);
+    }
+}
+
+template <bool COP, int NS>
+__global__ void __launch_bounds__(kThreads) k_states(Geo g, DevFields f, DevThermo th, double *__restrict__ UI,
+                                                     int ghost, int want_lam, int guard) {
+    if (guard && step_done(f)) return;
+    double lamx = 0.0, lamy = 0.0, lamz = 0.0;
+    states_body<COP, NS>(g, f, th, UI, ghost, want_lam, (long long)blockIdx.x * blockDim.x + threadIdx.x, lamx, lamy,
+                         lamz);
+    if (want_lam) lam_block_reduce(g, f, lamx, lamy, lamz);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -427,11 +441,11 @@ __device__ __forceinline__ double project(const double *lrow, int n, const doubl
 // and 4 along y (D = 0, 1) or z (D = 2), so the rows of a y or z stencil are shared in L1 by the
 // warps of a block. Returns false outside the face range.
 template <int D>
-__device__ __forceinline__ bool face_of_thread(const Geo &g, int &i, int &j, int &k) {
+__device__ __forceinline__ bool face_of(const Geo &g, int bx, int by, int bz, int &i, int &j, int &k) {
     const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
-    const int fi = blockIdx.x * 32 + threadIdx.x;
-    const int fj = D == 2 ? (int)blockIdx.y : (int)(blockIdx.y * 4 + threadIdx.y);
-    const int fk = D == 2 ? (int)(blockIdx.z * 4 + threadIdx.y) : (int)blockIdx.z;
+    const int fi = bx * 32 + threadIdx.x;
+    const int fj = D == 2 ? by : by * 4 + (int)threadIdx.y;
+    const int fk = D == 2 ? bz * 4 + (int)threadIdx.y : bz;
     if (fi >= nfx || fj >= nfy || fk >= nfz) return false;
     i = fi + g.Bx - (D == 0 ? 1 : 0);
     j = fj + g.By - (D == 1 ? 1 : 0);
@@ -439,21 +453,46 @@ __device__ __forceinline__ bool face_of_thread(const Geo &g, int &i, int &j, int
     return true;
 }
 template <int D>
-inline dim3 face_grid(const Geo &g) {
+__device__ __forceinline__ bool face_of_thread(const Geo &g, int &i, int &j, int &k) {
+    return face_of<D>(g, blockIdx.x, blockIdx.y, blockIdx.z, i, j, k);
+}
+template <int D>
+__host__ __device__ inline dim3 face_grid(const Geo &g) {
     const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
     if (D == 2) return dim3((nfx + 31) / 32, nfy, (nfz + 3) / 4);
     return dim3((nfx + 31) / 32, (nfy + 3) / 4, nfz);
 }
 
+// Face of a thread of a one-dimensional block of kThreads threads read as a tile of 2^ltx faces
+// along x by kThreads >> ltx faces along y (D = 0, 1) or z (D = 2); (bx, by, bz) is the tile.
+template <int D>
+__device__ __forceinline__ bool face_of_tile(const Geo &g, int bx, int by, int bz, int ltx, int &i, int &j, int &k) {
+    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
+    const int lx = (int)threadIdx.x & ((1 << ltx) - 1), ly = (int)threadIdx.x >> ltx, ty = kThreads >> ltx;
+    const int fi = (bx << ltx) + lx;
+    const int fj = D == 2 ? by : by * ty + ly;
+    const int fk = D == 2 ? bz * ty + ly : bz;
+    if (fi >= nfx || fj >= nfy || fk >= nfz) return false;
+    i = fi + g.Bx - (D == 0 ? 1 : 0);
+    j = fj + g.By - (D == 1 ? 1 : 0);
+    k = fk + g.Bz - (D == 2 ? 1 : 0);
+    return true;
+}
+template <int D>
+__host__ __device__ inline dim3 face_grid_tile(const Geo &g, int ltx) {
+    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
+    const int tx = 1 << ltx, ty = kThreads >> ltx;
+    if (D == 2) return dim3((nfx + tx - 1) / tx, nfy, (nfz + ty - 1) / ty);
+    return dim3((nfx + tx - 1) / tx, (nfy + ty - 1) / ty, nfz);
+}
+
 template <int D, bool COP, int NS, int ORDER>
-__global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevThermo th, const double *__restrict__ UI,
-                                                    int artificial, const double *__restrict__ glf_d, int guard) {
+__device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, const DevThermo &th,
+                                           const double *__restrict__ UI, int artificial,
+                                           const double *__restrict__ glf_d, int i, int j, int k) {
     using S = Sys<COP, NS>;
     constexpr int E = S::E;
-    if (guard && step_done(f)) return;
     const long long P = g.pitch;
-    int i, j, k;
-    if (!face_of_thread<D>(g, i, j, k)) return;
     const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
     const long long idl = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long idr = idl + stride;
@@ -537,6 +576,15 @@ __global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevTherm
     for (int n = 0; n < E; n++) Fw[n * P + idl] = acc[n];
 }
 
+template <int D, bool COP, int NS, int ORDER>
+__global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevThermo th, const double *__restrict__ UI,
+                                                    int artificial, const double *__restrict__ glf_d, int guard) {
+    if (guard && step_done(f)) return;
+    int i, j, k;
+    if (!face_of_thread<D>(g, i, j, k)) return;
+    faces_body<D, COP, NS, ORDER>(g, f, th, UI, artificial, glf_d, i, j, k);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Flux divergence (UpdateFluidLU, Reconstruction_kernels.hpp:201-234) fused with the SSP-RK3
 // stage (UpdateURK3rdKernel, Update_kernels.hpp:64-94) and the NaN / Inf / negative density check
@@ -544,19 +592,15 @@ __global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevTherm
 // dt_dev != nullptr reads dt from the device (graph replay), else dt is the argument.
 // ---------------------------------------------------------------------------------------------
 template <int E>
-__global__ void __launch_bounds__(kThreads) k_div_rk(Geo g, DevFields f, int flag, double dt_arg,
-                                                     const double *__restrict__ dt_dev, int do_rk, int store_lu,
-                                                     int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void div_rk_body(const Geo &g, const DevFields &f, int flag, double dt, int do_rk,
+                                            int store_lu, long long t) {
     const long long P = g.pitch;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
     const int i = (int)(t % g.Xi) + g.Bx;
     const long long r = t / g.Xi;
     const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
     const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long sy = g.Xmax, sz = (long long)g.Xmax * g.Ymax;
-    const double dt = dt_dev ? dt_dev[0] : dt_arg;
     int code = 0;
 #pragma unroll
     for (int n = 0; n < E; n++) {
@@ -587,6 +631,15 @@ __global__ void __launch_bounds__(kThreads) k_div_rk(Geo g, DevFields f, int fla
         atomicOr(&f.err[ERR_STATE], 1);
         f.err[ERR_I] = i, f.err[ERR_J] = j, f.err[ERR_K] = k;
     }
+}
+
+template <int E>
+__global__ void __launch_bounds__(kThreads) k_div_rk(Geo g, DevFields f, int flag, double dt_arg,
+                                                     const double *__restrict__ dt_dev, int do_rk, int store_lu,
+                                                     int guard) {
+    if (guard && step_done(f)) return;
+    div_rk_body<E>(g, f, flag, dt_dev ? dt_dev[0] : dt_arg, do_rk, store_lu,
+                   (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // SSP-RK3 stage from a stored LU (UpdateURK3rdKernel, Update_kernels.hpp:64-94), inner cells.
@@ -640,7 +693,7 @@ __global__ void __launch_bounds__(kThreads) k_estimate_nan(Geo g, const double *
 // One-thread kernel: dt = CFL / sum(lambda_d / delta_d) from the maxima of the last k_states,
 // clipped to the target time as XFLUIDS::Evolution does (src/XFLUIDS.cpp:196-200); resets the
 // maxima; marks the step done when the target time is reached.
-static __global__ void k_dt_step(Geo g, DevFields f, double cfl) {
+__device__ __forceinline__ void dt_step_body(const Geo &g, const DevFields &f, double cfl) {
     double *b = f.dtbuf;
     if (b[4] != 0.0) return;
     const double t = b[1], target = b[2];
@@ -660,6 +713,7 @@ static __global__ void k_dt_step(Geo g, DevFields f, double cfl) {
     b[3] += 1.0;
     f.lam[0] = f.lam[1] = f.lam[2] = 0ull;
 }
+static __global__ void k_dt_step(Geo g, DevFields f, double cfl) { dt_step_body(g, f, cfl); }
 
 }  // namespace XFG_KNS
 }  // namespace xfg

@@ -16,14 +16,12 @@ namespace XFG_KNS {
 // Primitive recovery of the mixed form. Single gas: from the FP64 state converted once to FP32.
 // Mixture: the FP64 recovery of k_states (Newton in FP64), followed by the FP32 copies.
 template <bool COP, int NS>
-__global__ void __launch_bounds__(kThreads) k_states_mixed(Geo g, DevFields f, DevThermo th, double *__restrict__ UI,
-                                                           int ghost, int want_lam, int guard) {
+__device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields &f, const DevThermo &th,
+                                                  double *__restrict__ UI, int ghost, int want_lam, long long id,
+                                                  float &lamx, float &lamy, float &lamz) {
     using S = Sys<COP, NS>;
     constexpr int E = S::E, NCOP = S::NCOP;
-    if (guard && step_done(f)) return;
     const long long P = g.pitch, N = g.ncell();
-    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    float lamx = 0.f, lamy = 0.f, lamz = 0.f;
     if (id < N) {
         float Uf[E];
         float rho, u, v, w, p, H, c;
@@ -118,25 +116,36 @@ __global__ void __launch_bounds__(kThreads) k_states_mixed(Geo g, DevFields f, D
             if (!(lamz >= 0.f)) lamz = __int_as_float(0x7f800000);
         }
     }
-    if (want_lam) {
+}
+
+__device__ __forceinline__ void lam_block_reduce_f(const Geo &g, const DevFields &f, float lamx, float lamy, float lamz) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            lamx = fmaxf(lamx, __shfl_xor_sync(0xffffffffu, lamx, o));
-            lamy = fmaxf(lamy, __shfl_xor_sync(0xffffffffu, lamy, o));
-            lamz = fmaxf(lamz, __shfl_xor_sync(0xffffffffu, lamz, o));
-        }
-        __shared__ float red[3][kThreads / 32];
-        const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        if (lane == 0) red[0][wid] = lamx, red[1][wid] = lamy, red[2][wid] = lamz;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            float a = red[0][0], b = red[1][0], c = red[2][0];
-            for (int q = 1; q < kThreads / 32; q++) a = fmaxf(a, red[0][q]), b = fmaxf(b, red[1][q]), c = fmaxf(c, red[2][q]);
-            if (g.dimx) atomic_max_nonneg(&f.lam[0], (double)a);
-            if (g.dimy) atomic_max_nonneg(&f.lam[1], (double)b);
-            if (g.dimz) atomic_max_nonneg(&f.lam[2], (double)c);
-        }
+    for (int o = 16; o > 0; o >>= 1) {
+        lamx = fmaxf(lamx, __shfl_xor_sync(0xffffffffu, lamx, o));
+        lamy = fmaxf(lamy, __shfl_xor_sync(0xffffffffu, lamy, o));
+        lamz = fmaxf(lamz, __shfl_xor_sync(0xffffffffu, lamz, o));
     }
+    __shared__ float red[3][kThreads / 32];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) red[0][wid] = lamx, red[1][wid] = lamy, red[2][wid] = lamz;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = red[0][0], b = red[1][0], c = red[2][0];
+        for (int q = 1; q < (int)(blockDim.x >> 5); q++) a = fmaxf(a, red[0][q]), b = fmaxf(b, red[1][q]), c = fmaxf(c, red[2][q]);
+        if (g.dimx) atomic_max_nonneg(&f.lam[0], (double)a);
+        if (g.dimy) atomic_max_nonneg(&f.lam[1], (double)b);
+        if (g.dimz) atomic_max_nonneg(&f.lam[2], (double)c);
+    }
+}
+
+template <bool COP, int NS>
+__global__ void __launch_bounds__(kThreads) k_states_mixed(Geo g, DevFields f, DevThermo th, double *__restrict__ UI,
+                                                           int ghost, int want_lam, int guard) {
+    if (guard && step_done(f)) return;
+    float lamx = 0.f, lamy = 0.f, lamz = 0.f;
+    states_mixed_body<COP, NS>(g, f, th, UI, ghost, want_lam, (long long)blockIdx.x * blockDim.x + threadIdx.x, lamx,
+                               lamy, lamz);
+    if (want_lam) lam_block_reduce_f(g, f, lamx, lamy, lamz);
 }
 
 template <int D, int E>
@@ -172,14 +181,11 @@ __device__ __forceinline__ float project_r(const float *lrow, int n, const float
 
 // FP32 characteristic WENO flux at face (i+1/2) of direction D (same structure as k_faces).
 template <int D, bool COP, int NS, int ORDER>
-__global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, DevThermo th, int artificial,
-                                                          const double *__restrict__ glf_d, int guard) {
+__device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &f, const DevThermo &th, int artificial,
+                                                 const double *__restrict__ glf_d, int i, int j, int k) {
     using S = Sys<COP, NS>;
     constexpr int E = S::E;
-    if (guard && step_done(f)) return;
     const long long P = g.pitch;
-    int i, j, k;
-    if (!face_of_thread<D>(g, i, j, k)) return;
     const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
     const long long idl = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long idr = idl + stride;
@@ -294,21 +300,26 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
     for (int n = 0; n < E; n++) Fw[n * P + idl] = acc[n];
 }
 
+template <int D, bool COP, int NS, int ORDER>
+__global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, DevThermo th, int artificial,
+                                                          const double *__restrict__ glf_d, int guard) {
+    if (guard && step_done(f)) return;
+    int i, j, k;
+    if (!face_of_thread<D>(g, i, j, k)) return;
+    faces_mixed_body<D, COP, NS, ORDER>(g, f, th, artificial, glf_d, i, j, k);
+}
+
 // Divergence of the FP32 face fluxes, accumulated into the FP64 state by the RK stage.
 template <int E>
-__global__ void __launch_bounds__(kThreads) k_div_rk_mixed(Geo g, DevFields f, int flag, double dt_arg,
-                                                           const double *__restrict__ dt_dev, int do_rk, int store_lu,
-                                                           int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void div_rk_mixed_body(const Geo &g, const DevFields &f, int flag, double dt, int do_rk,
+                                                  int store_lu, long long t) {
     const long long P = g.pitch;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
     const int i = (int)(t % g.Xi) + g.Bx;
     const long long r = t / g.Xi;
     const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
     const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long sy = g.Xmax, sz = (long long)g.Xmax * g.Ymax;
-    const double dt = dt_dev ? dt_dev[0] : dt_arg;
     const float fdx = (float)g._dx, fdy = (float)g._dy, fdz = (float)g._dz;
     int code = 0;
 #pragma unroll
@@ -340,6 +351,15 @@ __global__ void __launch_bounds__(kThreads) k_div_rk_mixed(Geo g, DevFields f, i
         atomicOr(&f.err[ERR_STATE], 1);
         f.err[ERR_I] = i, f.err[ERR_J] = j, f.err[ERR_K] = k;
     }
+}
+
+template <int E>
+__global__ void __launch_bounds__(kThreads) k_div_rk_mixed(Geo g, DevFields f, int flag, double dt_arg,
+                                                           const double *__restrict__ dt_dev, int do_rk, int store_lu,
+                                                           int guard) {
+    if (guard && step_done(f)) return;
+    div_rk_mixed_body<E>(g, f, flag, dt_dev ? dt_dev[0] : dt_arg, do_rk, store_lu,
+                         (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 }  // namespace XFG_KNS

@@ -1,0 +1,187 @@
+"""Continuous-batching request server for independent solves.
+
+A request is one XFLUIDS run of its own grid to its own end time (a 1D two-state or a 2D
+four-quadrant Riemann problem, WENO5 LLF, SSP-RK3). Requests arrive on a seeded Poisson trace.
+The server owns one Ensemble whose device pool is the HBM budget; the state of every admitted
+request stays resident on the device until it finishes. The loop alternates
+
+  1. admit: waiting requests, in arrival order, take a slot while a slot and pool memory are free
+     (xfg_ensemble_add, which also runs the request's first BoundaryCondition + UpdateStates);
+  2. run: `chunk` fused steps of every admitted request, one batched launch sequence per step,
+     replayed from a CUDA graph (re-captured only when membership changed);
+  3. retire: requests that reached their end time are copied out and leave, freeing their slot
+     and memory for the queue.
+
+Requests arriving while others run are admitted at the next chunk boundary, so their work
+overlaps on the device with the requests already running. Time to solution = completion time -
+arrival time (queueing + service), measured on the host wall clock from the trace start. In
+replay mode (realtime=False, for tests) one request joins per chunk and its clock starts when it
+joins.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import cases
+from .abi import LLF
+from .ensemble import Ensemble
+from .mesh import make_scheme
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str            # "1d" or "2d"
+    n: int               # cells per side
+    t_end: float
+    arrival: float       # seconds after the trace start
+    block: object = None
+    U: np.ndarray = None
+    # filled by the server
+    start: float = float("nan")     # arrival on the server clock (the enqueue time in replay mode)
+    admitted: float = float("nan")
+    done: float = float("nan")
+    steps: int = 0
+    t: float = 0.0
+    error: int = 0
+    result: np.ndarray = field(default=None, repr=False)
+
+    @property
+    def cells(self) -> int:
+        return self.n if self.kind == "1d" else self.n * self.n
+
+    @property
+    def tts(self) -> float:
+        return self.done - self.start
+
+
+def make_request(rid, kind, n, t_end, arrival, rng, precision=0) -> Request:
+    """Build the grid and initial state of one request; states are drawn like the ensemble's
+    (rho in U[0.1,2], u,v in U[-1,1], p in U[0.05,2])."""
+    if kind == "1d":
+        q = cases.riemann_states(rng)
+        b, _, _, U, _ = cases.riemann1d(n, (q[0, 0], q[0, 1], q[0, 3]), (q[1, 0], q[1, 1], q[1, 3]),
+                                        precision=precision)
+    else:
+        b, _, _, U, _ = cases.riemann2d(n, cases.riemann_states(rng), precision=precision)
+    return Request(rid, kind, int(n), float(t_end), float(arrival), b, np.ascontiguousarray(U).reshape(-1))
+
+
+def poisson_trace(count, rate=200.0, seed=0, lo=8.0, hi=11.0, frac_2d=0.5, t_lo=0.1, t_hi=0.3, n_max=None):
+    """The first `count` requests of a seeded Poisson stream: exponential inter-arrival times of
+    mean 1/rate, 1D or 2D with probability frac_2d, cells per side round(2^U[lo,hi]), end time
+    U[t_lo,t_hi]. n_max caps the size (small test traces only)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for rid in range(count):
+        t += rng.exponential(1.0 / rate)
+        kind = "2d" if rng.uniform() < frac_2d else "1d"
+        n = int(np.rint(2.0 ** rng.uniform(lo, hi)))
+        if n_max:
+            n = min(n, n_max)
+        out.append(make_request(rid, kind, n, rng.uniform(t_lo, t_hi), t, rng))
+    return out
+
+
+def serving_scheme(precision=0):
+    return make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=precision)
+
+
+class Server:
+    def __init__(self, precision=0, hbm_budget=32 << 30, capacity=64, chunk=16, device=0, keep_results=True):
+        self.scheme = serving_scheme(precision)
+        self.ens = Ensemble(self.scheme, capacity=capacity, pool_bytes=int(hbm_budget), device=device)
+        self.capacity, self.chunk, self.keep = capacity, chunk, keep_results
+        self.device_ms = 0.0
+        self.chunks = 0
+        self.max_running = 0
+
+    def close(self):
+        self.ens.close()
+
+    def run(self, trace, realtime=True):
+        """Serve `trace` (Requests sorted by arrival) to completion. realtime=False replays the
+        arrivals in order without waiting for the wall clock (tests)."""
+        pending = list(trace)
+        waiting, running = [], {}
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        while pending or waiting or running:
+            clock = now()
+            while pending and (pending[0].arrival <= clock or not realtime):
+                r = pending.pop(0)
+                r.start = r.arrival if realtime else clock
+                waiting.append(r)
+                if not realtime:
+                    break
+            # admit in arrival order while slots and memory allow
+            while waiting:
+                r = waiting[0]
+                if Ensemble.member_bytes(r.block, self.scheme.precision) > self.ens.pool_bytes:
+                    raise ValueError(f"request {r.rid} ({r.kind} {r.n}) does not fit the HBM budget")
+                slot = self.ens.add(r.block, r.U, r.t_end)
+                if slot is None:
+                    break
+                r.admitted = now()
+                running[slot] = waiting.pop(0)
+            if not running:
+                if pending and realtime:
+                    time.sleep(max(0.0, pending[0].arrival - now()))
+                continue
+            self.max_running = max(self.max_running, len(running))
+            _, ms = self.ens.advance(self.chunk)
+            self.device_ms += ms
+            self.chunks += 1
+            clock = now()
+            for slot in list(running):
+                st = self.ens.status(slot)
+                if st["done"] or st["error"] or st["t"] >= running[slot].t_end:
+                    r = running.pop(slot)
+                    r.done, r.steps, r.t, r.error = clock, st["steps"], st["t"], st["error"]
+                    if self.keep:
+                        r.result = self.ens.get_state(slot)
+                    self.ens.remove(slot)
+        return trace
+
+
+def summary(trace, wall_s=None, device_ms=None):
+    tts = np.array([r.tts for r in trace])
+    work = float(sum(r.cells * r.steps for r in trace))
+    span = max(r.done for r in trace) - min(r.start for r in trace)
+    out = {"requests": len(trace), "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
+           "max_s": float(tts.max()), "makespan_s": float(span), "cell_updates": work,
+           "cell_updates_per_s": work / span, "errors": int(sum(1 for r in trace if r.error))}
+    if device_ms is not None:
+        out["device_s"] = device_ms * 1e-3
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description="serve a seeded Poisson trace of Riemann solves")
+    ap.add_argument("--requests", type=int, default=12)
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--budget-gb", type=float, default=32.0)
+    ap.add_argument("--chunk", type=int, default=16)
+    a = ap.parse_args()
+    prec = 1 if a.precision == "mixed" else 0
+    trace = poisson_trace(a.requests, a.rate, a.seed)
+    srv = Server(prec, hbm_budget=int(a.budget_gb * (1 << 30)), chunk=a.chunk, keep_results=False)
+    try:
+        srv.run(trace)
+        s = summary(trace, device_ms=srv.device_ms)
+    finally:
+        srv.close()
+    s.update({"precision": a.precision, "rate": a.rate, "seed": a.seed})
+    print(json.dumps(s))
+
+
+if __name__ == "__main__":
+    main()
