@@ -27,6 +27,7 @@ import numpy as np  # noqa: E402
 
 # DRAM bytes per face of the FP64 x-face kernel measured by ncu on a small case, scaled per face
 # (profiles/k_faces_fp64_vortex.md); None until a capture exists.
+THERMO_JSON = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "thermo_tables.json")
 NCU_FACE_BYTES_FP64 = None
 
 
@@ -262,6 +263,49 @@ def bench_serving(local, count, precision, fp64_check_work=3e8):
     return out
 
 
+def bench_mixing_layer(args, local, steps):
+    """3D inert temporal mixing layer (512 x 256 x 256, 5 species H2/O2/N2/H2O/AR, 7-coefficient
+    thermo of the reference's runtime.dat, WENO7 LLF), FP64 and mixed from the same state: one
+    warm-up step (graph capture), a reset, then `steps` timed steps; relative L1 / Linf of the
+    mixed state against the FP64 state at the same step count."""
+    from xfluids_gb300 import thermo
+    from xfluids_gb300.abi import MIXED
+    from xfluids_gb300.fluid import Fluid
+    th = thermo.load_thermal(cases_mod().MIXING_SPECIES, 0, tables_json=THERMO_JSON)
+    b, s, th, U, T = cases_mod().mixing_layer((512, 256, 256), thermal=th)
+    res, states = {}, {}
+    for prec in (0, MIXED):
+        s.precision = prec
+        f = Fluid(b, s, th, device=local)
+        f.InitialU(U, T)
+        f.initialize()
+        f.advance(1)
+        f.InitialU(U, T)
+        f.initialize()
+        f.time = 0.0
+        st, t, k, ms = f.advance_timed(steps)
+        cells = b.X_inner * b.Y_inner * b.Z_inner
+        res["fp64" if prec == 0 else "mixed"] = {"value": cells * k / (ms * 1e-3), "ms_per_step": ms / k,
+                                                 "steps": k, "status": st, "t": t}
+        states[prec] = f.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 9)[b.inner_slices()].reshape(-1, 9)
+        f.close()
+    d = np.abs(states[MIXED] - states[0])
+    scale = np.abs(states[0]).mean(axis=0)
+    live = scale > 0  # the H2O density is zero in this mixing layer (no reaction)
+    d, states[0], scale = d[:, live], states[0][:, live], scale[live]
+    res.update({"workload": "3D temporal mixing layer 512x256x256, 5 species, WENO7-JS LLF, SSP-RK3, CFL 0.5",
+                "cells": b.X_inner * b.Y_inner * b.Z_inner,
+                "mixed_speedup_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+                "l1_rel_mixed_vs_fp64": float((d.mean(axis=0) / scale).max()),
+                "linf_rel_mixed_vs_fp64": float((d.max(axis=0) / np.abs(states[0]).max(axis=0)).max())})
+    return res
+
+
+def cases_mod():
+    from xfluids_gb300 import cases
+    return cases
+
+
 def run_gpu_arm(args, world, rank, local):
     from xfluids_gb300 import cases
     from xfluids_gb300.abi import MIXED
@@ -366,6 +410,7 @@ def run_gpu_arm(args, world, rank, local):
                "linf_mixed_vs_fp64": float(max(x.max() for x in diff))}
         del s64, smx, diff
     serving = bench_serving(local, args.serve_requests, MIXED) if args.serve_requests > 0 else None
+    mixing = bench_mixing_layer(args, local, args.mixing_steps) if args.mixing_steps > 0 else None
     d.close()
     if rank != 0:
         return 0
@@ -398,6 +443,7 @@ def run_gpu_arm(args, world, rank, local):
                   "fp32_peak_tflops": peaks["fp32_flops"] / 1e12},
         "ensemble": ens or None,
         "serving": serving,
+        "mixing_layer": mixing,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-updates/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_steps} steps of the 1024^2 vortex ({cpu_el:.1f} s) on the oracle restatement"},
         "clocks": clk.summary(),
@@ -417,6 +463,7 @@ def main():
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--ensemble", type=int, default=1, help="run the 256-member batched ensemble (0 = skip)")
     ap.add_argument("--serve-requests", type=int, default=8, help="requests of the serving trace (0 = skip)")
+    ap.add_argument("--mixing-steps", type=int, default=2, help="timed steps of the 3D mixing layer (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()

@@ -171,7 +171,9 @@ def mixing_layer(shape=(512, 256, 256), thermal=None, length=0.01, seed=1234, pr
     b = make_block((nx, ny, nz), dom, [PERIODIC, PERIODIC, ybc, ybc, PERIODIC, PERIODIC], cfl=0.5)
     s = make_scheme(cop=True, num_species=5, scheme_order=order, artificial_type=LLF, thermo=thermo_kind,
                     ghost_species=False, precision=precision)
-    X, Y, Z = cell_centres(b)
+    # the mean state depends on y only: build it on the y column, then broadcast (same values as
+    # evaluating every cell)
+    Y = (np.arange(b.Ymax) - b.Bwidth_Y + 0.5) * b.dy
     ymid = 0.5 * dom[1]
     wgt = 0.5 * (1.0 + np.tanh((Y - ymid) / (0.01 * length)))  # 1 upper, 0 lower
     y_up = np.array([0.0, 0.233, 0.767, 0.0, 0.0])
@@ -188,15 +190,25 @@ def mixing_layer(shape=(512, 256, 256), thermal=None, length=0.01, seed=1234, pr
     c = np.sqrt(gam * Rmix * T)
     c_up = float(np.sqrt(gam.max() * Rmix.min() * 1200.0))
     c_lo = float(np.sqrt(gam.min() * Rmix.max() * 300.0))
-    u = wgt * (0.6 * c_up) + (1.0 - wgt) * (-0.6 * c_lo)
+    u0 = wgt * (0.6 * c_up) + (1.0 - wgt) * (-0.6 * c_lo)
+    col = lambda a: a[None, :, None]  # (Zmax, Ymax, Xmax) broadcast of a y column
     kk, jj, ii = np.meshgrid(np.arange(b.Zmax), np.arange(b.Ymax), np.arange(b.Xmax), indexing="ij")
-    amp = noise * c
-    u = u + amp * _hash_uniform(seed, ii, jj, kk)
+    amp = col(noise * c)
+    u = col(u0) + amp * _hash_uniform(seed, ii, jj, kk)
     v = amp * _hash_uniform(seed + 1, ii, jj, kk)
     w = amp * _hash_uniform(seed + 2, ii, jj, kk)
+    del kk, jj, ii
     e = h - Rmix * T
-    Et = rho * (e + 0.5 * (u * u + v * v + w * w))
-    U = np.concatenate([np.stack([rho, rho * u, rho * v, rho * w, Et], axis=-1),
-                        rho[..., None] * Ys[..., :4]], axis=-1)
-    U = np.ascontiguousarray(U.reshape(-1, 9))
+    rho3 = np.broadcast_to(col(rho), u.shape)
+    Et = rho3 * (col(e) + 0.5 * (u * u + v * v + w * w))
+    U = np.empty(u.shape + (9,))
+    U[..., 0] = rho3
+    U[..., 1] = rho3 * u
+    U[..., 2] = rho3 * v
+    U[..., 3] = rho3 * w
+    U[..., 4] = Et
+    for n in range(4):
+        U[..., 5 + n] = col(rho * Ys[..., n])
+    U = U.reshape(-1, 9)
+    T = np.ascontiguousarray(np.broadcast_to(col(T), u.shape))
     return b, s, thermal, U, np.ascontiguousarray(T.reshape(-1))

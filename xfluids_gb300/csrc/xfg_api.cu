@@ -177,6 +177,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     const size_t arr8 = (size_t)h->P * 8, arr4 = align_up((size_t)h->P * 4, 256);
     // layout of the pool
     size_t nd = 3 * E + 12 + (scheme->cop ? NS : 0);           // U, U1, LU, primitives, y
+    if (scheme->cop) nd += 3 + (NS - 1);                        // per-cell sound-speed terms
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;  // single-gas fast path extras
     if (fast1) nd += 2 + 3 * (block->DimX + block->DimY + block->DimZ);
     for (int d = 0; d < 3; d++)
@@ -207,7 +208,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     f.U = take8(E), f.U1 = take8(E), f.LU = take8(E);
     f.rho = take8(1), f.u = take8(1), f.v = take8(1), f.w = take8(1), f.p = take8(1), f.H = take8(1);
     f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
-    if (scheme->cop) f.y = take8(NS);
+    if (scheme->cop) f.y = take8(NS), f.xc = take8(3 + (NS - 1));
     if (fast1) {
         f.sr = take8(1), f.isr = take8(1);
         for (int d = 0; d < 3; d++)

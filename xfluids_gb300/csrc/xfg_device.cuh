@@ -71,6 +71,8 @@ struct DevFields {
     float *Fwf[3];             // FP32 face fluxes (mixed form)
     double *sr, *isr;          // sqrt(rho) and 1/sqrt(rho) per cell (single-gas FP64 fast path)
     double *eab[3];            // |u_d - c|, |u_d|, |u_d + c| per cell and direction (same path)
+    double *xc;                // mixtures: per-cell terms of the interface sound speed (3 + NCOP
+                               // components, see cop_cell_terms); null = the faces compute them
     unsigned long long *lam;   // dt wave-speed maxima (3 x bit patterns of non-negative doubles)
     double *dtbuf;             // [0] dt of the step, [1] time, [2] target time, [3] steps done
     int *err;                  // error words: [0] state NaN code, [1] primitive error, [2] i, [3] j, [4] k

@@ -104,6 +104,35 @@ __global__ void __launch_bounds__(kThreads) k_bc(Geo g, double *__restrict__ U, 
 // EstimatePrimitiveVarKernel (Estimate_kernels.hpp); the GetDt maxima of |u_d| + sqrt(1.4 p/rho)
 // over all cells (GlobalDt_block.hpp:31-66) when want_lam.
 // ---------------------------------------------------------------------------------------------
+// Per-cell terms of the multi-component interface sound speed (SoundSpeedMultiSpecies,
+// Utils_device.hpp:42-140): the cell halves of every Roe-weighted average the face forms, with the
+// reference's expressions, so a face reading them gets the values it would compute itself.
+//   xc[0] gamma = Cp / (Cp - Ru / W)           xc[1] (gamma - 1) (q^2/2 - h_N + Cp R_N T / R)
+//   xc[2] e = H - q^2/2 - p / rho               xc[3 + n] (gamma - 1) ((h_N - h_n) + Cp (R_n - R_N) T / R)
+template <int NS>
+__device__ __forceinline__ void cop_cell_terms(const DevThermo &th, const double *yi, double T, double Cp, double u,
+                                               double v, double w, double H, double p, double rho, double *xc,
+                                               long long P, long long id) {
+    constexpr int NCOP = NS - 1;
+    double h[NS];
+#pragma unroll
+    for (int n = 0; n < NS; n++) h[n] = enthalpy(th, T, n);
+    const double wi = mix_W_inv<NS>(th, yi);
+    const double gm = Cp / (Cp - kRu * wi);
+    const double q2 = u * u + v * v + w * w;
+    const double Rm = wi * kRu;
+    const double RN = th.Ri[NCOP];
+    const double RNT = RN * T;
+    xc[id] = gm;
+    xc[P + id] = (gm - 1.0) * (0.5 * q2 - h[NCOP] + Cp * RNT / Rm);
+    xc[2 * P + id] = H - 0.5 * q2 - p / rho;
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) {
+        const double Rin_RN = th.Ri[n] - RN;
+        xc[(3 + n) * P + id] = (gm - 1.0) * ((-h[n] + h[NCOP]) + Cp * Rin_RN * T / Rm);
+    }
+}
+
 template <bool COP, int NS>
 __device__ __forceinline__ void states_body(const Geo &g, const DevFields &f, const DevThermo &th,
                                             double *__restrict__ UI, int ghost, int want_lam, long long id,
@@ -156,6 +185,7 @@ __device__ __forceinline__ void states_body(const Geo &g, const DevFields &f, co
         const double c = sqrt(gamma * p * rho1);
         f.rho[id] = rho, f.u[id] = u, f.v[id] = v, f.w[id] = w, f.p[id] = p, f.H[id] = H, f.c[id] = c;
         f.e[id] = tme, f.gamma[id] = gamma;
+        if (COP && f.xc) cop_cell_terms<NS>(th, yi, T, Cp, u, v, w, H, p, rho, f.xc, P, id);
         if (!COP && !XFG_STRICT_BUILD && f.sr) {  // inputs of the single-gas fast face kernel
             const double isr = rsqrt_nr(rho);
             f.isr[id] = isr;
@@ -322,38 +352,53 @@ __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, con
         F._yi[0] = 1.0;
     } else {
         constexpr int NCOP = NS - 1;
-        double yl[NS], yr[NS], hl[NS], hr[NS];
-        const double Tl = f.T[l], Tr = f.T[r];
+        double yl[NS], yr[NS];
 #pragma unroll
         for (int n = 0; n < NS; n++) {
             yl[n] = f.y[n * P + l];
             yr[n] = f.y[n * P + r];
-            hl[n] = enthalpy(th, Tl, n);
-            hr[n] = enthalpy(th, Tr, n);
             F._yi[n] = (yl[n] + D * yr[n]) * D1;
         }
-        const double Cpl = mix_Cp<NS>(th, yl, Tl), Cpr = mix_Cp<NS>(th, yr, Tr);
-        const double wl_ = mix_W_inv<NS>(th, yl), wr_ = mix_W_inv<NS>(th, yr);
-        const double gl = Cpl / (Cpl - kRu * wl_), gr = Cpr / (Cpr - kRu * wr_);  // get_CopGamma(yi, T)
-        Gamma0 = (gl + D * gr) * D1;
-        const double q2l = ul * ul + vl * vl + wl * wl, q2r = ur * ur + vr * vr + wr * wr;
-        const double Rl = wl_ * kRu, Rr = wr_ * kRu;
-        const double el = Hl - 0.5 * q2l - pl / rl, er = Hr - 0.5 * q2r - pr / rr;
-        const double RN = th.Ri[NCOP];
-        auto dpdrho = [&](double hN, double q2, double Cp, double Rm, double T, double gm) {
-            double RNT = RN * T;
-            return (gm - 1.0) * (0.5 * q2 - hN + Cp * RNT / Rm);
-        };
-        const double _dpdrho = (dpdrho(hl[NCOP], q2l, Cpl, Rl, Tl, gl) + D * dpdrho(hr[NCOP], q2r, Cpr, Rr, Tr, gr)) * D1;
+        // cell terms (cop_cell_terms): gamma, dp/drho, e, dp/drho_i of each side
+        double gl, gr, el, er, _dpdrho;
         double dpdrhoi[NCOP > 0 ? NCOP : 1], drhoi[NCOP > 0 ? NCOP : 1];
+        if (f.xc) {
+            const double *xc = f.xc;
+            gl = xc[l], gr = xc[r];
+            _dpdrho = (xc[P + l] + D * xc[P + r]) * D1;
+            el = xc[2 * P + l], er = xc[2 * P + r];
 #pragma unroll
-        for (int n = 0; n < NCOP; n++) {
-            const double Rin_RN = th.Ri[n] - RN;
-            const double a = (gl - 1.0) * ((-hl[n] + hl[NCOP]) + Cpl * Rin_RN * Tl / Rl);
-            const double b = (gr - 1.0) * ((-hr[n] + hr[NCOP]) + Cpr * Rin_RN * Tr / Rr);
-            dpdrhoi[n] = (a + D * b) * D1;
-            drhoi[n] = rr * yr[n] - rl * yl[n];
+            for (int n = 0; n < NCOP; n++) {
+                dpdrhoi[n] = (xc[(3 + n) * P + l] + D * xc[(3 + n) * P + r]) * D1;
+                drhoi[n] = rr * yr[n] - rl * yl[n];
+            }
+        } else {
+            double hl[NS], hr[NS];
+            const double Tl = f.T[l], Tr = f.T[r];
+#pragma unroll
+            for (int n = 0; n < NS; n++) hl[n] = enthalpy(th, Tl, n), hr[n] = enthalpy(th, Tr, n);
+            const double Cpl = mix_Cp<NS>(th, yl, Tl), Cpr = mix_Cp<NS>(th, yr, Tr);
+            const double wl_ = mix_W_inv<NS>(th, yl), wr_ = mix_W_inv<NS>(th, yr);
+            gl = Cpl / (Cpl - kRu * wl_), gr = Cpr / (Cpr - kRu * wr_);  // get_CopGamma(yi, T)
+            const double q2l = ul * ul + vl * vl + wl * wl, q2r = ur * ur + vr * vr + wr * wr;
+            const double Rl = wl_ * kRu, Rr = wr_ * kRu;
+            el = Hl - 0.5 * q2l - pl / rl, er = Hr - 0.5 * q2r - pr / rr;
+            const double RN = th.Ri[NCOP];
+            auto dpdrho = [&](double hN, double q2, double Cp, double Rm, double T, double gm) {
+                double RNT = RN * T;
+                return (gm - 1.0) * (0.5 * q2 - hN + Cp * RNT / Rm);
+            };
+            _dpdrho = (dpdrho(hl[NCOP], q2l, Cpl, Rl, Tl, gl) + D * dpdrho(hr[NCOP], q2r, Cpr, Rr, Tr, gr)) * D1;
+#pragma unroll
+            for (int n = 0; n < NCOP; n++) {
+                const double Rin_RN = th.Ri[n] - RN;
+                const double a = (gl - 1.0) * ((-hl[n] + hl[NCOP]) + Cpl * Rin_RN * Tl / Rl);
+                const double b = (gr - 1.0) * ((-hr[n] + hr[NCOP]) + Cpr * Rin_RN * Tr / Rr);
+                dpdrhoi[n] = (a + D * b) * D1;
+                drhoi[n] = rr * yr[n] - rl * yl[n];
+            }
         }
+        Gamma0 = (gl + D * gr) * D1;
         const double _prho = (pl / rl + D * (pr / rr)) * D1 +
                              0.5 * D * D1 * D1 * ((ur - ul) * (ur - ul) + (vr - vl) * (vr - vl) + (wr - wl) * (wr - wl));
         const double _dpdE = ((gl - 1.0) + D * (gr - 1.0)) * D1;
