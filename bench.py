@@ -28,7 +28,9 @@ import numpy as np  # noqa: E402
 # DRAM bytes per face of the FP64 x-face kernel measured by ncu on a small case, scaled per face
 # (profiles/k_faces_fp64_vortex.md); None until a capture exists.
 THERMO_JSON = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "thermo_tables.json")
-NCU_FACE_BYTES_FP64 = None
+# DRAM bytes per face of the FP64 x-face kernel: 674.2 MB read + 152.8 MB written in one ncu
+# capture of the 2048^2 vortex (4.196 M faces); traffic grows with the faces of a launch
+NCU_FACE_BYTES_FP64 = (674.218496e6 + 152.813568e6) / (2049 * 2048)
 
 
 def dist_env():
@@ -433,6 +435,7 @@ def run_gpu_arm(args, world, rank, local):
         "roofline": {"bound": "fp64", "kernel": "k_faces<x> (FP64 characteristic WENO5 face flux)",
                      "achieved": achieved / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
                      "frac": achieved / 1e12 / fp64_peak, "traffic": traffic,
+                     "traffic_note": "DRAM bytes per launch, ncu capture of the 2048^2 vortex scaled by faces",
                      "algorithmic_flops_per_face": fpf, "faces_per_launch": faces_per_launch,
                      "launch_ms": face_launch_ms,
                      "peak_source": "measured FP64 FMA chain on this GPU (xfg_measure_pipe_peaks); MEASURED_PEAKS.json has no FP64 figure"},
