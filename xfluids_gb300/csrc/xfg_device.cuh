@@ -328,32 +328,41 @@ __device__ __forceinline__ double weno5_body(double v1, double v2, double v3, do
     return (s1 + s2 + s3);
 }
 // FP64 fast form of the body: the same smoothness indicators, weights and candidates arranged for
-// fused multiply-adds; returns the weighted candidate sum and the weight sum separately (the
-// caller normalises both sides of a face with one reciprocal each).
+// fused multiply-adds. The indicators are carried as s_k / 13 (13 a^2 + 3 b^2 + eps, all over 13):
+// the weights are homogeneous of degree zero in the s_k, so the factor cancels. The linear
+// weights d_k and the 1/6 of the candidates are folded into the candidate coefficients. Returns
+// the weighted candidate sum and the weight sum separately (the caller normalises both sides of a
+// face with one reciprocal).
+constexpr double kW313 = 3.0 / 13.0, kWeps13 = 1.0e-6 / 13.0;
+constexpr double kQ1a = 0.1 * 2.0 / 6.0, kQ1b = 0.1 * -7.0 / 6.0, kQ1c = 0.1 * 11.0 / 6.0;
+constexpr double kQ2a = -0.1, kQ2b = 0.5, kQ2c = 0.2;         // 0.6 / 6 * (-1, 5, 2)
+constexpr double kQ3a = 0.1, kQ3b = 0.25, kQ3c = -0.05;       // 0.3 / 6 * (2, 5, -1)
 __device__ __forceinline__ void weno5_body_nd(double v1, double v2, double v3, double v4, double v5, double &num,
                                               double &den) {
     double a = fma(-2.0, v2, v1) + v3;
     double b = fma(3.0, v3, fma(-4.0, v2, v1));
-    const double s1 = fma(13.0 * a, a, fma(3.0 * b, b, 1.0E-6));
+    const double s1 = fma(a, a, fma(kW313 * b, b, kWeps13));
     a = fma(-2.0, v3, v2) + v4;
     b = v2 - v4;
-    const double s2 = fma(13.0 * a, a, fma(3.0 * b, b, 1.0E-6));
+    const double s2 = fma(a, a, fma(kW313 * b, b, kWeps13));
     a = fma(-2.0, v4, v3) + v5;
-    b = fma(-4.0, v4, 3.0 * v3) + v5;
-    const double s3 = fma(13.0 * a, a, fma(3.0 * b, b, 1.0E-6));
+    b = fma(3.0, v3, fma(-4.0, v4, v5));
+    const double s3 = fma(a, a, fma(kW313 * b, b, kWeps13));
     const double p23 = s2 * s3, p13 = s1 * s3, p12 = s1 * s2;
-    const double a1 = 0.1 * p23 * p23, a2 = 0.6 * p13 * p13, a3 = 0.3 * p12 * p12;
-    const double q1 = fma(11.0, v3, fma(-7.0, v2, 2.0 * v1));
-    const double q2 = fma(2.0, v4, fma(5.0, v3, -v2));
-    const double q3 = fma(5.0, v4, fma(2.0, v3, -v5));
-    num = fma(a3, q3, fma(a2, q2, a1 * q1));
-    den = a1 + a2 + a3;
+    const double P1 = p23 * p23, P2 = p13 * p13, P3 = p12 * p12;
+    const double q1 = fma(kQ1c, v3, fma(kQ1b, v2, kQ1a * v1));
+    const double q2 = fma(kQ2c, v4, fma(kQ2b, v3, kQ2a * v2));
+    const double q3 = fma(kQ3c, v5, fma(kQ3b, v4, kQ3a * v3));
+    num = fma(P3, q3, fma(P2, q2, P1 * q1));
+    den = fma(0.3, P3, fma(0.6, P2, 0.1 * P1));
 }
+// nf / df + nm / dm with one reciprocal: for indicators s_k between 1e-6 and 1e17 each weight sum
+// lies in [1e-30, 1e64] and their product in [1e-60, 1e128], far from overflow and subnormals
 __device__ __forceinline__ double weno5_fast(const double *pp, const double *mm) {
     double nf, df, nm, dm;
     weno5_body_nd(pp[1], pp[2], pp[3], pp[4], pp[5], nf, df);
     weno5_body_nd(mm[6], mm[5], mm[4], mm[3], mm[2], nm, dm);
-    return fma(nf, rcp_nr(df), nm * rcp_nr(dm)) * kSix;
+    return fma(nf, dm, nm * df) * rcp_nr(df * dm);
 }
 
 // FP32 form: the same candidates and smoothness indicators; the weights use the division form
