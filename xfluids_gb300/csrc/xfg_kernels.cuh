@@ -531,6 +531,109 @@ __host__ __device__ inline dim3 face_grid_tile(const Geo &g, int ltx) {
     return dim3((nfx + tx - 1) / tx, (nfy + ty - 1) / ty, nfz);
 }
 
+// Single-gas WENO5 face of the FP64 fast path with the eigenvector products factored. For a
+// single gas (b3 = 0) the rows of L (RoeAverageLeft_x/y/z) share their partial sums: with
+// T.x = u x1 + v x2 + w x3 - x4, A.x = b2/2 x0 - b1/2 T.x and B.x = (un x0 - x_{D+1}) / (2c),
+// row 0 is A + B, row E-1 is A - B, the entropy row D+1 is ent0 x0 + T.x and the two shear rows
+// are one fused multiply-add each. The columns of R (RoeAverageRight_*) factor the same way:
+// with S = fl0 + fl4, Sb = S + b1 fl_{D+1} and Dc = c (fl4 - fl0), component 0 is Sb, a velocity
+// component k is vel_k Sb (+ Dc for k = D+1, +- the shear flux otherwise) and the energy is
+// H Sb + un Dc - fl_{D+1} + the shear terms. Same operations as the general body, regrouped.
+template <int D>
+__device__ __forceinline__ void faces_fast5_body(const Geo &g, const DevFields &f, const DevThermo &th,
+                                                 const double *__restrict__ UI, int artificial,
+                                                 const double *__restrict__ glf_d, int i, int j, int k) {
+    const long long P = g.pitch;
+    const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
+    const long long idl = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    const long long idr = idl + stride;
+    FaceState<1> F;
+    face_state_fast(f, th, idl, idr, F);
+    const double vel[3] = {F._u, F._v, F._w};
+    const double un = vel[D];
+    const double *__restrict__ Fl = f.F[D];
+    // artificial viscosity of the acoustic fields (0, 4) and of the others (1..3)
+    double a0, a1, a4;
+    if (artificial == XFG_LLF) {
+        const double *__restrict__ ea = f.eab[D];
+        a0 = 0.0, a1 = 0.0, a4 = 0.0;
+#pragma unroll
+        for (int m = -2; m <= 3; m++) {
+            const long long q = idl + m * stride;
+            a0 = fmax(a0, __ldg(ea + q));
+            a1 = fmax(a1, __ldg(ea + P + q));
+            a4 = fmax(a4, __ldg(ea + 2 * P + q));
+        }
+    } else if (artificial == XFG_ROE) {
+        a0 = fabs(un - F._c), a1 = fabs(un), a4 = fabs(un + F._c);
+    } else {
+        a0 = glf_d[0], a1 = glf_d[1], a4 = glf_d[2];
+    }
+    const double h0 = 0.5 * a0, h1 = 0.5 * a1, h4 = 0.5 * a4;
+    const double hb1 = 0.5 * F.b1, hb2 = 0.5 * F.b2, hc1 = 0.5 * F._c1, ent0 = F.ent0;
+    // acoustic and entropy fields
+    double p0[8], m0[8], p1[8], m1[8], p4[8], m4[8];
+#pragma unroll
+    for (int m = -2; m <= 3; m++) {
+        const long long q = idl + m * stride;
+        double pa[2][3];  // [U, F][row 0, row D+1, row 4]
+#pragma unroll
+        for (int a = 0; a < 2; a++) {
+            const double *__restrict__ A = a == 0 ? UI : Fl;
+            const double x0 = __ldg(A + q), x1 = __ldg(A + P + q), x2 = __ldg(A + 2 * P + q);
+            const double x3 = __ldg(A + 3 * P + q), x4 = __ldg(A + 4 * P + q);
+            const double xd = D == 0 ? x1 : (D == 1 ? x2 : x3);
+            const double t = fma(F._u, x1, fma(F._v, x2, fma(F._w, x3, -x4)));
+            const double av = fma(hb2, x0, -hb1 * t);
+            const double bv = hc1 * fma(un, x0, -xd);
+            pa[a][0] = av + bv;
+            pa[a][1] = fma(ent0, x0, t);
+            pa[a][2] = av - bv;
+        }
+        const double f0 = 0.5 * pa[1][0], f1 = 0.5 * pa[1][1], f4 = 0.5 * pa[1][2];
+        p0[m + 3] = fma(h0, pa[0][0], f0), m0[m + 3] = fma(-h0, pa[0][0], f0);
+        p1[m + 3] = fma(h1, pa[0][1], f1), m1[m + 3] = fma(-h1, pa[0][1], f1);
+        p4[m + 3] = fma(h4, pa[0][2], f4), m4[m + 3] = fma(-h4, pa[0][2], f4);
+    }
+    const double fl0 = weno5_fast(p0, m0), fl1 = weno5_fast(p1, m1), fl4 = weno5_fast(p4, m4);
+    // shear fields: sa along the first transverse velocity, sb along the second
+    // (x: v, w; y: u, w; z: u, v); row of sa: (c_a x0 + s_a x_ka), with the signs of RoeAverageLeft
+    constexpr int ka = D == 0 ? 2 : 1, kb = D == 2 ? 2 : 3;
+    const double va = vel[ka - 1], vb = vel[kb - 1];
+    // left rows: x (v,0,-1,0,0), (-w,0,0,1,0); y (-u,1,0,0,0), (w,0,0,-1,0); z (u,-1,0,0,0), (-v,0,1,0,0)
+    constexpr double sa = D == 1 ? 1.0 : -1.0, sb = D == 0 ? 1.0 : (D == 1 ? -1.0 : 1.0);
+    double pa_[8], ma_[8], pb_[8], mb_[8];
+#pragma unroll
+    for (int m = -2; m <= 3; m++) {
+        const long long q = idl + m * stride;
+        const double ua = fma(-sa * va, __ldg(UI + q), sa * __ldg(UI + ka * P + q));
+        const double fa = fma(-sa * va, __ldg(Fl + q), sa * __ldg(Fl + ka * P + q));
+        const double ub = fma(-sb * vb, __ldg(UI + q), sb * __ldg(UI + kb * P + q));
+        const double fb = fma(-sb * vb, __ldg(Fl + q), sb * __ldg(Fl + kb * P + q));
+        const double hfa = 0.5 * fa, hfb = 0.5 * fb;
+        pa_[m + 3] = fma(h1, ua, hfa), ma_[m + 3] = fma(-h1, ua, hfa);
+        pb_[m + 3] = fma(h1, ub, hfb), mb_[m + 3] = fma(-h1, ub, hfb);
+    }
+    const double fla = weno5_fast(pa_, ma_), flb = weno5_fast(pb_, mb_);
+    // right eigenvectors: columns of the shear fields carry sa (sb) at component ka (kb) and
+    // sa va (sb vb) in the energy, as RoeAverageRight_*
+    const double S = fl0 + fl4;
+    const double Sb = fma(F.b1, fl1, S);
+    const double Dc = F._c * (fl4 - fl0);
+    double acc[5];
+    acc[0] = Sb;
+#pragma unroll
+    for (int c = 1; c <= 3; c++) {
+        if (c == D + 1) acc[c] = fma(vel[c - 1], Sb, Dc);
+        else if (c == ka) acc[c] = fma(vel[c - 1], Sb, sa * fla);
+        else acc[c] = fma(vel[c - 1], Sb, sb * flb);
+    }
+    acc[4] = fma(F._H, Sb, fma(un, Dc, fma(sa * va, fla, fma(sb * vb, flb, -fl1))));
+    double *Fw = f.Fw[D];
+#pragma unroll
+    for (int n = 0; n < 5; n++) Fw[n * P + idl] = acc[n];
+}
+
 template <int D, bool COP, int NS, int ORDER>
 __device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, const DevThermo &th,
                                            const double *__restrict__ UI, int artificial,
@@ -547,6 +650,12 @@ __device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, con
     // (a handle without those arrays gets the general form)
     constexpr bool FAST_BUILD = !COP && !XFG_STRICT_BUILD;
     const bool FAST = FAST_BUILD && f.sr && f.isr && f.eab[D];
+    if constexpr (FAST_BUILD && ORDER == 5) {
+        if (FAST) {
+            faces_fast5_body<D>(g, f, th, UI, artificial, glf_d, i, j, k);
+            return;
+        }
+    }
     FaceState<NS> F;
     double Gamma0;
     if (FAST_BUILD && FAST) {
