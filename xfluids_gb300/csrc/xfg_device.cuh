@@ -365,6 +365,44 @@ __device__ __forceinline__ double weno5_fast(const double *pp, const double *mm)
     return fma(nf, dm, nm * df) * rcp_nr(df * dm);
 }
 
+// Form of the body for doubled inputs v' = 2 v (the split fluxes f +- a u without the factor 1/2)
+// written around the centre value: each candidate is q_k / 6 = v3 + r_k with
+// r_1 = a_1/12 + b_1/4, r_2 = a_2/12 - b_2/4, r_3 = a_3/12 - b_3/4 (a_k, b_k the differences of the
+// smoothness indicators), so that with weights summing to one WENO(v) = v3 + sum w_k r_k. Doubling
+// the input multiplies the indicators by 4: with eps scaled by 4 the weights are unchanged and
+// WENO(v) = WENO'(v') / 2; the 1/2 and the linear weights d_k are folded into the r coefficients.
+constexpr double kWeps13x4 = 4.0 * kWeps13;
+constexpr double kRa1 = 0.5 * 0.1 / 12.0, kRb1 = 0.5 * 0.1 / 4.0;
+constexpr double kRa2 = 0.5 * 0.6 / 12.0, kRb2 = -0.5 * 0.6 / 4.0;
+constexpr double kRa3 = 0.5 * 0.3 / 12.0, kRb3 = -0.5 * 0.3 / 4.0;
+__device__ __forceinline__ void weno5_body_r(double v1, double v2, double v3, double v4, double v5, double &num,
+                                             double &den) {
+    const double a1 = fma(-2.0, v2, v1) + v3;
+    const double b1 = fma(3.0, v3, fma(-4.0, v2, v1));
+    const double s1 = fma(a1, a1, fma(kW313 * b1, b1, kWeps13x4));
+    const double a2 = fma(-2.0, v3, v2) + v4;
+    const double b2 = v2 - v4;
+    const double s2 = fma(a2, a2, fma(kW313 * b2, b2, kWeps13x4));
+    const double a3 = fma(-2.0, v4, v3) + v5;
+    const double b3 = fma(3.0, v3, fma(-4.0, v4, v5));
+    const double s3 = fma(a3, a3, fma(kW313 * b3, b3, kWeps13x4));
+    const double p23 = s2 * s3, p13 = s1 * s3, p12 = s1 * s2;
+    const double P1 = p23 * p23, P2 = p13 * p13, P3 = p12 * p12;
+    const double r1 = fma(kRa1, a1, kRb1 * b1);
+    const double r2 = fma(kRa2, a2, kRb2 * b2);
+    const double r3 = fma(kRa3, a3, kRb3 * b3);
+    num = fma(P3, r3, fma(P2, r2, P1 * r1));
+    den = fma(0.3, P3, fma(0.6, P2, 0.1 * P1));
+}
+// WENO5 face flux (both sides) from the doubled split fluxes pp2 = f + a u, mm2 = f - a u
+// (indices m + 3 for stencil offsets m = -2..3), one reciprocal for both sides
+__device__ __forceinline__ double weno5_fast2(const double *pp2, const double *mm2) {
+    double nf, df, nm, dm;
+    weno5_body_r(pp2[1], pp2[2], pp2[3], pp2[4], pp2[5], nf, df);
+    weno5_body_r(mm2[6], mm2[5], mm2[4], mm2[3], mm2[2], nm, dm);
+    return fma(0.5, pp2[3] + mm2[4], fma(nf, dm, nm * df) * rcp_nr(df * dm));
+}
+
 // FP32 form: the same candidates and smoothness indicators; the weights use the division form
 // d_k / s_k^2 (equal to the product form) so that s^4 cannot overflow single precision.
 __device__ __forceinline__ float weno5_body(float v1, float v2, float v3, float v4, float v5) {

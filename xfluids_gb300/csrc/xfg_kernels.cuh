@@ -538,7 +538,8 @@ __host__ __device__ inline dim3 face_grid_tile(const Geo &g, int ltx) {
 // are one fused multiply-add each. The columns of R (RoeAverageRight_*) factor the same way:
 // with S = fl0 + fl4, Sb = S + b1 fl_{D+1} and Dc = c (fl4 - fl0), component 0 is Sb, a velocity
 // component k is vel_k Sb (+ Dc for k = D+1, +- the shear flux otherwise) and the energy is
-// H Sb + un Dc - fl_{D+1} + the shear terms. Same operations as the general body, regrouped.
+// H Sb + un Dc - fl_{D+1} + the shear terms. The split fluxes enter WENO doubled (f +- a u,
+// weno5_fast2). The same flux as the general body, with the operations regrouped.
 template <int D>
 __device__ __forceinline__ void faces_fast5_body(const Geo &g, const DevFields &f, const DevThermo &th,
                                                  const double *__restrict__ UI, int artificial,
@@ -569,9 +570,8 @@ __device__ __forceinline__ void faces_fast5_body(const Geo &g, const DevFields &
     } else {
         a0 = glf_d[0], a1 = glf_d[1], a4 = glf_d[2];
     }
-    const double h0 = 0.5 * a0, h1 = 0.5 * a1, h4 = 0.5 * a4;
     const double hb1 = 0.5 * F.b1, hb2 = 0.5 * F.b2, hc1 = 0.5 * F._c1, ent0 = F.ent0;
-    // acoustic and entropy fields
+    // acoustic and entropy fields; split fluxes doubled (f +- a u), see weno5_fast2
     double p0[8], m0[8], p1[8], m1[8], p4[8], m4[8];
 #pragma unroll
     for (int m = -2; m <= 3; m++) {
@@ -590,12 +590,11 @@ __device__ __forceinline__ void faces_fast5_body(const Geo &g, const DevFields &
             pa[a][1] = fma(ent0, x0, t);
             pa[a][2] = av - bv;
         }
-        const double f0 = 0.5 * pa[1][0], f1 = 0.5 * pa[1][1], f4 = 0.5 * pa[1][2];
-        p0[m + 3] = fma(h0, pa[0][0], f0), m0[m + 3] = fma(-h0, pa[0][0], f0);
-        p1[m + 3] = fma(h1, pa[0][1], f1), m1[m + 3] = fma(-h1, pa[0][1], f1);
-        p4[m + 3] = fma(h4, pa[0][2], f4), m4[m + 3] = fma(-h4, pa[0][2], f4);
+        p0[m + 3] = fma(a0, pa[0][0], pa[1][0]), m0[m + 3] = fma(-a0, pa[0][0], pa[1][0]);
+        p1[m + 3] = fma(a1, pa[0][1], pa[1][1]), m1[m + 3] = fma(-a1, pa[0][1], pa[1][1]);
+        p4[m + 3] = fma(a4, pa[0][2], pa[1][2]), m4[m + 3] = fma(-a4, pa[0][2], pa[1][2]);
     }
-    const double fl0 = weno5_fast(p0, m0), fl1 = weno5_fast(p1, m1), fl4 = weno5_fast(p4, m4);
+    const double fl0 = weno5_fast2(p0, m0), fl1 = weno5_fast2(p1, m1), fl4 = weno5_fast2(p4, m4);
     // shear fields: sa along the first transverse velocity, sb along the second
     // (x: v, w; y: u, w; z: u, v); row of sa: (c_a x0 + s_a x_ka), with the signs of RoeAverageLeft
     constexpr int ka = D == 0 ? 2 : 1, kb = D == 2 ? 2 : 3;
@@ -610,11 +609,10 @@ __device__ __forceinline__ void faces_fast5_body(const Geo &g, const DevFields &
         const double fa = fma(-sa * va, __ldg(Fl + q), sa * __ldg(Fl + ka * P + q));
         const double ub = fma(-sb * vb, __ldg(UI + q), sb * __ldg(UI + kb * P + q));
         const double fb = fma(-sb * vb, __ldg(Fl + q), sb * __ldg(Fl + kb * P + q));
-        const double hfa = 0.5 * fa, hfb = 0.5 * fb;
-        pa_[m + 3] = fma(h1, ua, hfa), ma_[m + 3] = fma(-h1, ua, hfa);
-        pb_[m + 3] = fma(h1, ub, hfb), mb_[m + 3] = fma(-h1, ub, hfb);
+        pa_[m + 3] = fma(a1, ua, fa), ma_[m + 3] = fma(-a1, ua, fa);
+        pb_[m + 3] = fma(a1, ub, fb), mb_[m + 3] = fma(-a1, ub, fb);
     }
-    const double fla = weno5_fast(pa_, ma_), flb = weno5_fast(pb_, mb_);
+    const double fla = weno5_fast2(pa_, ma_), flb = weno5_fast2(pb_, mb_);
     // right eigenvectors: columns of the shear fields carry sa (sb) at component ka (kb) and
     // sa va (sb vb) in the energy, as RoeAverageRight_*
     const double S = fl0 + fl4;
