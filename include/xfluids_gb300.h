@@ -84,6 +84,9 @@ typedef struct xfg_scheme {
     int ghost_species;     /* GhostSpecies: renormalise Y and write it back into U */
     double ncop_gamma;     /* NCOP_Gamma, ratio of specific heats without COP */
     int precision;         /* xfg_precision */
+    int positivity;        /* PositivityPreserving (src/read_ini/settings/read_json.cpp:68): the flux
+                              limiter of FDM_Method/positive-definite_eigen/PositivityPreserving_kernels.hpp
+                              after each face sweep (ConVenction_block.hpp:328-410); 0 = off */
 } xfg_scheme;
 
 /* Arrays a caller can read back (xfg_get_array). */

@@ -23,6 +23,8 @@ PRIMS = ["rho", "p", "u", "v", "w", "c", "H", "T"]
 FLAVOURS = {
     "ncop_w5_llf": (5, 1), "ncop_w7_llf": (5, 1), "ncop_w5_roe": (5, 1), "ncop_w5_glf": (5, 1),
     "cop4g_w5_llf_nasa": (8, 4), "cop5_w7_llf_janaf": (9, 5),
+    # built with PositivityPreserving on (-DPOSP=1, and the JSON key below)
+    "ncop_w5_llf_pp": (5, 1), "cop5_w5_llf_janaf_pp": (9, 5),
 }
 
 
@@ -30,7 +32,7 @@ def available(flavour: str) -> bool:
     return os.access(os.path.join(REF_DIR, flavour, "xfluids_ref"), os.X_OK)
 
 
-def _case_json(block, cfl, domain):
+def _case_json(block, cfl, domain, positivity=False):
     res = [block.X_inner if block.DimX else 0, block.Y_inner if block.DimY else 0,
            block.Z_inner if block.DimZ else 0]
     return {
@@ -38,7 +40,7 @@ def _case_json(block, cfl, domain):
                 "nOutMax": 0, "OutInterval": 100000000, "OutBoundary": 0, "CFLnumber": cfl, "OutDAT": 0,
                 "OutVTI": 0, "UseAdvRange": False, "OutTimeStamps": ["1000.0: {-C=X,0.0,0.0;-V=rho,P,T}"]},
         "mpi": {"mx": 1, "my": 1, "mz": 1, "DeviceSelect": [1, 0, 0]},
-        "equations": {"Sources_React": False, "PositivityPreserving": False},
+        "equations": {"Sources_React": False, "PositivityPreserving": bool(positivity)},
         "sources": {},
         "mesh": {"DOMAIN_Size": list(domain), "Resolution": res, "Boundarys": [int(b) for b in block.Boundarys],
                  "Ghost_width": [block.Bwidth_X or 4, block.Bwidth_Y or 4, block.Bwidth_Z or 4]},
@@ -58,7 +60,7 @@ def run_reference(flavour, block, U, T=None, steps=1, t_end=1e300, domain=None):
     U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
     assert U.size == E * N
     with open(os.path.join(REF_DIR, flavour, "case.json"), "w") as f:
-        json.dump(_case_json(block, block.CFLnumber, domain), f)
+        json.dump(_case_json(block, block.CFLnumber, domain, positivity=flavour.endswith("_pp")), f)
     with tempfile.TemporaryDirectory() as d:
         fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
         with open(fin, "wb") as f:

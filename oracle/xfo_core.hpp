@@ -844,12 +844,81 @@ void lu_divergence(const Config &cf, Fields<R> &f) {
             }
 }
 
+// PositivityPreservingKernel, FDM_Method/positive-definite_eigen/PositivityPreserving_kernels.hpp:5-76,
+// launched per direction over the inner cells after all face sweeps (ConVenction_block.hpp:328-410):
+// the face i+1/2 of inner cell i is blended toward the Lax-Friedrichs flux with
+// lambda_0 = uvw_c_max[d] (the maxima of the last GetDt) and lambda = CFL / lambda_0, first for
+// the density floor min(rho, 1e-13) of both neighbours, then (mixtures) for each mass fraction
+// with floor 0. The theta of each species blends the already blended face flux, while the
+// predicted states of the species test keep the density-corrected FF.
+template <class R>
+inline R pp_min(R a, R b) { return (b < a) ? b : a; }  // sycl::min of the shim
+template <class R>
+void pp_limit(const Config &cf, Fields<R> &f, const std::vector<R> &UI, int d) {
+    const xfg_block &b = cf.bl;
+    const int E = cf.E(), NCOP = cf.NCOP();
+    const size_t stride = d == 0 ? 1 : (d == 1 ? (size_t)b.Xmax : (size_t)b.Xmax * b.Ymax);
+    const std::vector<R> &Fl = d == 0 ? f.FluxF : (d == 1 ? f.FluxG : f.FluxH);
+    std::vector<R> &Fw = f.Fw[d];
+    const R lambda_0 = f.uvw_c_max[d];
+    const R lambda = R(b.CFLnumber) / lambda_0;
+    const R eps_rho = R(1.0e-13), eps_y = R(0.0);
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = b.Bwidth_Z; k < b.Z_inner + b.Bwidth_Z; k++)
+        for (int j = b.Bwidth_Y; j < b.Y_inner + b.Bwidth_Y; j++)
+            for (int i = b.Bwidth_X; i < b.X_inner + b.Bwidth_X; i++) {
+                const size_t id_l = (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i, id_r = id_l + stride;
+                const R *UU = &UI[E * id_l], *UP = &UI[E * id_r];
+                const R *Fll = &Fl[E * id_l], *Flr = &Fl[E * id_r];
+                R *Fwall = &Fw[E * id_l];
+                R F_LF[kMaxE], FF_LF[kMaxE], FF[kMaxE];
+                for (int n = 0; n < E; n++) {
+                    F_LF[n] = R(0.5) * (Fll[n] + Flr[n] + lambda_0 * (UU[n] - UP[n]));
+                    FF_LF[n] = R(2.0) * lambda * F_LF[n];
+                    FF[n] = R(2.0) * lambda * Fwall[n];
+                }
+                R theta_u = R(1.0), theta_p = R(1.0);
+                R rho_min = pp_min(UU[0], eps_rho);
+                if (UU[0] - FF[0] < rho_min) theta_u = (UU[0] - FF_LF[0] - rho_min) / (FF[0] - FF_LF[0]);
+                rho_min = pp_min(UP[0], eps_rho);
+                if (UP[0] + FF[0] < rho_min) theta_p = (UP[0] + FF_LF[0] - rho_min) / (FF_LF[0] - FF[0]);
+                R theta = pp_min(theta_u, theta_p);
+                for (int n = 0; n < E; n++) {
+                    FF[n] = (R(1.0) - theta) * FF_LF[n] + theta * FF[n];
+                    Fwall[n] = (R(1.0) - theta) * F_LF[n] + theta * Fwall[n];
+                }
+                if (NCOP > 0) {
+                    const R _rhoq = R(1.0) / (UU[0] - FF[0]), _rhou = R(1.0) / (UU[0] - FF_LF[0]);
+                    const R _rhoqp = R(1.0) / (UP[0] + FF[0]), _rhoup = R(1.0) / (UP[0] + FF_LF[0]);
+                    for (int n = 0; n < NCOP; n++) {
+                        const int tid = n + 5;
+                        const R yq = (UU[tid] - FF[tid]) * _rhoq, yu = (UU[tid] - FF_LF[tid]) * _rhou;
+                        const R yqp = (UP[tid] + FF[tid]) * _rhoqp, yup = (UP[tid] + FF_LF[tid]) * _rhoup;
+                        theta_u = R(1.0), theta_p = R(1.0);
+                        if (yq < eps_y) {
+                            const R yi_min = pp_min(yu, eps_y);
+                            theta_u = (yu - yi_min + R(1.0e-40)) / (yu - yq + R(1.0e-40));
+                        }
+                        if (yqp < eps_y) {
+                            const R yi_min = pp_min(yup, eps_y);
+                            theta_p = (yup - yi_min + R(1.0e-40)) / (yup - yqp + R(1.0e-40));
+                        }
+                        theta = pp_min(theta_u, theta_p);
+                        for (int nn = 0; nn < E; nn++) Fwall[nn] = (R(1.0) - theta) * F_LF[nn] + theta * Fwall[nn];
+                    }
+                }
+            }
+}
+
 template <class R>
 void compute_lu(const Config &cf, Fields<R> &f, const std::vector<R> &UI) {
     const int dims[3] = {cf.bl.DimX, cf.bl.DimY, cf.bl.DimZ};
     lu_eigen(cf, f);
     for (int d = 0; d < 3; d++)
         if (dims[d]) lu_faces(cf, f, UI, d);
+    if (cf.sc.positivity)
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) pp_limit(cf, f, UI, d);
     lu_divergence(cf, f);
 }
 

@@ -35,6 +35,12 @@ CASES = {
     "insert64_cop4_ghost_nasa_w5": ("cop4g_w5_llf_nasa", lambda: H.insert_st(64), (0.1, 1.0, 1.0)),
     "mixing5_12x8x6_janaf_w7": ("cop5_w7_llf_janaf", lambda: H.mixing_small((12, 8, 6)),
                                 (0.01, 0.01 * 8 / 12, 0.01 * 6 / 12)),
+    # PositivityPreserving on: cases where the limiter acts (without it the first two go negative)
+    "pp_riemann88_32_w5_llf": ("ncop_w5_llf_pp", H.with_positivity(lambda: H.riemann_member(88, 32)), None),
+    "pp_riemann1d108_w5_llf": ("ncop_w5_llf_pp", H.with_positivity(H.riemann1d_strong), None),
+    "pp_mixing5_12x8x6_janaf_w5": ("cop5_w5_llf_janaf_pp",
+                                   H.with_positivity(lambda: H.mixing_small((12, 8, 6), order=5)),
+                                   (0.01, 0.01 * 8 / 12, 0.01 * 6 / 12)),
 }
 
 
@@ -42,9 +48,11 @@ def block_fields(b):
     return {k: getattr(b, k) for k, _ in b._fields_ if k != "Boundarys"} | {"Boundarys": list(b.Boundarys)}
 
 
-def main():
+def main(only=None):
     subprocess.run(["bash", os.path.join(ROOT, "oracle", "ref", "build_ref.sh")], check=True)
     for name, (flav, mk, domain) in CASES.items():
+        if only and name not in only:
+            continue
         b, s, th, U, T = mk()
         recs = run_reference(flav, b, U, T, steps=2, domain=domain)
         E = s.Emax
@@ -67,4 +75,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -114,3 +114,26 @@ def insert_st(n=200, order=5, ghost=True, thermo_kind=1):
     return b, s, th, np.ascontiguousarray(U.reshape(-1, 8)), np.ascontiguousarray(T.reshape(-1))
 
 
+
+
+def riemann_member(q, n, seed=0):
+    """Quadrant states of member q of the seeded 256-member Riemann ensemble on an n^2 grid."""
+    _, rng = cases.ensemble_sizes(256, seed)
+    for _ in range(q):
+        cases.riemann_states(rng)
+    return cases.riemann2d(n, cases.riemann_states(rng))
+
+
+def with_positivity(mk):
+    def build():
+        b, s, th, U, T = mk()
+        s.positivity = 1
+        return b, s, th, U, T
+    return build
+
+
+def riemann1d_strong(n=108):
+    """1D two-state Riemann problem whose first RK stage drives the density negative without the
+    positivity limiter (rho, u, p) = (1.84, -0.494, 0.0911) | (0.189, -0.503, 0.656)."""
+    return cases.riemann1d(n, (1.8397073266913917, -0.4944626440950872, 0.09109694116558763),
+                           (0.18863925211238564, -0.5028604535820342, 0.6556118842537302))

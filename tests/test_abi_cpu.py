@@ -43,7 +43,8 @@ int main(void) {
     printf("%zu %zu %zu\n", sizeof(xfg_block), sizeof(xfg_thermal), sizeof(xfg_scheme));
     printf("%zu %zu %zu\n", offsetof(xfg_block, dx), offsetof(xfg_block, CFLnumber), offsetof(xfg_block, Boundarys));
     printf("%zu %zu\n", offsetof(xfg_thermal, Hia), offsetof(xfg_thermal, Hib));
-    printf("%zu %zu\n", offsetof(xfg_scheme, ncop_gamma), offsetof(xfg_scheme, precision));
+    printf("%zu %zu %zu\n", offsetof(xfg_scheme, ncop_gamma), offsetof(xfg_scheme, precision),
+           offsetof(xfg_scheme, positivity));
     return 0;
 }
 """
@@ -58,7 +59,7 @@ def test_struct_layouts_match_header():
         vals = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     B, T, S = abi.Block, abi.Thermal, abi.Scheme
     expect = [C.sizeof(B), C.sizeof(T), C.sizeof(S), B.dx.offset, B.CFLnumber.offset, B.Boundarys.offset,
-              T.Hia.offset, T.Hib.offset, S.ncop_gamma.offset, S.precision.offset]
+              T.Hia.offset, T.Hib.offset, S.ncop_gamma.offset, S.precision.offset, S.positivity.offset]
     assert vals == expect
 
 

@@ -72,6 +72,12 @@ CASES = {
     "insert_st_janaf_weno7": lambda: H.insert_st(100, order=7, ghost=False, thermo_kind=0),
     "mixing5_weno7_janaf": lambda: H.mixing_small(),
     "mixing5_weno5_nasa_roe": lambda: H.mixing_small((16, 12, 8), order=5, thermo_kind=1, artificial=ROE),
+    # positivity limiter on (cases where it acts: without it the first two turn negative)
+    "pp_riemann88": H.with_positivity(lambda: H.riemann_member(88, 32)),
+    "pp_riemann1d": H.with_positivity(H.riemann1d_strong),
+    "pp_mixing5_weno5_janaf": H.with_positivity(lambda: H.mixing_small((12, 8, 6), order=5)),
+    "pp_blast3d_weno7": H.with_positivity(lambda: H.blast3d(order=7)),
+    "pp_insert_st_ghost_nasa": H.with_positivity(lambda: H.insert_st(120)),
 }
 
 
@@ -82,7 +88,8 @@ def test_stagewise_parity(name, precision, cuda_lib):
     print(f"{name}: worst normwise relative difference {worst:.3e}")
 
 
-@pytest.mark.parametrize("name", ["vortex64", "blast3d_weno7_glf", "riemann2d_weno7_sym", "mixing5_weno7_janaf"])
+@pytest.mark.parametrize("name", ["vortex64", "blast3d_weno7_glf", "riemann2d_weno7_sym", "mixing5_weno7_janaf",
+                                  "pp_riemann88", "pp_mixing5_weno5_janaf"])
 def test_strict_is_bitwise(name, cuda_lib):
     """Without contraction the CUDA path performs the reference's operation sequence: every array
     of every stage is bit-identical to the oracle (no log/exp on these cases)."""
@@ -90,7 +97,8 @@ def test_strict_is_bitwise(name, cuda_lib):
     assert worst == 0.0
 
 
-@pytest.mark.parametrize("name", ["vortex64", "sod_weno5_llf", "mixing5_weno7_janaf", "blast3d_weno5"])
+@pytest.mark.parametrize("name", ["vortex64", "sod_weno5_llf", "mixing5_weno7_janaf", "blast3d_weno5", "pp_riemann88",
+                                  "pp_mixing5_weno5_janaf"])
 def test_fused_step_and_graph(name, cuda_lib):
     b, s, th, U, T = CASES[name]()
     E = s.Emax
@@ -178,3 +186,23 @@ def test_nan_detection(cuda_lib):
     st, t, dt = f.step()
     assert st > 0
     f.close()
+
+
+def test_positivity_limiter_acts_and_keeps_density_positive(cuda_lib):
+    """Without the limiter the first stage of this member drives the density negative (status
+    10000); with it the run goes on and the density stays positive, FP64 and mixed form."""
+    for prec in (FP64, MIXED):
+        b, s, th, U, T = H.riemann_member(88, 32)
+        s.precision = prec
+        f = _fluid(b, s, th, U, T)
+        f.initialize()
+        st, _, _ = f.advance(3)
+        assert st != 0
+        f.close()
+        s.positivity = 1
+        f = _fluid(b, s, th, U, T)
+        f.initialize()
+        st, t, n = f.advance(20)
+        assert st == 0 and n == 20
+        assert H.inner_aos(b, f.get("U"), 5)[:, 0].min() > 0.0
+        f.close()

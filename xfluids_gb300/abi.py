@@ -78,7 +78,7 @@ class Scheme(C.Structure):
     _fields_ = [
         ("cop", C.c_int), ("num_species", C.c_int), ("scheme_order", C.c_int),
         ("artificial_type", C.c_int), ("thermo", C.c_int), ("ghost_species", C.c_int),
-        ("ncop_gamma", C.c_double), ("precision", C.c_int),
+        ("ncop_gamma", C.c_double), ("precision", C.c_int), ("positivity", C.c_int),
     ]
 
     @property

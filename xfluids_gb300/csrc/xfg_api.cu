@@ -110,6 +110,7 @@ static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *
     if (s->scheme_order != 5 && s->scheme_order != 7) return fail(-1, "scheme_order must be 5 or 7 (got %d)", s->scheme_order);
     if (s->artificial_type < 1 || s->artificial_type > 3) return fail(-1, "artificial_type must be 1..3");
     if (s->precision < 0 || s->precision > 2) return fail(-1, "precision must be 0 (fp64), 1 (mixed) or 2 (fp64 strict)");
+    if (s->positivity != 0 && s->positivity != 1) return fail(-1, "positivity must be 0 or 1");
     if (s->cop && (s->num_species < 2 || s->num_species > XFG_MAX_SPECIES))
         return fail(-1, "num_species %d out of range for COP", s->num_species);
     if (!s->cop && s->num_species != 1) return fail(-1, "num_species must be 1 without COP");
@@ -249,6 +250,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     for (int q = 0; q < 6; q++) h->ctx.bc[q] = block->Boundarys[q];
     h->ctx.glf = scheme->artificial_type == XFG_GLF ? (const double *)h->glf : nullptr;
     h->ctx.precision = scheme->precision;
+    h->ctx.cfl = block->CFLnumber;
     e = cudaMallocHost(&h->host_dtbuf, 8 * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&h->host_err, 64 * sizeof(int));
     for (int q = 0; q < 4 && e == cudaSuccess; q++) e = cudaEventCreate(&h->ev[q]);
@@ -369,6 +371,9 @@ static void launch_lu(xfg_handle *h, double *UI, int guard) {
     if (h->sc.artificial_type == XFG_GLF) h->ops->glf(h->ctx, h->glf, guard);
     for (int d = 0; d < 3; d++)
         if (dims[d]) h->ops->faces(h->ctx, d, UI, guard);
+    if (h->sc.positivity)  // after all sweeps, ConVenction_block.hpp:328-410; lambda_0 in dtbuf[5..7]
+        for (int d = 0; d < 3; d++)
+            if (dims[d]) h->ops->pp(h->ctx, d, UI, h->ctx.f.dtbuf + 5, guard);
 }
 
 int xfg_compute_lu(xfg_handle *h, int flag, float *timers23) {
@@ -413,6 +418,9 @@ int xfg_get_dt(xfg_handle *h, double *dt) {
     for (int q = 0; q < 3; q++) std::memcpy(&l[q], &lam[q], 8);
     const double dtref = l[0] * h->bl._dx + l[1] * h->bl._dy + l[2] * h->bl._dz;
     *dt = h->bl.CFLnumber / dtref;
+    // the positivity limiter of the following stages uses these maxima (uvw_c_max, Fluids.cpp:899-908)
+    CK(cudaMemcpyAsync(h->ctx.f.dtbuf + 5, l, sizeof l, cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
     return 0;
 }
 

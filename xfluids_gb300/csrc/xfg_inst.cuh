@@ -80,11 +80,26 @@ struct Inst {
         k_estimate_nan<E><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, UI, c.f.LU, pos);
     }
 
+    template <int D>
+    static void pp_d(const LaunchCtx &c, const double *UI, const double *lam0, int guard) {
+        const long long n = (long long)c.g.Xi * c.g.Yi * c.g.Zi;
+        if (MIXED)
+            k_pp_mixed<D, COP, NS><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, UI, lam0, c.cfl, guard);
+        else
+            k_pp<D, COP, NS><<<grid_for(n, kThreads), kThreads, 0, c.st>>>(c.g, c.f, UI, lam0, c.cfl, guard);
+    }
+    static void pp(const LaunchCtx &c, int d, const double *UI, const double *lam0, int guard) {
+        if (d == 0) pp_d<0>(c, UI, lam0, guard);
+        else if (d == 1) pp_d<1>(c, UI, lam0, guard);
+        else pp_d<2>(c, UI, lam0, guard);
+    }
+
     // tables for scheme order 5 and 7, registered under precision id `prec`
     static const Ops *table(int order, int prec) {
         static Ops t[2][3];
         Ops &o = t[order == 7][prec];
-        o = Ops{COP ? 1 : 0, NS, order, prec, bc, states, order == 7 ? faces<7> : faces<5>, div_rk, glf, rk, estimate_nan};
+        o = Ops{COP ? 1 : 0, NS, order, prec, bc, states, order == 7 ? faces<7> : faces<5>, div_rk, glf, rk, estimate_nan,
+                pp};
         return &o;
     }
 };

@@ -745,6 +745,88 @@ __global__ void __launch_bounds__(kThreads) k_faces(Geo g, DevFields f, DevTherm
 }
 
 // ---------------------------------------------------------------------------------------------
+// Positivity-preserving flux limiter (PositivityPreservingKernel, FDM_Method/positive-definite_eigen/
+// PositivityPreserving_kernels.hpp:5-76), one thread per inner cell i and its face i+1/2 along D,
+// launched after the face sweeps (ConVenction_block.hpp:328-410). The face flux is blended toward
+// the Lax-Friedrichs flux 0.5 (F_l + F_r + lambda_0 (U_l - U_r)), lambda_0 = the GetDt wave-speed
+// maximum of the step along D and lambda = CFL / lambda_0, with the largest theta that keeps
+// rho_l - 2 lambda F and rho_r + 2 lambda F above min(rho, 1e-13); mixtures then limit each mass
+// fraction against 0 the same way. FT is the storage type of the fluxes (FP64, or FP32 in the
+// mixed form); the limiter computes in FP64.
+// ---------------------------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ R pp_min(R a, R b) { return (b < a) ? b : a; }
+
+template <int D, int E, int NCOP, class FT>
+__device__ __forceinline__ void pp_body(const Geo &g, const double *__restrict__ UI, const FT *__restrict__ Fl,
+                                        FT *__restrict__ Fw, double lambda_0, double lambda, long long t) {
+    if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
+    const long long P = g.pitch;
+    const int i = (int)(t % g.Xi) + g.Bx;
+    const long long r = t / g.Xi;
+    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
+    const long long l = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i, rr = l + stride;
+    double F_LF[E], FF_LF[E], FF[E], Fwall[E];
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        const double ul = UI[n * P + l], ur = UI[n * P + rr];
+        F_LF[n] = 0.5 * ((double)Fl[n * P + l] + (double)Fl[n * P + rr] + lambda_0 * (ul - ur));
+        FF_LF[n] = 2.0 * lambda * F_LF[n];
+        Fwall[n] = (double)Fw[n * P + l];
+        FF[n] = 2.0 * lambda * Fwall[n];
+    }
+    const double UU0 = UI[l], UP0 = UI[rr];
+    double theta_u = 1.0, theta_p = 1.0;
+    double rho_min = pp_min(UU0, 1.0e-13);
+    if (UU0 - FF[0] < rho_min) theta_u = (UU0 - FF_LF[0] - rho_min) / (FF[0] - FF_LF[0]);
+    rho_min = pp_min(UP0, 1.0e-13);
+    if (UP0 + FF[0] < rho_min) theta_p = (UP0 + FF_LF[0] - rho_min) / (FF_LF[0] - FF[0]);
+    double theta = pp_min(theta_u, theta_p);
+#pragma unroll
+    for (int n = 0; n < E; n++) {
+        FF[n] = (1.0 - theta) * FF_LF[n] + theta * FF[n];
+        Fwall[n] = (1.0 - theta) * F_LF[n] + theta * Fwall[n];
+    }
+    if (NCOP > 0) {
+        const double _rhoq = 1.0 / (UU0 - FF[0]), _rhou = 1.0 / (UU0 - FF_LF[0]);
+        const double _rhoqp = 1.0 / (UP0 + FF[0]), _rhoup = 1.0 / (UP0 + FF_LF[0]);
+#pragma unroll
+        for (int n = 0; n < NCOP; n++) {
+            const int tid = n + 5;
+            const double ul = UI[tid * P + l], ur = UI[tid * P + rr];
+            const double yq = (ul - FF[tid]) * _rhoq, yu = (ul - FF_LF[tid]) * _rhou;
+            const double yqp = (ur + FF[tid]) * _rhoqp, yup = (ur + FF_LF[tid]) * _rhoup;
+            theta_u = 1.0, theta_p = 1.0;
+            if (yq < 0.0) {
+                const double yi_min = pp_min(yu, 0.0);
+                theta_u = (yu - yi_min + 1.0e-40) / (yu - yq + 1.0e-40);
+            }
+            if (yqp < 0.0) {
+                const double yi_min = pp_min(yup, 0.0);
+                theta_p = (yup - yi_min + 1.0e-40) / (yup - yqp + 1.0e-40);
+            }
+            theta = pp_min(theta_u, theta_p);
+#pragma unroll
+            for (int nn = 0; nn < E; nn++) Fwall[nn] = (1.0 - theta) * F_LF[nn] + theta * Fwall[nn];
+        }
+    }
+#pragma unroll
+    for (int n = 0; n < E; n++) Fw[n * P + l] = (FT)Fwall[n];
+}
+
+// lam0: the step's GetDt maxima (3 doubles on the device: saved by k_dt_step, or by xfg_get_dt)
+template <int D, bool COP, int NS>
+__global__ void __launch_bounds__(kThreads) k_pp(Geo g, DevFields f, const double *__restrict__ UI,
+                                                 const double *__restrict__ lam0, double cfl, int guard) {
+    if (guard && step_done(f)) return;
+    using S = Sys<COP, NS>;
+    const double l0 = lam0[D];
+    pp_body<D, S::E, S::NCOP, double>(g, UI, f.F[D], f.Fw[D], l0, cfl / l0,
+                                      (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Flux divergence (UpdateFluidLU, Reconstruction_kernels.hpp:201-234) fused with the SSP-RK3
 // stage (UpdateURK3rdKernel, Update_kernels.hpp:64-94) and the NaN / Inf / negative density check
 // of EstimateFluidNANKernel (src/Fluids.cpp:43-86), on inner cells. store_lu keeps LU in memory.
@@ -870,6 +952,7 @@ __device__ __forceinline__ void dt_step_body(const Geo &g, const DevFields &f, d
     b[0] = dt;
     b[1] = t + dt;
     b[3] += 1.0;
+    b[5] = lx, b[6] = ly, b[7] = lz;  // lambda_0 of the positivity limiter during this step
     f.lam[0] = f.lam[1] = f.lam[2] = 0ull;
 }
 static __global__ void k_dt_step(Geo g, DevFields f, double cfl) { dt_step_body(g, f, cfl); }

@@ -311,6 +311,17 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
 }
 
 // Divergence of the FP32 face fluxes, accumulated into the FP64 state by the RK stage.
+// Positivity limiter of the mixed form: the FP32 physical and face fluxes, the FP64 state.
+template <int D, bool COP, int NS>
+__global__ void __launch_bounds__(kThreads) k_pp_mixed(Geo g, DevFields f, const double *__restrict__ UI,
+                                                       const double *__restrict__ lam0, double cfl, int guard) {
+    if (guard && step_done(f)) return;
+    using S = Sys<COP, NS>;
+    const double l0 = lam0[D];
+    pp_body<D, S::E, S::NCOP, float>(g, UI, f.Ff[D], f.Fwf[D], l0, cfl / l0,
+                                     (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 template <int E>
 __device__ __forceinline__ void div_rk_mixed_body(const Geo &g, const DevFields &f, int flag, double dt, int do_rk,
                                                   int store_lu, long long t) {

@@ -76,6 +76,8 @@ extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *
     if (scheme->scheme_order != 5 && scheme->scheme_order != 7) return fail(-1, "scheme_order must be 5 or 7");
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_FP64_STRICT)
         return fail(-1, "xfg_compute_lu_noalloc serves the FP64 forms (precision 0 or 2)");
+    if (scheme->positivity)
+        return fail(-1, "xfg_compute_lu_noalloc has no positivity limiter (it needs the step's GetDt maxima)");
     if (scheme->cop && !T) return fail(-1, "a mixture needs the temperature T (Newton warm start)");
     if (scheme->cop && (scheme->num_species < 2 || scheme->num_species > XFG_MAX_SPECIES || thermal->num_species != scheme->num_species))
         return fail(-1, "num_species out of range or inconsistent with thermal");

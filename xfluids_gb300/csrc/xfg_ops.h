@@ -21,6 +21,7 @@ struct LaunchCtx {
     int bc[6];
     const double *glf;                 // GLF maxima per direction (9 doubles) or nullptr
     int precision;                     // xfg_precision
+    double cfl;                        // CFLnumber (positivity limiter)
 };
 
 struct Ops {
@@ -33,6 +34,7 @@ struct Ops {
     void (*glf)(const LaunchCtx &, unsigned long long *out, int guard);
     void (*rk)(const LaunchCtx &, int flag, double dt);
     void (*estimate_nan)(const LaunchCtx &, const double *UI, int *pos);
+    void (*pp)(const LaunchCtx &, int d, const double *UI, const double *lam0, int guard);
 };
 
 // Message returned by xfg_last_error() on this host thread.

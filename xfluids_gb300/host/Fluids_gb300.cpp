@@ -60,6 +60,7 @@ xfg_scheme to_scheme() {
     s.ncop_gamma = 1.4;
 #endif
     s.precision = XFG_FP64;
+    s.positivity = PositivityPreserving ? 1 : 0;  // read_json.cpp:68
     return s;
 }
 

@@ -31,7 +31,7 @@ def make_block(resolution, domain_size, boundarys, cfl=0.5, bwidth=4, domain_min
 
 
 def make_scheme(cop=False, num_species=1, scheme_order=5, artificial_type=LLF, thermo=1,
-                ghost_species=False, ncop_gamma=1.4, precision=0) -> Scheme:
+                ghost_species=False, ncop_gamma=1.4, precision=0, positivity=False) -> Scheme:
     s = Scheme()
     s.cop = int(bool(cop))
     s.num_species = int(num_species) if cop else 1
@@ -41,6 +41,7 @@ def make_scheme(cop=False, num_species=1, scheme_order=5, artificial_type=LLF, t
     s.ghost_species = int(bool(ghost_species))
     s.ncop_gamma = float(ncop_gamma)
     s.precision = int(precision)
+    s.positivity = int(bool(positivity))
     return s
 
 
