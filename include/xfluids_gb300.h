@@ -197,6 +197,14 @@ int xfg_device_array(xfg_handle *h, int which, double **ptr, size_t *pitch);
  * out[1] = FP32, out[2] = SM clock (MHz) reported by the driver during the run (0 if unknown). */
 int xfg_measure_pipe_peaks(int device, double *out);
 
+/* Checkpoint files in the reference's format (XFLUIDS::Output_Ubak / Read_Ubak,
+ * src/XFLUIDS.cpp:658-724): int Step, double Time, float duration, then U in the reference layout
+ * (Emax doubles per cell, ghosts included), packed. Read loads U (and U1 = U) and sets the
+ * handle's time; like Read_Ubak it restores no temperature (mixtures warm-start the Newton
+ * iteration from the T already in the handle). Follow with xfg_boundary + xfg_update_states. */
+int xfg_checkpoint_write(xfg_handle *h, const char *path, int step, double time, float duration);
+int xfg_checkpoint_read(xfg_handle *h, const char *path, int *step, double *time, float *duration);
+
 /* ------------------------------------------------------------------------------------------
  * Ensemble of independent single-gas grids (batched ensemble, request serving).
  * No single counterpart in the reference, which advances one block per process: the members are
@@ -237,6 +245,17 @@ int xfg_ensemble_status(xfg_ensemble *e, int slot, double *t, int *steps, int *d
 
 /* Copy a member's state U out (AoS, host or device pointer). */
 int xfg_ensemble_get_state(xfg_ensemble *e, int slot, double *U_aos);
+
+/* A member as a checkpoint file of the reference's format (see xfg_checkpoint_write), with its
+ * step count and time; and a member admitted from such a file (U, time and step count restored,
+ * then BoundaryCondition + UpdateStates as xfg_ensemble_add; returns 1 / 2 like it). The file
+ * holds no dt: lam_out (3 doubles, may be NULL) receives the GetDt maxima the member's next step
+ * would use, and lam_in (may be NULL) restores them, so that a resumed member takes the steps the
+ * saved one would have taken; without it the next dt comes from the restored U, as after the
+ * reference's Read_Ubak. */
+int xfg_ensemble_checkpoint_write(xfg_ensemble *e, int slot, const char *path, float duration, double *lam_out);
+int xfg_ensemble_add_checkpoint(xfg_ensemble *e, const xfg_block *block, const char *path, double target_t,
+                                const double *lam_in, int *slot);
 
 /* Launch schedule of the batched step (the autotuner's knobs). None changes the operations of a
  * step: FP64 results are bit-identical under every schedule, mixed-precision results agree to FP32

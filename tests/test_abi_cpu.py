@@ -86,3 +86,20 @@ def test_ensemble_rejects_unsupported_schemes_before_touching_a_device(cuda_lib)
         sc = make_scheme(**{"scheme_order": 5, "artificial_type": abi.LLF, **kw})
         with pytest.raises(abi.XfgError):
             Ensemble(sc, capacity=2, pool_bytes=1 << 20)
+
+
+def test_checkpoint_format_is_the_references(tmp_path):
+    """int32 Step, float64 Time, float32 duration, then U, packed (XFLUIDS.cpp:658-724)."""
+    import numpy as np
+    from xfluids_gb300 import checkpoint
+    U = np.arange(40, dtype=np.float64) * 0.5
+    p = tmp_path / "ck"
+    checkpoint.write(p, 17, 0.125, 3.5, U)
+    raw = p.read_bytes()
+    assert len(raw) == 4 + 8 + 4 + 8 * 40
+    assert raw[:4] == (17).to_bytes(4, "little")
+    assert np.frombuffer(raw[4:12], "<f8")[0] == 0.125 and np.frombuffer(raw[12:16], "<f4")[0] == 3.5
+    step, t, dur, V = checkpoint.read(p, 40)
+    assert (step, t, dur) == (17, 0.125, 3.5) and np.array_equal(U, V)
+    with pytest.raises(ValueError):
+        checkpoint.read(p, 41)

@@ -144,6 +144,10 @@ def lib():
         "xfg_ensemble_status": [P, I, pd, pi, pi],
         "xfg_ensemble_get_state": [P, I, P],
         "xfg_ensemble_set_option": [P, I, I],
+        "xfg_ensemble_checkpoint_write": [P, I, C.c_char_p, C.c_float, P],
+        "xfg_ensemble_add_checkpoint": [P, C.POINTER(Block), C.c_char_p, D, P, pi],
+        "xfg_checkpoint_write": [P, C.c_char_p, I, D, C.c_float],
+        "xfg_checkpoint_read": [P, C.c_char_p, pi, pd, C.POINTER(C.c_float)],
         "xfg_ensemble_get_option": [P, I, pi],
         "xfg_ensemble_active": [P],
     })

@@ -295,6 +295,46 @@ int xfg_set_state(xfg_handle *h, const double *U_aos, const double *T) {
     return 0;
 }
 
+// Checkpoint file of XFLUIDS::Output_Ubak / Read_Ubak (src/XFLUIDS.cpp:658-724): int Step,
+// double Time, float duration, then U in the reference layout (Emax doubles per cell, all cells
+// with ghosts), packed, host byte order.
+int xfg_checkpoint_write(xfg_handle *h, const char *path, int step, double time, float duration) {
+    if (!h || !path) return fail(-1, "null argument");
+    std::vector<double> U((size_t)h->N * h->E);
+    int rc = xfg_get_array(h, XFG_U, U.data());
+    if (rc) return rc;
+    std::FILE *fp = std::fopen(path, "wb");
+    if (!fp) return fail(-1, "cannot open %s for writing", path);
+    bool ok = std::fwrite(&step, sizeof step, 1, fp) == 1 && std::fwrite(&time, sizeof time, 1, fp) == 1 &&
+              std::fwrite(&duration, sizeof duration, 1, fp) == 1 &&
+              std::fwrite(U.data(), sizeof(double), U.size(), fp) == U.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? 0 : fail(-1, "write of %s failed", path);
+}
+
+int xfg_checkpoint_read(xfg_handle *h, const char *path, int *step, double *time, float *duration) {
+    if (!h || !path) return fail(-1, "null argument");
+    std::FILE *fp = std::fopen(path, "rb");
+    if (!fp) return fail(-1, "cannot open %s", path);
+    int st = 0;
+    double t = 0.0;
+    float dur = 0.f;
+    std::vector<double> U((size_t)h->N * h->E);
+    bool ok = std::fread(&st, sizeof st, 1, fp) == 1 && std::fread(&t, sizeof t, 1, fp) == 1 &&
+              std::fread(&dur, sizeof dur, 1, fp) == 1 && std::fread(U.data(), sizeof(double), U.size(), fp) == U.size();
+    const bool extra = ok && std::fgetc(fp) != EOF;
+    std::fclose(fp);
+    if (!ok || extra)
+        return fail(-1, "%s is not a checkpoint of this block (expected 16 + %zu bytes)", path, U.size() * sizeof(double));
+    int rc = xfg_set_state(h, U.data(), nullptr);
+    if (rc) return rc;
+    h->t = t;
+    if (step) *step = st;
+    if (time) *time = t;
+    if (duration) *duration = dur;
+    return 0;
+}
+
 int xfg_get_array(xfg_handle *h, int which, double *out) {
     if (!h || !out) return fail(-1, "null argument");
     CK(cudaSetDevice(h->device));

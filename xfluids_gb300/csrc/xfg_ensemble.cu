@@ -164,7 +164,7 @@ __global__ void kb_soa_to_aos(const double *__restrict__ soa, double *__restrict
 size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 thread_local std::string g_eerr;
-int efail(int code, const char *fmt, const char *detail = "") {
+int efail(int code, const char *fmt, const char *detail = "") {  // fmt takes one %s
     char buf[512];
     snprintf(buf, sizeof buf, fmt, detail);
     set_last_error(buf);
@@ -592,6 +592,63 @@ int xfg_ensemble_get_option(xfg_ensemble *e, int option, int *value) {
     else if (option == XFG_ENS_GRAPH_STEPS) *value = e->graph_steps;
     else if (option >= XFG_ENS_TILE_1D && option <= XFG_ENS_TILE_3D) *value = e->ltx[option - XFG_ENS_TILE_1D];
     else return efail(-1, "unknown option%s");
+    return 0;
+}
+
+// A member as a checkpoint file of the reference's format (XFLUIDS::Output_Ubak,
+// src/XFLUIDS.cpp:658-687): its step count, time and U.
+int xfg_ensemble_checkpoint_write(xfg_ensemble *e, int slot, const char *path, float duration, double *lam_out) {
+    if (!e || !path || slot < 0 || slot >= e->capacity || e->m_len[slot] == 0) return efail(-1, "bad slot%s");
+    const Member &m = e->hm[slot];
+    std::vector<double> U((size_t)m.g.ncell() * 5);
+    int rc = xfg_ensemble_get_state(e, slot, U.data());
+    if (rc) return rc;
+    double b[8];
+    ECK(cudaMemcpy(b, m.f.dtbuf, sizeof b, cudaMemcpyDeviceToHost));
+    if (lam_out) {  // the GetDt maxima the member's next step will use
+        unsigned long long lam[3];
+        ECK(cudaMemcpy(lam, m.f.lam, sizeof lam, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < 3; q++) std::memcpy(&lam_out[q], &lam[q], 8);
+    }
+    const int step = (int)b[3];
+    const double time = b[1];
+    std::FILE *fp = std::fopen(path, "wb");
+    if (!fp) return efail(-1, "cannot open %s for writing", path);
+    bool ok = std::fwrite(&step, sizeof step, 1, fp) == 1 && std::fwrite(&time, sizeof time, 1, fp) == 1 &&
+              std::fwrite(&duration, sizeof duration, 1, fp) == 1 &&
+              std::fwrite(U.data(), sizeof(double), U.size(), fp) == U.size();
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? 0 : efail(-1, "write of %s failed", path);
+}
+
+// Admit a member from a checkpoint file (XFLUIDS::Read_Ubak, src/XFLUIDS.cpp:689-724): U, time and
+// step count as saved, then the member's BoundaryCondition + UpdateStates as xfg_ensemble_add.
+int xfg_ensemble_add_checkpoint(xfg_ensemble *e, const xfg_block *block, const char *path, double target_t,
+                                const double *lam_in, int *slot) {
+    if (!e || !block || !path || !slot) return efail(-1, "null argument%s");
+    *slot = -1;
+    const size_t n = (size_t)block->Xmax * block->Ymax * block->Zmax * 5;
+    std::FILE *fp = std::fopen(path, "rb");
+    if (!fp) return efail(-1, "cannot open %s", path);
+    int step = 0;
+    double time = 0.0;
+    float dur = 0.f;
+    std::vector<double> U(n);
+    bool ok = std::fread(&step, sizeof step, 1, fp) == 1 && std::fread(&time, sizeof time, 1, fp) == 1 &&
+              std::fread(&dur, sizeof dur, 1, fp) == 1 && std::fread(U.data(), sizeof(double), n, fp) == n;
+    const bool extra = ok && std::fgetc(fp) != EOF;
+    std::fclose(fp);
+    if (!ok || extra) return efail(-1, "%s is not a checkpoint of this block", path);
+    int rc = xfg_ensemble_add(e, block, U.data(), target_t, slot);
+    if (rc) return rc;  // 1 / 2: no slot or no memory, nothing admitted
+    const Member &m = e->hm[*slot];
+    const double tb[4] = {0.0, time, target_t, (double)step};
+    ECK(cudaMemcpy(m.f.dtbuf, tb, sizeof tb, cudaMemcpyHostToDevice));
+    if (lam_in) {  // continue with the dt the saved run would have taken next
+        unsigned long long lam[3];
+        for (int q = 0; q < 3; q++) std::memcpy(&lam[q], &lam_in[q], 8);
+        ECK(cudaMemcpy(m.f.lam, lam, sizeof lam, cudaMemcpyHostToDevice));
+    }
     return 0;
 }
 

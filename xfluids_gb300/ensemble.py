@@ -77,6 +77,29 @@ class Ensemble:
         check(lib().xfg_ensemble_get_state(self._e, slot, out.ctypes.data_as(C.c_void_p)))
         return out
 
+    def write_checkpoint(self, slot: int, path: str, duration: float = 0.0):
+        """The member as a checkpoint file of the reference's format (step count, time, U).
+        Returns the GetDt maxima its next step would use (for add_checkpoint's lam)."""
+        lam = np.zeros(3)
+        check(lib().xfg_ensemble_checkpoint_write(self._e, slot, str(path).encode(), float(duration),
+                                                  lam.ctypes.data_as(C.c_void_p)))
+        return [float(x) for x in lam]
+
+    def add_checkpoint(self, block: Block, path: str, target_t: float, lam=None):
+        """Admit a member from a checkpoint file (time and step count restored; with lam, also the
+        dt of its next step); slot or None."""
+        slot = C.c_int(-1)
+        lam_p = None
+        if lam is not None:
+            lam_a = np.ascontiguousarray(lam, dtype=np.float64)
+            lam_p = lam_a.ctypes.data_as(C.c_void_p)
+        rc = check(lib().xfg_ensemble_add_checkpoint(self._e, C.byref(block), str(path).encode(), float(target_t),
+                                                     lam_p, C.byref(slot)))
+        if rc in (NO_SLOT, NO_MEMORY):
+            return None
+        self.blocks[slot.value] = block
+        return slot.value
+
     def set_option(self, option, value: int):
         option = OPTIONS.get(option, option)
         check(lib().xfg_ensemble_set_option(self._e, int(option), int(value)))

@@ -55,6 +55,16 @@ class Fluid:
 
     set_state = InitialU
 
+    # -- checkpoints (XFLUIDS::Output_Ubak / Read_Ubak, src/XFLUIDS.cpp:658-724) -------------------
+    def write_checkpoint(self, path: str, step: int, time: float, duration: float = 0.0):
+        check(lib().xfg_checkpoint_write(self._h, str(path).encode(), int(step), float(time), float(duration)))
+
+    def read_checkpoint(self, path: str):
+        """Load U from a checkpoint file; returns (step, time, duration). Run initialize() next."""
+        st, t, dur = C.c_int(), C.c_double(), C.c_float()
+        check(lib().xfg_checkpoint_read(self._h, str(path).encode(), C.byref(st), C.byref(t), C.byref(dur)))
+        return st.value, t.value, dur.value
+
     def get(self, name: str) -> np.ndarray:
         n = self.block.ncell
         size = n * self.E if name in AOS_E else (n * self.NS if name == "y" else n)

@@ -22,13 +22,14 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import time
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import cases
-from .abi import LLF
+from . import cases, checkpoint
+from .abi import LLF, Block
 from .ensemble import Ensemble
 from .mesh import make_scheme
 
@@ -95,24 +96,34 @@ def serving_scheme(precision=0):
 
 class Server:
     def __init__(self, precision=0, hbm_budget=32 << 30, capacity=64, chunk=16, device=0, keep_results=True):
+        self.precision, self.hbm_budget, self.capacity, self.chunk, self.device = precision, int(hbm_budget), capacity, \
+            chunk, device
         self.scheme = serving_scheme(precision)
         self.ens = Ensemble(self.scheme, capacity=capacity, pool_bytes=int(hbm_budget), device=device)
-        self.capacity, self.chunk, self.keep = capacity, chunk, keep_results
+        self.keep = keep_results
         self.device_ms = 0.0
         self.chunks = 0
         self.max_running = 0
+        self.pending, self.waiting, self.running = [], [], {}
+        self.elapsed0 = 0.0   # server clock at the start of this process (non-zero after a resume)
 
     def close(self):
         self.ens.close()
 
-    def run(self, trace, realtime=True):
-        """Serve `trace` (Requests sorted by arrival) to completion. realtime=False replays the
-        arrivals in order without waiting for the wall clock (tests)."""
-        pending = list(trace)
-        waiting, running = [], {}
-        t0 = time.perf_counter()
+    def run(self, trace=None, realtime=True, max_chunks=None):
+        """Serve the submitted requests (and `trace`, Requests sorted by arrival) until all are
+        done, or for at most `max_chunks` chunks. realtime=False replays the arrivals in order
+        without waiting for the wall clock (tests)."""
+        if trace is not None:
+            self.pending.extend(trace)
+        pending, waiting, running = self.pending, self.waiting, self.running
+        t0 = time.perf_counter() - self.elapsed0
         now = lambda: time.perf_counter() - t0
+        self._now = now
+        done_chunks = 0
         while pending or waiting or running:
+            if max_chunks is not None and done_chunks >= max_chunks:
+                break
             clock = now()
             while pending and (pending[0].arrival <= clock or not realtime):
                 r = pending.pop(0)
@@ -138,6 +149,7 @@ class Server:
             _, ms = self.ens.advance(self.chunk)
             self.device_ms += ms
             self.chunks += 1
+            done_chunks += 1
             clock = now()
             for slot in list(running):
                 st = self.ens.status(slot)
@@ -147,7 +159,65 @@ class Server:
                     if self.keep:
                         r.result = self.ens.get_state(slot)
                     self.ens.remove(slot)
+        self.elapsed0 = now()
         return trace
+
+    # -- save / resume the server's resident state ---------------------------------------------
+    def save(self, directory):
+        """Write every unfinished request to `directory`: the running ones as checkpoint files of
+        the reference's format taken from the device (step count, time, state) with the dt maxima
+        of their next step, the queued ones as their initial state; plus manifest.json."""
+        os.makedirs(directory, exist_ok=True)
+        reqs = []
+        for slot, r in self.running.items():
+            path = os.path.join(directory, f"req{r.rid}.ckpt")
+            lam = self.ens.write_checkpoint(slot, path)
+            reqs.append(_req_record(r, "running", path, lam))
+        for state, queue in (("waiting", self.waiting), ("pending", self.pending)):
+            for r in queue:
+                path = os.path.join(directory, f"req{r.rid}.ckpt")
+                checkpoint.write(path, 0, 0.0, 0.0, r.U)
+                reqs.append(_req_record(r, state, path, None))
+        manifest = {"precision": self.precision, "hbm_budget": self.hbm_budget, "capacity": self.capacity,
+                    "chunk": self.chunk, "elapsed": self.elapsed0, "requests": reqs}
+        with open(os.path.join(directory, "manifest.json"), "w") as f:
+            json.dump(manifest, f, indent=1)
+
+    @classmethod
+    def resume(cls, directory, device=0, keep_results=True):
+        """A server holding the saved requests: running ones re-admitted from their checkpoints
+        (the steps they take next are the ones the saved server would have taken), queued ones
+        queued again. Continue with run()."""
+        with open(os.path.join(directory, "manifest.json")) as f:
+            m = json.load(f)
+        srv = cls(m["precision"], m["hbm_budget"], m["capacity"], m["chunk"], device, keep_results)
+        srv.elapsed0 = m["elapsed"]
+        for rec in m["requests"]:
+            b = Block()
+            for k, v in rec["block"].items():
+                if k == "Boundarys":
+                    for q in range(6):
+                        b.Boundarys[q] = v[q]
+                else:
+                    setattr(b, k, v)
+            r = Request(rec["rid"], rec["kind"], rec["n"], rec["t_end"], rec["arrival"], b, None)
+            r.start, r.admitted = rec["start"], rec["admitted"]
+            if rec["state"] == "running":
+                slot = srv.ens.add_checkpoint(b, rec["path"], r.t_end, rec["lam"])
+                if slot is None:
+                    raise RuntimeError("a saved running request does not fit the restored server")
+                srv.running[slot] = r
+            else:
+                r.U = checkpoint.read(rec["path"], b.ncell * 5)[3]
+                (srv.waiting if rec["state"] == "waiting" else srv.pending).append(r)
+        return srv
+
+
+def _req_record(r, state, path, lam):
+    b = r.block
+    block = {k: getattr(b, k) for k, _ in b._fields_ if k != "Boundarys"} | {"Boundarys": list(b.Boundarys)}
+    return {"rid": r.rid, "kind": r.kind, "n": r.n, "t_end": r.t_end, "arrival": r.arrival, "start": r.start,
+            "admitted": r.admitted, "state": state, "path": path, "lam": lam, "block": block}
 
 
 def summary(trace, wall_s=None, device_ms=None):
