@@ -23,6 +23,7 @@ PRIMS = ["rho", "p", "u", "v", "w", "c", "H", "T"]
 FLAVOURS = {
     "ncop_w5_llf": (5, 1), "ncop_w7_llf": (5, 1), "ncop_w5_roe": (5, 1), "ncop_w5_glf": (5, 1),
     "cop4g_w5_llf_nasa": (8, 4), "cop5_w7_llf_janaf": (9, 5),
+    "ncop_w6_llf": (5, 1), "cop5_w6_roe_janaf": (9, 5),
     # built with PositivityPreserving on (-DPOSP=1, and the JSON key below)
     "ncop_w5_llf_pp": (5, 1), "cop5_w5_llf_janaf_pp": (9, 5),
 }

@@ -683,6 +683,58 @@ R weno7(const R *f, const R *m) {
     return tp + tm;
 }
 
+// WENOCU6_BODYGPU, WENO6s_schemes.hpp:5-55: the three WENO5 indicators, a sixth-order global
+// indicator s6 from the tau_6k differences, the CU6 weights 20 + |s6 - s55| / (s_k + eps) with
+// linear weights (0.05, 0.45, 0.45, 0.05) and the four candidates; v1..v6 in upwind order.
+template <class R>
+R wenocu6_body(R v1, R v2, R v3, R v4, R v5, R v6, R eps) {
+    using std::fabs;
+    R s11 = v1 - R(2.0) * v2 + v3;
+    R s12 = v1 - R(4.0) * v2 + R(3.0) * v3;
+    R s1 = R(13.0) * s11 * s11 + R(3.0) * s12 * s12;
+    R s21 = v2 - R(2.0) * v3 + v4;
+    R s22 = v2 - v4;
+    R s2 = R(13.0) * s21 * s21 + R(3.0) * s22 * s22;
+    R s31 = v3 - R(2.0) * v4 + v5;
+    R s32 = R(3.0) * v3 - R(4.0) * v4 + v5;
+    R s3 = R(13.0) * s31 * s31 + R(3.0) * s32 * s32;
+    R tau61 = (R(259.0) * v6 - R(1895.0) * v5 + R(6670.0) * v4 - R(2590.0) * v3 - R(2785.0) * v2 + R(341.0) * v1) *
+              R(1.0 / 5760.0);
+    R tau62 = -(v5 - R(12.0) * v4 + R(22.0) * v3 - R(12.0) * v2 + v1) * R(1.0 / 16.0);
+    R tau63 = -(R(7.0) * v6 - R(47.0) * v5 + R(94.0) * v4 - R(70.0) * v3 + R(11.0) * v2 + R(5.0) * v1) * R(1.0 / 144.0);
+    R tau64 = (v5 - R(4.0) * v4 + R(6.0) * v3 - R(4.0) * v2 + v1) * R(1.0 / 24.0);
+    R tau65 = -(-v6 + R(5.0) * v5 - R(10.0) * v4 + R(10.0) * v3 - R(5.0) * v2 + v1) * R(1.0 / 120.0);
+    const R a1a1 = R(1.0), a2a2 = R(13.0 / 3.0), a1a3 = R(0.5), a3a3 = R(3129.0 / 80.0), a2a4 = R(4.2);
+    const R a1a5 = R(0.125), a4a4 = R(87617.0 / 140.0), a3a5 = R(14127.0 / 224.0), a5a5 = R(252337135.0 / 16128.0);
+    R s6 = (tau61 * tau61 * a1a1 + tau62 * tau62 * a2a2 + tau61 * tau63 * a1a3 + tau63 * tau63 * a3a3 +
+            tau62 * tau64 * a2a4 + tau61 * tau65 * a1a5 + tau64 * tau64 * a4a4 + tau63 * tau65 * a3a5 +
+            tau65 * tau65 * a5a5) * R(12.0);
+    R s55 = (s1 + s3 + R(4.0) * s2) * R(kSix);
+    R s5 = fabs(s6 - s55);
+    R r0 = R(20.0);
+    R r1 = r0 + s5 / (s1 + eps);
+    R r2 = r0 + s5 / (s2 + eps);
+    R r3 = r0 + s5 / (s3 + eps);
+    R r4 = r0 + s5 / (s6 + eps);
+    R a1 = R(0.05) * r1, a2 = R(0.45) * r2, a3 = R(0.45) * r3, a4 = R(0.05) * r4;
+    R tw1 = R(1.0) / (a1 + a2 + a3 + a4);
+    R w1 = a1 * tw1, w2 = a2 * tw1, w3 = a3 * tw1, w4 = a4 * tw1;
+    R temp = R(0.0);
+    temp += w1 * (R(2.0) * v1 - R(7.0) * v2 + R(11.0) * v3);
+    temp += w2 * (-v2 + R(5.0) * v3 + R(2.0) * v4);
+    temp += w3 * (R(2.0) * v3 + R(5.0) * v4 - v5);
+    temp += w4 * (R(11.0) * v4 - R(7.0) * v5 + R(2.0) * v6);
+    return temp;
+}
+// WENOCU6_GPU, WENO6s_schemes.hpp:58-84: epsilon = 1e-8 dl^2 with dl the cell size along the sweep
+template <class R>
+R wenocu6(const R *f, const R *m, R dl) {
+    const R eps = R(1.e-8) * dl * dl;
+    R temf = wenocu6_body(f[-2], f[-1], f[0], f[1], f[2], f[3], eps);
+    R temm = wenocu6_body(m[3], m[2], m[1], m[0], m[-1], m[-2], eps);
+    return (temf + temm) * R(kSix);
+}
+
 // ---------------------------------------------------------------------------------------------
 // Convective flux at face (i+1/2) in direction d:
 // ReconstructFlux{X,Y,Z}, Reconstruction_kernels.hpp:8-199 with MARCO_FLUXWALL_WENO5 / _WENO7
@@ -726,7 +778,7 @@ void face_flux(const Config &cf, const ThermoTable &tt, const Fields<R> &f, cons
             for (int m = -2; m < 4; m++) elm = fmax(elm, fabs(eig[E * (id_l + (long)m * (long)stride) + n]));
             av = at == XFG_ROE ? ev : (at == XFG_LLF ? elm : f.eigen_block[d][n]);
         }
-        // project U and F at points m = -3..4 (index m+3); WENO5 reads m = -2..3 only
+        // project U and F at points m = -3..4 (index m+3); WENO5 and WENO-CU6 read m = -2..3 only
         R pp[8], mm[8];
         const int m0 = order == 7 ? -3 : -2, m1 = order == 7 ? 4 : 3;
         for (int m = m0; m <= m1; m++) {
@@ -736,7 +788,8 @@ void face_flux(const Config &cf, const ThermoTable &tt, const Fields<R> &f, cons
             pp[m + 3] = R(0.5) * (ff + av * uf);
             mm[m + 3] = R(0.5) * (ff - av * uf);
         }
-        R f_flux = order == 7 ? weno7(&pp[3], &mm[3]) : weno5(&pp[3], &mm[3]);
+        const R dl = R(d == 0 ? b.dx : (d == 1 ? b.dy : b.dz));
+        R f_flux = order == 7 ? weno7(&pp[3], &mm[3]) : (order == 6 ? wenocu6(&pp[3], &mm[3], dl) : weno5(&pp[3], &mm[3]));
         Vec<R> r;
         right_col(cf, d, n, F, r);
         // _p[n][n1] = f_flux * r[n1]; Fwall[n1] = sum_n _p[n][n1]

@@ -35,6 +35,11 @@ CASES = {
     "insert64_cop4_ghost_nasa_w5": ("cop4g_w5_llf_nasa", lambda: H.insert_st(64), (0.1, 1.0, 1.0)),
     "mixing5_12x8x6_janaf_w7": ("cop5_w7_llf_janaf", lambda: H.mixing_small((12, 8, 6)),
                                 (0.01, 0.01 * 8 / 12, 0.01 * 6 / 12)),
+    # WENO-CU6 (scheme order 6)
+    "riemann20_cu6_llf": ("ncop_w6_llf", H.with_order(lambda: H.riemann_small(20), 6), None),
+    "mixing5_12x8x6_janaf_cu6_roe": ("cop5_w6_roe_janaf",
+                                     H.with_order(lambda: H.mixing_small((12, 8, 6), order=5, artificial=ROE), 6),
+                                     (0.01, 0.01 * 8 / 12, 0.01 * 6 / 12)),
     # PositivityPreserving on: cases where the limiter acts (without it the first two go negative)
     "pp_riemann88_32_w5_llf": ("ncop_w5_llf_pp", H.with_positivity(lambda: H.riemann_member(88, 32)), None),
     "pp_riemann1d108_w5_llf": ("ncop_w5_llf_pp", H.with_positivity(H.riemann1d_strong), None),

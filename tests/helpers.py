@@ -137,3 +137,11 @@ def riemann1d_strong(n=108):
     positivity limiter (rho, u, p) = (1.84, -0.494, 0.0911) | (0.189, -0.503, 0.656)."""
     return cases.riemann1d(n, (1.8397073266913917, -0.4944626440950872, 0.09109694116558763),
                            (0.18863925211238564, -0.5028604535820342, 0.6556118842537302))
+
+
+def with_order(mk, order):
+    def build():
+        b, s, th, U, T = mk()
+        s.scheme_order = order
+        return b, s, th, U, T
+    return build

@@ -66,7 +66,7 @@ def test_struct_layouts_match_header():
 def test_create_rejects_bad_arguments(cuda_lib):
     from xfluids_gb300 import cases
     b, s, th, U, T = cases.sod(32)
-    s.scheme_order = 6
+    s.scheme_order = 8
     h = C.c_void_p()
     rc = cuda_lib.xfg_create(C.byref(b), C.byref(s), C.byref(th), 0, C.byref(h))
     assert rc == -1 and not h.value
@@ -82,7 +82,7 @@ def test_ensemble_rejects_unsupported_schemes_before_touching_a_device(cuda_lib)
     from xfluids_gb300.ensemble import Ensemble
     from xfluids_gb300.mesh import make_scheme
     for kw in (dict(cop=True, num_species=2), dict(artificial_type=abi.GLF), dict(precision=2),
-               dict(scheme_order=6)):
+               dict(scheme_order=6), dict(positivity=True)):
         sc = make_scheme(**{"scheme_order": 5, "artificial_type": abi.LLF, **kw})
         with pytest.raises(abi.XfgError):
             Ensemble(sc, capacity=2, pool_bytes=1 << 20)

@@ -72,6 +72,10 @@ CASES = {
     "insert_st_janaf_weno7": lambda: H.insert_st(100, order=7, ghost=False, thermo_kind=0),
     "mixing5_weno7_janaf": lambda: H.mixing_small(),
     "mixing5_weno5_nasa_roe": lambda: H.mixing_small((16, 12, 8), order=5, thermo_kind=1, artificial=ROE),
+    # WENO-CU6
+    "riemann2d_cu6_llf": H.with_order(lambda: H.riemann_small(40), 6),
+    "blast3d_cu6_glf": H.with_order(lambda: H.blast3d(artificial=GLF), 6),
+    "mixing5_cu6_janaf_roe": H.with_order(lambda: H.mixing_small((16, 12, 8), order=5, artificial=ROE), 6),
     # positivity limiter on (cases where it acts: without it the first two turn negative)
     "pp_riemann88": H.with_positivity(lambda: H.riemann_member(88, 32)),
     "pp_riemann1d": H.with_positivity(H.riemann1d_strong),
@@ -89,7 +93,7 @@ def test_stagewise_parity(name, precision, cuda_lib):
 
 
 @pytest.mark.parametrize("name", ["vortex64", "blast3d_weno7_glf", "riemann2d_weno7_sym", "mixing5_weno7_janaf",
-                                  "pp_riemann88", "pp_mixing5_weno5_janaf"])
+                                  "pp_riemann88", "pp_mixing5_weno5_janaf", "riemann2d_cu6_llf", "mixing5_cu6_janaf_roe"])
 def test_strict_is_bitwise(name, cuda_lib):
     """Without contraction the CUDA path performs the reference's operation sequence: every array
     of every stage is bit-identical to the oracle (no log/exp on these cases)."""
@@ -206,3 +210,21 @@ def test_positivity_limiter_acts_and_keeps_density_positive(cuda_lib):
         assert st == 0 and n == 20
         assert H.inner_aos(b, f.get("U"), 5)[:, 0].min() > 0.0
         f.close()
+
+
+def test_mixed_cu6_close_to_fp64(cuda_lib):
+    """The mixed form with WENO-CU6 reconstruction stays close to the FP64 path."""
+    b, s, th, U, T = H.with_order(lambda: H.riemann_small(64), 6)()
+    f64 = _fluid(b, s, th, U, T)
+    b2, s2, _, _, _ = H.with_order(lambda: H.riemann_small(64), 6)()
+    s2.precision = MIXED
+    fmx = _fluid(b2, s2, th, U, T)
+    f64.initialize(), fmx.initialize()
+    st1, t1, n1 = f64.advance(10)
+    st2, t2, n2 = fmx.advance(40, t1)
+    assert st1 == 0 and st2 == 0
+    a, r = H.inner_aos(b, fmx.get("U"), 5), H.inner_aos(b, f64.get("U"), 5)
+    num, den = np.abs(a - r).mean(axis=0), np.abs(r).mean(axis=0)
+    rel = np.where(den > 0, num / np.where(den > 0, den, 1.0), num)   # rho w is zero in 2D
+    assert np.all(rel < 1e-4), rel
+    f64.close(), fmx.close()

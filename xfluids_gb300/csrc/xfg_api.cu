@@ -107,7 +107,8 @@ static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *t) {
     if (!b || !s || !t) return fail(-1, "null argument");
-    if (s->scheme_order != 5 && s->scheme_order != 7) return fail(-1, "scheme_order must be 5 or 7 (got %d)", s->scheme_order);
+    if (s->scheme_order < 5 || s->scheme_order > 7)
+        return fail(-1, "scheme_order must be 5 (WENO5), 6 (WENO-CU6) or 7 (WENO7) (got %d)", s->scheme_order);
     if (s->artificial_type < 1 || s->artificial_type > 3) return fail(-1, "artificial_type must be 1..3");
     if (s->precision < 0 || s->precision > 2) return fail(-1, "precision must be 0 (fp64), 1 (mixed) or 2 (fp64 strict)");
     if (s->positivity != 0 && s->positivity != 1) return fail(-1, "positivity must be 0 or 1");
@@ -236,6 +237,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     g.Bx = block->Bwidth_X, g.By = block->Bwidth_Y, g.Bz = block->Bwidth_Z;
     g.dimx = block->DimX, g.dimy = block->DimY, g.dimz = block->DimZ;
     g._dx = block->_dx, g._dy = block->_dy, g._dz = block->_dz;
+    g.dx = block->dx, g.dy = block->dy, g.dz = block->dz;
     g.pitch = h->P;
     DevThermo &th = h->ctx.th;
     std::memset(&th, 0, sizeof th);

@@ -56,6 +56,7 @@ struct Geo {
     int dimx, dimy, dimz;
     double _dx, _dy, _dz;
     long long pitch;  // elements between components of a SoA array
+    double dx, dy, dz;  // cell sizes (the WENO-CU6 epsilon)
     __host__ __device__ long long ncell() const { return (long long)Xmax * Ymax * Zmax; }
 };
 
@@ -401,6 +402,57 @@ __device__ __forceinline__ double weno5_fast2(const double *pp2, const double *m
     weno5_body_r(pp2[1], pp2[2], pp2[3], pp2[4], pp2[5], nf, df);
     weno5_body_r(mm2[6], mm2[5], mm2[4], mm2[3], mm2[2], nm, dm);
     return fma(0.5, pp2[3] + mm2[4], fma(nf, dm, nm * df) * rcp_nr(df * dm));
+}
+
+// WENOCU6_BODYGPU / WENOCU6_GPU (WENO6s_schemes.hpp:5-84): the WENO5 indicators, the sixth-order
+// indicator s6 of the tau_6k differences, the CU6 weights 20 + |s6 - s55| / (s_k + eps) with linear
+// weights (0.05, 0.45, 0.45, 0.05), eps = 1e-8 dl^2; the reference's operation order.
+template <class T>
+__device__ __forceinline__ T wenocu6_body(T v1, T v2, T v3, T v4, T v5, T v6, T eps) {
+    T s11 = v1 - T(2.0) * v2 + v3;
+    T s12 = v1 - T(4.0) * v2 + T(3.0) * v3;
+    T s1 = T(13.0) * s11 * s11 + T(3.0) * s12 * s12;
+    T s21 = v2 - T(2.0) * v3 + v4;
+    T s22 = v2 - v4;
+    T s2 = T(13.0) * s21 * s21 + T(3.0) * s22 * s22;
+    T s31 = v3 - T(2.0) * v4 + v5;
+    T s32 = T(3.0) * v3 - T(4.0) * v4 + v5;
+    T s3 = T(13.0) * s31 * s31 + T(3.0) * s32 * s32;
+    T tau61 = (T(259.0) * v6 - T(1895.0) * v5 + T(6670.0) * v4 - T(2590.0) * v3 - T(2785.0) * v2 + T(341.0) * v1) *
+              T(1.0 / 5760.0);
+    T tau62 = -(v5 - T(12.0) * v4 + T(22.0) * v3 - T(12.0) * v2 + v1) * T(1.0 / 16.0);
+    T tau63 = -(T(7.0) * v6 - T(47.0) * v5 + T(94.0) * v4 - T(70.0) * v3 + T(11.0) * v2 + T(5.0) * v1) * T(1.0 / 144.0);
+    T tau64 = (v5 - T(4.0) * v4 + T(6.0) * v3 - T(4.0) * v2 + v1) * T(1.0 / 24.0);
+    T tau65 = -(-v6 + T(5.0) * v5 - T(10.0) * v4 + T(10.0) * v3 - T(5.0) * v2 + v1) * T(1.0 / 120.0);
+    const T a1a1 = T(1.0), a2a2 = T(13.0 / 3.0), a1a3 = T(0.5), a3a3 = T(3129.0 / 80.0), a2a4 = T(4.2);
+    const T a1a5 = T(0.125), a4a4 = T(87617.0 / 140.0), a3a5 = T(14127.0 / 224.0), a5a5 = T(252337135.0 / 16128.0);
+    T s6 = (tau61 * tau61 * a1a1 + tau62 * tau62 * a2a2 + tau61 * tau63 * a1a3 + tau63 * tau63 * a3a3 +
+            tau62 * tau64 * a2a4 + tau61 * tau65 * a1a5 + tau64 * tau64 * a4a4 + tau63 * tau65 * a3a5 +
+            tau65 * tau65 * a5a5) * T(12.0);
+    T s55 = (s1 + s3 + T(4.0) * s2) * T(kSix);
+    T s5 = fabs(s6 - s55);
+    T r0 = T(20.0);
+    T r1 = r0 + s5 / (s1 + eps);
+    T r2 = r0 + s5 / (s2 + eps);
+    T r3 = r0 + s5 / (s3 + eps);
+    T r4 = r0 + s5 / (s6 + eps);
+    T a1 = T(0.05) * r1, a2 = T(0.45) * r2, a3 = T(0.45) * r3, a4 = T(0.05) * r4;
+    T tw1 = T(1.0) / (a1 + a2 + a3 + a4);
+    T w1 = a1 * tw1, w2 = a2 * tw1, w3 = a3 * tw1, w4 = a4 * tw1;
+    T temp = T(0.0);
+    temp += w1 * (T(2.0) * v1 - T(7.0) * v2 + T(11.0) * v3);
+    temp += w2 * (-v2 + T(5.0) * v3 + T(2.0) * v4);
+    temp += w3 * (T(2.0) * v3 + T(5.0) * v4 - v5);
+    temp += w4 * (T(11.0) * v4 - T(7.0) * v5 + T(2.0) * v6);
+    return temp;
+}
+// pp, mm indexed by stencil offset m + 3, m = -2..3 used
+template <class T>
+__device__ __forceinline__ T wenocu6(const T *pp, const T *mm, T dl) {
+    const T eps = T(1.e-8) * dl * dl;
+    T temf = wenocu6_body(pp[1], pp[2], pp[3], pp[4], pp[5], pp[6], eps);
+    T temm = wenocu6_body(mm[6], mm[5], mm[4], mm[3], mm[2], mm[1], eps);
+    return (temf + temm) * T(kSix);
 }
 
 // FP32 form: the same candidates and smoothness indicators; the weights use the division form

@@ -94,12 +94,13 @@ struct Inst {
         else pp_d<2>(c, UI, lam0, guard);
     }
 
-    // tables for scheme order 5 and 7, registered under precision id `prec`
+    // tables for scheme orders 5 (WENO5-JS), 6 (WENO-CU6) and 7 (WENO7), registered under
+    // precision id `prec`
     static const Ops *table(int order, int prec) {
-        static Ops t[2][3];
-        Ops &o = t[order == 7][prec];
-        o = Ops{COP ? 1 : 0, NS, order, prec, bc, states, order == 7 ? faces<7> : faces<5>, div_rk, glf, rk, estimate_nan,
-                pp};
+        static Ops t[3][3];
+        Ops &o = t[order - 5][prec];
+        o = Ops{COP ? 1 : 0, NS, order, prec, bc, states, order == 7 ? faces<7> : (order == 6 ? faces<6> : faces<5>),
+                div_rk, glf, rk, estimate_nan, pp};
         return &o;
     }
 };
@@ -109,8 +110,7 @@ template <bool COP, int NS, bool MIXED>
 struct Registrar {
     explicit Registrar(std::initializer_list<int> precisions) {
         for (int prec : precisions) {
-            register_ops(Inst<COP, NS, MIXED>::table(5, prec));
-            register_ops(Inst<COP, NS, MIXED>::table(7, prec));
+            for (int order = 5; order <= 7; order++) register_ops(Inst<COP, NS, MIXED>::table(order, prec));
         }
     }
 };

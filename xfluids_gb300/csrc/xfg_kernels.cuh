@@ -325,7 +325,8 @@ static __global__ void __launch_bounds__(kThreads) k_glf(Geo g, DevFields f, uns
 // Characteristic WENO flux at face (i+1/2) of direction D, one thread per face:
 // ReconstructFlux{X,Y,Z} (Reconstruction_kernels.hpp:8-199) with MARCO_ROE, MARCO_NOCOPC2 /
 // MARCO_COPC2 (ReconstructSoundSpeed, Utils_device.hpp:102-140), RoeAverageLeft/Right
-// (Eigen_matrix.hpp:7-455) and MARCO_FLUXWALL_WENO5 / _WENO7 (Eigen_callback.h:127-230).
+// (Eigen_matrix.hpp:7-455) and MARCO_FLUXWALL_WENO5 / _WENO7 (Eigen_callback.h:127-230), with
+// WENO5-JS, WENO-CU6 (scheme order 6) or WENO7.
 // Local eigenvalues (GetLocalEigen) are formed on the fly from u_d and c of the window cells.
 // ---------------------------------------------------------------------------------------------
 template <bool COP, int NS>
@@ -667,7 +668,7 @@ __device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, con
 
     // LLF window maxima of |u_d - c|, |u_d|, |u_d + c| over m = -2..3 (WENO5)
     double lm0 = 0.0, lm1 = 0.0, lm2 = 0.0;
-    if (ORDER == 5 && artificial == XFG_LLF) {
+    if (ORDER != 7 && artificial == XFG_LLF) {
         if (FAST_BUILD && FAST) {
             const double *__restrict__ ea = f.eab[D];
 #pragma unroll
@@ -721,7 +722,10 @@ __device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, con
                 mm[m + 3] = 0.5 * (ff - av * uf);
             }
         }
-        const double fl = ORDER == 7 ? weno7(pp, mm) : (FAST_BUILD ? weno5_fast(pp, mm) : weno5(pp, mm));
+        double fl;
+        if constexpr (ORDER == 7) fl = weno7(pp, mm);
+        else if constexpr (ORDER == 6) fl = wenocu6(pp, mm, D == 0 ? g.dx : (D == 1 ? g.dy : g.dz));
+        else fl = FAST_BUILD ? weno5_fast(pp, mm) : weno5(pp, mm);
 #pragma unroll
         for (int kk = 0; kk < E; kk++) {
             const int kind = right_kind(D, E, n, kk);

@@ -232,7 +232,7 @@ __device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &
     const float *__restrict__ vd = pf + (1 + D) * P;
     const float *__restrict__ cf = pf + 6 * P;
     float lm0 = 0.f, lm1 = 0.f, lm2 = 0.f;
-    if (ORDER == 5 && artificial == XFG_LLF) {
+    if (ORDER != 7 && artificial == XFG_LLF) {
 #pragma unroll
         for (int m = -2; m <= 3; m++) {
             const long long q = idl + m * stride;
@@ -287,7 +287,10 @@ __device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &
             pp[m + 3] = 0.5f * (ff + av * uf);
             mm[m + 3] = 0.5f * (ff - av * uf);
         }
-        const float fl = ORDER == 7 ? weno7(pp, mm) : weno5(pp, mm);
+        float fl;
+        if constexpr (ORDER == 7) fl = weno7(pp, mm);
+        else if constexpr (ORDER == 6) fl = wenocu6(pp, mm, (float)(D == 0 ? g.dx : (D == 1 ? g.dy : g.dz)));
+        else fl = weno5(pp, mm);
 #pragma unroll
         for (int kk = 0; kk < E; kk++) {
             const int kind = right_kind(D, E, n, kk);

@@ -73,7 +73,7 @@ size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *scheme, const xfg_thermal *thermal,
                                       const double *U_aos, const double *T, double *LU_aos, void *stream) {
     if (!block || !scheme || !thermal || !U_aos || !LU_aos) return fail(-1, "null argument");
-    if (scheme->scheme_order != 5 && scheme->scheme_order != 7) return fail(-1, "scheme_order must be 5 or 7");
+    if (scheme->scheme_order < 5 || scheme->scheme_order > 7) return fail(-1, "scheme_order must be 5, 6 or 7");
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_FP64_STRICT)
         return fail(-1, "xfg_compute_lu_noalloc serves the FP64 forms (precision 0 or 2)");
     if (scheme->positivity)
@@ -143,6 +143,7 @@ extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *
     c.g.Bx = block->Bwidth_X, c.g.By = block->Bwidth_Y, c.g.Bz = block->Bwidth_Z;
     c.g.dimx = block->DimX, c.g.dimy = block->DimY, c.g.dimz = block->DimZ;
     c.g._dx = block->_dx, c.g._dy = block->_dy, c.g._dz = block->_dz;
+    c.g.dx = block->dx, c.g.dy = block->dy, c.g.dz = block->dz;
     c.g.pitch = P;
     for (int n = 0; n < XFG_MAX_SPECIES; n++) c.th.Ri[n] = thermal->Ri[n], c.th._Wi[n] = thermal->_Wi[n];
     for (int q = 0; q < XFG_MAX_SPECIES * 21; q++) c.th.Hia[q] = thermal->Hia[q];
