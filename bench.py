@@ -303,6 +303,44 @@ def bench_mixing_layer(args, local, steps):
     return res
 
 
+def bench_accuracy(local, n=192, t_end=0.5):
+    """Free-running drift of the FP64 path against the oracle (same steps, no resynchronisation)
+    and the error of FP64 and mixed against the exact vortex, 2D vortex n^2 to t_end."""
+    from oracle import xfo
+    from xfluids_gb300.abi import MIXED
+    from xfluids_gb300.fluid import Fluid
+    cs = cases_mod()
+    xfo.set_threads(os.cpu_count() or 1)
+    b, s, th, U, T = cs.isentropic_vortex(n)
+    o = xfo.Oracle(b, s, th, U, T)
+    o.initialize()
+    t, n_o = 0.0, 0
+    while t < t_end:
+        t, _ = o.step(t_end)
+        n_o += 1
+    sl = b.inner_slices()
+    ref = o.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 5)[sl].reshape(-1, 5)
+    rho_ex = cs.isentropic_vortex_exact(b, t_end)[sl].reshape(-1)
+    out = {"workload": f"2D isentropic vortex {n}^2 to t = {t_end}", "steps": n_o}
+    for name, prec in (("fp64", 0), ("mixed", MIXED)):
+        s.precision = prec
+        f = Fluid(b, s, th, device=local)
+        f.InitialU(U, T)
+        f.initialize()
+        tg, k = 0.0, 0
+        while tg < t_end:
+            _, tg, k = f.advance(64, t_end)
+        g = f.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 5)[sl].reshape(-1, 5)
+        f.close()
+        d = np.abs(g - ref)
+        out[name] = {"steps": k, "l1_vs_oracle": float(d.mean()),
+                     "max_normwise_vs_oracle": float((d.max(axis=0) / np.abs(ref).max(axis=0)).max()),
+                     "l1_rho_vs_exact": float(np.abs(g[:, 0] - rho_ex).mean()),
+                     "linf_rho_vs_exact": float(np.abs(g[:, 0] - rho_ex).max())}
+    out["oracle_l1_rho_vs_exact"] = float(np.abs(ref[:, 0] - rho_ex).mean())
+    return out
+
+
 def cases_mod():
     from xfluids_gb300 import cases
     return cases
@@ -413,6 +451,7 @@ def run_gpu_arm(args, world, rank, local):
         del s64, smx, diff
     serving = bench_serving(local, args.serve_requests, MIXED) if args.serve_requests > 0 else None
     mixing = bench_mixing_layer(args, local, args.mixing_steps) if args.mixing_steps > 0 else None
+    accuracy = bench_accuracy(local) if args.accuracy else None
     d.close()
     if rank != 0:
         return 0
@@ -447,6 +486,7 @@ def run_gpu_arm(args, world, rank, local):
         "ensemble": ens or None,
         "serving": serving,
         "mixing_layer": mixing,
+        "accuracy": accuracy,
         "cpu_baseline": {"value": cpu_val, "unit": "cell-updates/s", "cores": cpu_threads, "kind": "port",
                          "sample": f"{cpu_steps} steps of the 1024^2 vortex ({cpu_el:.1f} s) on the oracle restatement"},
         "clocks": clk.summary(),
@@ -467,6 +507,7 @@ def main():
     ap.add_argument("--ensemble", type=int, default=1, help="run the 256-member batched ensemble (0 = skip)")
     ap.add_argument("--serve-requests", type=int, default=8, help="requests of the serving trace (0 = skip)")
     ap.add_argument("--mixing-steps", type=int, default=2, help="timed steps of the 3D mixing layer (0 = skip)")
+    ap.add_argument("--accuracy", type=int, default=1, help="FP64 drift vs the oracle and error vs the exact vortex")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()

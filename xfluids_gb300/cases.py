@@ -49,6 +49,16 @@ def isentropic_vortex(n=1024, cfl=0.5, precision=0, beta=5.0):
     return b, s, empty_thermal(), U, None
 
 
+def isentropic_vortex_exact(b, t, beta=5.0):
+    """Exact density of the vortex at time t: the initial vortex carried by the free stream
+    (1, 1) on the periodic [0,10]^2."""
+    X, Y, _ = cell_centres(b)
+    xv = np.mod(X - t, 10.0) - 5.0
+    yv = np.mod(Y - t, 10.0) - 5.0
+    r2 = xv * xv + yv * yv
+    return (1.0 - beta * beta * np.exp(1.0 - r2) / 28.0 / math.pi / math.pi) ** 2.5
+
+
 def sod(n=1024, cfl=0.5, precision=0, order=5):
     """1D Sod shock tube on [0,1]: (1, 0, 1) | (0.125, 0, 0.1) at x = 0.5, transmissive ends."""
     b = make_block((n, 0, 0), (1.0, 1.0, 1.0), [OUTFLOW] * 6, cfl=cfl)
