@@ -228,3 +228,25 @@ def test_mixed_cu6_close_to_fp64(cuda_lib):
     rel = np.where(den > 0, num / np.where(den > 0, den, 1.0), num)   # rho w is zero in 2D
     assert np.all(rel < 1e-4), rel
     f64.close(), fmx.close()
+
+
+def test_mixed_single_gas_glf_and_primitives(cuda_lib):
+    """Single-gas mixed form: the GLF maxima come from its FP32 primitives (the form writes no FP64
+    primitives during the step) and the primitives a caller reads back are those of the last
+    UpdateFluidStates; both close to the FP64 path."""
+    b, s, th, U, T = H.blast3d(artificial=GLF)
+    f64 = _fluid(b, s, th, U, T)
+    b2, s2, _, _, _ = H.blast3d(artificial=GLF)
+    s2.precision = MIXED
+    fmx = _fluid(b2, s2, th, U, T)
+    f64.initialize(), fmx.initialize()
+    st1, t1, n1 = f64.advance(5)
+    st2, t2, n2 = fmx.advance(30, t1)
+    assert st1 == 0 and st2 == 0 and abs(t2 - t1) <= 1e-12 * t1
+    a, r = H.inner_aos(b, fmx.get("U"), 5), H.inner_aos(b, f64.get("U"), 5)
+    num, den = np.abs(a - r).mean(axis=0), np.abs(r).mean(axis=0)
+    assert np.all(num / den < 1e-5), num / den
+    for nm in ("rho", "p", "u", "c", "H"):
+        x, y = fmx.get(nm), f64.get(nm)
+        assert np.abs(x - y).max() <= 1e-4 * np.abs(y).max(), nm
+    f64.close(), fmx.close()

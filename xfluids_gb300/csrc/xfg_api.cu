@@ -75,6 +75,17 @@ __global__ void k_soa_to_aos(const double *__restrict__ soa, double *__restrict_
     int n = (int)(t % E);
     aos[t] = soa[n * P + id];
 }
+// FP64 primitive arrays of the single-gas mixed form (which keeps them in FP32 only), filled from
+// its FP32 face primitives when a caller reads them: the values of the last UpdateFluidStates.
+__global__ void k_prims_from_primf(Geo g, DevFields f, double gamma) {
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= g.ncell()) return;
+    const long long P = g.pitch;
+    const double rho = f.primf[id], p = f.primf[5 * P + id];
+    f.rho[id] = rho, f.u[id] = f.primf[P + id], f.v[id] = f.primf[2 * P + id], f.w[id] = f.primf[3 * P + id];
+    f.H[id] = f.primf[4 * P + id], f.p[id] = p, f.c[id] = f.primf[6 * P + id];
+    f.gamma[id] = gamma, f.e[id] = p / ((gamma - 1.0) * rho);
+}
 __global__ void k_set_time(double *dtbuf, double t, double target) {
     dtbuf[0] = 0.0, dtbuf[1] = t, dtbuf[2] = target, dtbuf[3] = 0.0, dtbuf[4] = 0.0;
 }
@@ -341,6 +352,9 @@ int xfg_get_array(xfg_handle *h, int which, double *out) {
     if (!h || !out) return fail(-1, "null argument");
     CK(cudaSetDevice(h->device));
     DevFields &f = h->ctx.f;
+    const bool prim = which >= XFG_RHO && which <= XFG_E && which != XFG_T;
+    if (prim && h->sc.precision == XFG_MIXED && !h->sc.cop)
+        k_prims_from_primf<<<grid_for(h->N, 256), 256, 0, h->st>>>(h->ctx.g, f, h->sc.ncop_gamma);
     const double *src = nullptr;
     int comps = 1;
     switch (which) {

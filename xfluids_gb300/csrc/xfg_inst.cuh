@@ -69,7 +69,10 @@ struct Inst {
     static void glf(const LaunchCtx &c, unsigned long long *out, int guard) {
         // running maxima over the whole run (zeroed once when the handle is created), as the
         // reference's reductions fold in the previous eigen_block values
-        k_glf<<<grid_for(c.g.ncell(), kThreads), kThreads, 0, c.st>>>(c.g, c.f, out, guard);
+        if (MIXED && !COP)  // the single-gas mixed form keeps its primitives in FP32 only
+            k_glf_mixed<<<grid_for(c.g.ncell(), kThreads), kThreads, 0, c.st>>>(c.g, c.f, out, guard);
+        else
+            k_glf<<<grid_for(c.g.ncell(), kThreads), kThreads, 0, c.st>>>(c.g, c.f, out, guard);
     }
     static void rk(const LaunchCtx &c, int flag, double dt) {
         long long n = (long long)c.g.Xi * c.g.Yi * c.g.Zi;

@@ -149,6 +149,30 @@ __global__ void __launch_bounds__(kThreads) k_states_mixed(Geo g, DevFields f, D
     if (want_lam) lam_block_reduce_f(g, f, lamx, lamy, lamz);
 }
 
+// GLF maxima of the single-gas mixed form from its FP32 face primitives (this form writes no FP64
+// primitives): max over all cells of |u_d - c|, |u_d|, |u_d + c| (ConVenction_block.hpp:115-215).
+static __global__ void __launch_bounds__(kThreads) k_glf_mixed(Geo g, DevFields f, unsigned long long *glf, int guard) {
+    if (guard && step_done(f)) return;
+    const long long N = g.ncell(), P = g.pitch;
+    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double m[9];
+    for (int q = 0; q < 9; q++) m[q] = 0.0;
+    if (id < N) {
+        const double c = f.primf[6 * P + id];
+        for (int d = 0; d < 3; d++) {
+            const double v = f.primf[(1 + d) * P + id];
+            m[3 * d + 0] = fabs(v - c);
+            m[3 * d + 1] = fabs(v);
+            m[3 * d + 2] = fabs(v + c);
+        }
+    }
+    for (int q = 0; q < 9; q++) {
+        double x = m[q];
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&glf[q], x);
+    }
+}
+
 template <int D, int E>
 __device__ __forceinline__ float project_f(const float *lrow, int n, const float *__restrict__ A, long long P, long long q) {
     float acc = 0.f;
