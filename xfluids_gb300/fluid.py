@@ -65,10 +65,15 @@ class Fluid:
         check(lib().xfg_checkpoint_read(self._h, str(path).encode(), C.byref(st), C.byref(t), C.byref(dur)))
         return st.value, t.value, dur.value
 
-    def get(self, name: str) -> np.ndarray:
+    def get(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        """Array `name` in the reference layout; into `out` when given (e.g. a PinnedArray's
+        array, so that the device-to-host copy runs at the link's speed)."""
         n = self.block.ncell
         size = n * self.E if name in AOS_E else (n * self.NS if name == "y" else n)
-        out = np.empty(size, dtype=np.float64)
+        if out is None:
+            out = np.empty(size, dtype=np.float64)
+        elif out.size != size or out.dtype != np.float64 or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError(f"out must be a contiguous float64 array of {size} values")
         check(lib().xfg_get_array(self._h, ARRAYS[name], out.ctypes.data_as(C.c_void_p)))
         return out
 

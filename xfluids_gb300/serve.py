@@ -226,7 +226,9 @@ def summary(trace, wall_s=None, device_ms=None):
     span = max(r.done for r in trace) - min(r.start for r in trace)
     out = {"requests": len(trace), "p50_s": float(np.percentile(tts, 50)), "p99_s": float(np.percentile(tts, 99)),
            "max_s": float(tts.max()), "makespan_s": float(span), "cell_updates": work,
-           "cell_updates_per_s": work / span, "errors": int(sum(1 for r in trace if r.error))}
+           "cell_updates_per_s": work / span, "errors": int(sum(1 for r in trace if r.error)),
+           # arrival rate the server sustains at this throughput: throughput / mean work per request
+           "sustainable_rate_req_s": (work / span) / (work / len(trace)) if work > 0 else 0.0}
     if device_ms is not None:
         out["device_s"] = device_ms * 1e-3
     return out
