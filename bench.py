@@ -49,9 +49,12 @@ class Dist:
         if world > 1:
             import torch
             import torch.distributed as td
-            torch.cuda.set_device(local)
-            td.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+            cuda = torch.cuda.is_available()
+            if cuda:
+                torch.cuda.set_device(local)
+            td.init_process_group("nccl" if cuda else "gloo")
             self.td, self.torch = td, torch
+            self.device = "cuda" if cuda else "cpu"
 
     def barrier(self):
         if self.world > 1:
@@ -60,14 +63,14 @@ class Dist:
     def max(self, x):
         if self.world == 1:
             return x
-        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device="cuda")
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device=self.device)
         self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
         return float(t.item())
 
     def sum(self, x):
         if self.world == 1:
             return x
-        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device="cuda")
+        t = self.torch.tensor([float(x)], dtype=self.torch.float64, device=self.device)
         self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
         return float(t.item())
 
