@@ -87,7 +87,26 @@ typedef struct xfg_scheme {
     int positivity;        /* PositivityPreserving (src/read_ini/settings/read_json.cpp:68): the flux
                               limiter of FDM_Method/positive-definite_eigen/PositivityPreserving_kernels.hpp
                               after each face sweep (ConVenction_block.hpp:328-410); 0 = off */
+    int viscous;           /* Visc | Visc_Heat << 1 | Visc_Diffu << 2 (cmake/init_options.cmake:81-91):
+                              fourth-order viscous, heat-conduction and diffusion fluxes subtracted
+                              from the face fluxes (ConVenction_block.hpp:419-566); mixtures only,
+                              needs xfg_set_transport */
 } xfg_scheme;
+
+/* Transport data of a viscous run: the fitted coefficients Setup::GetFitCoefficient computes
+ * (src/read_ini/src/viscfit.cpp:148-200) and the species characteristics of transport_data.dat,
+ * as Thermal holds them (src/include/global_setup.h:202-208), plus the two diffusion limiters of
+ * Block (src/read_ini/src/iniset.cpp:358-359). */
+#define XFG_FIT_ORDER 4      /* order_polynominal_fitted */
+#define XFG_SPCH 9           /* SPCH_Sz: geo, epsilon_kB, d, mue, alpha, Zrot_298, Wi, Vis, SID */
+typedef struct xfg_transport {
+    int num_species;
+    double visc[XFG_MAX_SPECIES * XFG_FIT_ORDER];                     /* ln(mu) in powers of ln(T) */
+    double therm[XFG_MAX_SPECIES * XFG_FIT_ORDER];                    /* ln(kappa) in powers of ln(T) */
+    double dkj[XFG_MAX_SPECIES * XFG_MAX_SPECIES * XFG_FIT_ORDER];    /* ln(p D_kj), k-major */
+    double species_chara[XFG_MAX_SPECIES * XFG_SPCH];
+    double yil_limiter, dim_limiter;                                  /* Block::Yil_limiter, Dim_limiter */
+} xfg_transport;
 
 /* Arrays a caller can read back (xfg_get_array). */
 enum xfg_array {
@@ -196,6 +215,11 @@ int xfg_device_array(xfg_handle *h, int which, double **ptr, size_t *pitch);
  * FMA chain; used as the roofline denominator of the compute-bound kernels. out[0] = FP64,
  * out[1] = FP32, out[2] = SM clock (MHz) reported by the driver during the run (0 if unknown). */
 int xfg_measure_pipe_peaks(int device, double *out);
+
+/* Transport data of a viscous scheme (xfg_scheme.viscous != 0); required before the first
+ * xfg_compute_lu / xfg_step of such a handle. The drop-in copies Setup::h_thermal's fitted
+ * coefficients and species characteristics. */
+int xfg_set_transport(xfg_handle *h, const xfg_transport *tr);
 
 /* Checkpoint files in the reference's format (XFLUIDS::Output_Ubak / Read_Ubak,
  * src/XFLUIDS.cpp:658-724): int Step, double Time, float duration, then U in the reference layout

@@ -25,6 +25,8 @@ FLAVOURS=(
   # WENO-CU6 (SCHEME_ORDER=6, schemes_device.hpp:18-19)
   "ncop_w6_llf|-DSCHEME_ORDER=6 -DArtificial_type=2 -DNUM_SPECIES=1 -DNUM_COP=0 -DNCOP_Gamma=1.4 -DThermo=1|2D-EulerVortex|runtime.dat/NO-COP"
   "cop5_w6_roe_janaf|-DCOP -DSCHEME_ORDER=6 -DArtificial_type=1 -DThermo=0|1D-X-Y-Z/insert-st|cases/mixing5"
+  # viscous, heat-conduction and diffusion fluxes (init_options.cmake:81-91)
+  "cop5_w5_llf_janaf_visc|-DCOP -DSCHEME_ORDER=5 -DArtificial_type=2 -DThermo=0 -UVisc -DVisc=1 -DVisc_Heat=1 -DVisc_Diffu=1|1D-X-Y-Z/insert-st|cases/mixing5"
   # PositivityPreserving on (init_sample.cmake:218-219 sets POSP=1 for the samples that use it)
   "ncop_w5_llf_pp|-DSCHEME_ORDER=5 -DArtificial_type=2 -DNUM_SPECIES=1 -DNUM_COP=0 -DNCOP_Gamma=1.4 -DThermo=1 -UPOSP -DPOSP=1|2D-EulerVortex|runtime.dat/NO-COP"
   "cop5_w5_llf_janaf_pp|-DCOP -DSCHEME_ORDER=5 -DArtificial_type=2 -DThermo=0 -UPOSP -DPOSP=1|1D-X-Y-Z/insert-st|cases/mixing5"

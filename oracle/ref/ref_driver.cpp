@@ -8,6 +8,9 @@
 //                U, U1, LU (E*ncell each), rho, p, u, v, w, c, H, T (ncell each), y (NUM_SPECIES*ncell)
 //   XFREF_STEPS  number of time steps
 //   XFREF_TEND   end time (the dt clip of XFLUIDS::Evolution)
+//   XFREF_TRANSPORT (viscous builds) file for the fitted transport coefficients of Setup: int32 NS,
+//                int32 order, visc (NS*order), therm (NS*order), Dkj (NS*NS*order), species_chara
+//                (NS*SPCH_Sz), Yil_limiter, Dim_limiter (doubles)
 // The sequence mirrors main.cpp:36-49 and the loop body of XFLUIDS::Evolution (src/XFLUIDS.cpp:172-214).
 #include <cstdio>
 #include <cstdlib>
@@ -36,6 +39,19 @@ int main(int argc, char *argv[]) {
     solver.AllocateMemory(setup.q);
     solver.InitialCondition(setup.q);
     Fluid *fl = solver.fluids[0];
+#if Visc
+    if (const char *tp = getenv("XFREF_TRANSPORT")) {
+        FILE *ft = fopen(tp, "wb");
+        const int ns = NUM_SPECIES, order = order_polynominal_fitted;
+        put(ft, &ns, 4), put(ft, &order, 4);
+        for (int k = 0; k < ns; k++) put(ft, setup.h_thermal.fitted_coefficients_visc[k], 8 * order);
+        for (int k = 0; k < ns; k++) put(ft, setup.h_thermal.fitted_coefficients_therm[k], 8 * order);
+        for (int k = 0; k < ns * ns; k++) put(ft, setup.h_thermal.Dkj_matrix[k], 8 * order);
+        put(ft, setup.h_thermal.species_chara, 8 * ns * SPCH_Sz);
+        put(ft, &setup.BlSz.Yil_limiter, 8), put(ft, &setup.BlSz.Dim_limiter, 8);
+        fclose(ft);
+    }
+#endif
     const size_t ncell = (size_t)setup.BlSz.Xmax * setup.BlSz.Ymax * setup.BlSz.Zmax;
 
     FILE *fi = fopen(in, "rb");

@@ -24,6 +24,7 @@ FLAVOURS = {
     "ncop_w5_llf": (5, 1), "ncop_w7_llf": (5, 1), "ncop_w5_roe": (5, 1), "ncop_w5_glf": (5, 1),
     "cop4g_w5_llf_nasa": (8, 4), "cop5_w7_llf_janaf": (9, 5),
     "ncop_w6_llf": (5, 1), "cop5_w6_roe_janaf": (9, 5),
+    "cop5_w5_llf_janaf_visc": (9, 5),
     # built with PositivityPreserving on (-DPOSP=1, and the JSON key below)
     "ncop_w5_llf_pp": (5, 1), "cop5_w5_llf_janaf_pp": (9, 5),
 }
@@ -49,7 +50,22 @@ def _case_json(block, cfl, domain, positivity=False):
     }
 
 
-def run_reference(flavour, block, U, T=None, steps=1, t_end=1e300, domain=None):
+def read_transport(path):
+    """The fitted transport coefficients dumped by a viscous reference build (XFREF_TRANSPORT)."""
+    raw = open(path, "rb").read()
+    ns, order = struct.unpack_from("<ii", raw, 0)
+    a = np.frombuffer(raw, dtype=np.float64, offset=8)
+    o = 0
+    out = {}
+    for name, n in (("visc", ns * order), ("therm", ns * order), ("dkj", ns * ns * order), ("chara", ns * 9),
+                    ("limits", 2)):
+        out[name] = a[o:o + n].copy()
+        o += n
+    out["ns"], out["order"] = ns, order
+    return out
+
+
+def run_reference(flavour, block, U, T=None, steps=1, t_end=1e300, domain=None, transport_out=None):
     """Returns a list of stage records {step, flag, dt, t, U, U1, LU, rho, ..., y}."""
     E, NS = FLAVOURS[flavour]
     exe_rel = os.path.join(".", flavour, "xfluids_ref")
@@ -70,6 +86,8 @@ def run_reference(flavour, block, U, T=None, steps=1, t_end=1e300, domain=None):
             if T is not None:
                 f.write(np.ascontiguousarray(T, dtype=np.float64).tobytes())
         env = dict(os.environ, XFREF_IN=fin, XFREF_OUT=fout, XFREF_STEPS=str(steps), XFREF_TEND=repr(float(t_end)))
+        if transport_out:
+            env["XFREF_TRANSPORT"] = os.path.abspath(transport_out)
         r = subprocess.run([exe_rel], cwd=REF_DIR, env=env, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference run failed ({r.returncode}): {r.stderr[-2000:]} {r.stdout[-2000:]}")

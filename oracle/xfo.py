@@ -11,7 +11,7 @@ import subprocess
 
 import numpy as np
 
-from xfluids_gb300.abi import Block, Scheme, Thermal, ARRAYS, AOS_E
+from xfluids_gb300.abi import Block, Scheme, Thermal, Transport, ARRAYS, AOS_E
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
@@ -49,7 +49,7 @@ def lib():
             "xfo_set_threads": [I], "xfo_set_state": [P, P, P], "xfo_boundary": [P, I],
             "xfo_update_states": [P, I], "xfo_compute_lu": [P, I], "xfo_update_rk3": [P, I, D],
             "xfo_get_dt": [P, C.POINTER(D)], "xfo_step": [P, D, C.POINTER(D), C.POINTER(D)],
-            "xfo_set_time": [P, D], "xfo_get_array": [P, I, P],
+            "xfo_set_time": [P, D], "xfo_get_array": [P, I, P], "xfo_set_transport": [P, C.POINTER(Transport)],
             "xfo_count_flops": [C.POINTER(Block), C.POINTER(Scheme), C.POINTER(Thermal), P, P, I,
                                 C.POINTER(C.c_uint64)],
         }.items():
@@ -66,12 +66,15 @@ def set_threads(n: int) -> int:
 class Oracle:
     """One fluid block on the CPU, stage-by-stage like class Fluid."""
 
-    def __init__(self, block: Block, scheme: Scheme, thermal: Thermal, U: np.ndarray, T=None):
+    def __init__(self, block: Block, scheme: Scheme, thermal: Thermal, U: np.ndarray, T=None, transport=None):
         self.block, self.scheme, self.thermal = block, scheme, thermal
         self.E = scheme.Emax
         self.h = lib().xfo_create(C.byref(block), C.byref(scheme), C.byref(thermal))
         if not self.h:
             raise MemoryError("oracle allocation failed")
+        if transport is not None:
+            self.transport = transport
+            lib().xfo_set_transport(self.h, C.byref(transport))
         self.set_state(U, T)
 
     def __del__(self):

@@ -67,6 +67,11 @@ xfo_handle *xfo_create(const xfg_block *bl, const xfg_scheme *sc, const xfg_ther
 
 void xfo_destroy(xfo_handle *h) { delete h; }
 
+int xfo_set_transport(xfo_handle *h, const xfg_transport *tr) {
+    h->s.cf.tr = *tr;
+    return 0;
+}
+
 int xfo_set_state(xfo_handle *h, const double *U, const double *T) {
     load(h->s, U, T);
     return 0;

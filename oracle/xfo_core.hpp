@@ -177,6 +177,7 @@ struct Config {
     xfg_block bl;
     xfg_scheme sc;
     xfg_thermal th;
+    xfg_transport tr;  // viscous schemes
     int E() const { return sc.cop ? sc.num_species + 4 : 5; }
     int NS() const { return sc.num_species; }
     int NCOP() const { return sc.cop ? sc.num_species - 1 : 0; }
@@ -193,12 +194,17 @@ struct Fields {
     std::vector<R> eig[3];        // eigen_local_{x,y,z}, AoS Emax
     R eigen_block[3][kMaxE];      // GLF maxima
     R uvw_c_max[3];
+    std::vector<R> Vde, mu, kappa, Dkm, hi;  // viscous: 9 velocity derivatives, transport, enthalpies
     void alloc(const Config &cf) {
         size_t n = cf.ncell(), E = cf.E();
         for (std::vector<R> *a : {&U, &U1, &LU, &FluxF, &FluxG, &FluxH, &Fw[0], &Fw[1], &Fw[2], &eig[0], &eig[1], &eig[2]})
             a->assign(n * E, R(0.0));
         for (std::vector<R> *a : {&rho, &p, &u, &v, &w, &this->c, &gamma, &e, &H, &T, &Cp, &Rm}) a->assign(n, R(0.0));
         y.assign(n * cf.NS(), R(0.0));
+        if (cf.sc.viscous) {
+            Vde.assign(9 * n, R(0.0)), mu.assign(n, R(0.0)), kappa.assign(n, R(0.0));
+            Dkm.assign(n * cf.NS(), R(0.0)), hi.assign(n * cf.NS(), R(0.0));
+        }
         for (int d = 0; d < 3; d++)
             for (int k = 0; k < kMaxE; k++) eigen_block[d][k] = R(0.0);
         for (int d = 0; d < 3; d++) uvw_c_max[d] = R(0.0);
@@ -907,6 +913,8 @@ void lu_divergence(const Config &cf, Fields<R> &f) {
 template <class R>
 inline R pp_min(R a, R b) { return (b < a) ? b : a; }  // sycl::min of the shim
 template <class R>
+inline R pp_max(R a, R b) { return (a < b) ? b : a; }  // sycl::max of the shim
+template <class R>
 void pp_limit(const Config &cf, Fields<R> &f, const std::vector<R> &UI, int d) {
     const xfg_block &b = cf.bl;
     const int E = cf.E(), NCOP = cf.NCOP();
@@ -963,6 +971,300 @@ void pp_limit(const Config &cf, Fields<R> &f, const std::vector<R> &UI, int d) {
             }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Viscous, heat-conduction and diffusion fluxes (Visc / Visc_Heat / Visc_Diffu), fourth order:
+// GetCellCenterDerivative (viscosity/Visc_block.hpp:7-84), Gettransport_coeff_aver
+// (Visc_kernels.hpp:226-245, Visc_device.h), the diffusion limiter reduction and
+// GetWallViscousFlux{X,Y,Z} (Fourth_Order/Visc_Order_kernels.hpp, Flux_discrete.h), launched by
+// ConVenction_block.hpp:419-566 after the face sweeps (and the positivity limiter).
+// ---------------------------------------------------------------------------------------------
+enum { DUCX, DVCX, DWCX, DUCY, DVCY, DWCY, DUCZ, DVCZ, DWCZ };
+constexpr double kTwle = 1.0 / 12.0, kTwfr = 1.0 / 24.0, kSxtn = 1.0 / 16.0;
+
+// Viscosity / Thermal_conductivity / the numerator of GetDkj (Visc_device.h:8-100): exp of the
+// fitted cubic in ln T (Horner from the highest power)
+template <class R>
+R fit_exp(const double *c, R T) {
+    using std::exp;
+    using std::log;
+    R v = R(c[XFG_FIT_ORDER - 1]);
+    for (int i = XFG_FIT_ORDER - 2; i >= 0; i--) v = v * log(T) + R(c[i]);
+    return exp(v);
+}
+// PHI (Visc_device.h:30-38), the Wilke mixing factor of species k with j
+template <class R>
+R wilke_phi(const xfg_transport &tr, int k, int j, R T) {
+    using std::pow;
+    using std::sqrt;
+    const double *sk = &tr.species_chara[k * XFG_SPCH], *sj = &tr.species_chara[j * XFG_SPCH];
+    const int ik = (int)sk[8], ij = (int)sj[8];
+    R phi = R(pow(sj[6] / sk[6], 0.25)) *
+            pow(fit_exp(&tr.visc[ik * XFG_FIT_ORDER], T) / fit_exp(&tr.visc[ij * XFG_FIT_ORDER], T), R(0.5));
+    phi = (phi + R(1.0)) * (phi + R(1.0)) * R(0.5) / R(sqrt(2.0));
+    phi = phi * R(pow(1.0 + sk[6] / sj[6], -0.5));
+    return phi;
+}
+
+// GetInnerCellCenterDerivativeKernel (Fourth_Order/Visc_Order_kernels.hpp:16-72) on the cells
+// [B-2, inner+B+2) of each active direction, then CenterDerivativeBCKernel{X,Y,Z}
+// (Visc_kernels.hpp:7-204) on the ghost layers in that order. Derivatives along an absent
+// direction are zero (the reference multiplies a read outside the array by DimZ_t = 0).
+template <class R>
+void velocity_derivatives(const Config &cf, Fields<R> &f) {
+    const xfg_block &b = cf.bl;
+    const int dims[3] = {b.DimX, b.DimY, b.DimZ};
+    const int r0[3] = {b.DimX ? b.Bwidth_X - 2 : 0, b.DimY ? b.Bwidth_Y - 2 : 0, b.DimZ ? b.Bwidth_Z - 2 : 0};
+    const int r1[3] = {b.DimX ? b.X_inner + b.Bwidth_X + 2 : 1, b.DimY ? b.Y_inner + b.Bwidth_Y + 2 : 1,
+                       b.DimZ ? b.Z_inner + b.Bwidth_Z + 2 : 1};
+    const size_t n = cf.ncell(), st[3] = {1, (size_t)b.Xmax, (size_t)b.Xmax * b.Ymax};
+    const R inv[3] = {R(b._dx), R(b._dy), R(b._dz)};
+    const R dt[3] = {R(b.DimX), R(b.DimY), R(b.DimZ)};
+    const std::vector<R> *vel[3] = {&f.u, &f.v, &f.w};
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = r0[2]; k < r1[2]; k++)
+        for (int j = r0[1]; j < r1[1]; j++)
+            for (int i = r0[0]; i < r1[0]; i++) {
+                const size_t id = (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i;
+                for (int d = 0; d < 3; d++)      // derivative direction
+                    for (int c = 0; c < 3; c++) {  // velocity component
+                        R val = R(0.0);
+                        if (dims[d]) {
+                            const std::vector<R> &q = *vel[c];
+                            val = (R(8.0) * (q[id + st[d]] - q[id - st[d]]) - (q[id + 2 * st[d]] - q[id - 2 * st[d]])) *
+                                  inv[d] * R(kTwle) * dt[d];
+                            if (c != d) val = val * dt[c];
+                        } else {
+                            val = R(0.0) * dt[d];
+                        }
+                        f.Vde[(3 * d + c) * n + id] = val;
+                    }
+            }
+    // ghost layers: the four components each direction's flux reads
+    static const int comps[3][4] = {{DUCY, DUCZ, DVCY, DWCZ}, {DVCX, DVCZ, DUCX, DWCZ}, {DWCX, DWCY, DUCX, DVCY}};
+    const int ext[3] = {b.Xmax, b.Ymax, b.Zmax}, inner[3] = {b.X_inner, b.Y_inner, b.Z_inner};
+    const int bw[3] = {b.Bwidth_X, b.Bwidth_Y, b.Bwidth_Z};
+    for (int d = 0; d < 3; d++) {
+        if (!dims[d]) continue;
+        const int ta = d == 0 ? b.Ymax : b.Xmax, tb = d == 2 ? b.Ymax : b.Zmax;
+        for (int side = 0; side < 2; side++) {
+            const int BC = b.Boundarys[2 * d + side];
+            const int mirror_offset = side == 0 ? 0 : inner[d];
+            const int index_inner = side == 0 ? bw[d] : ext[d] - bw[d] - 1;
+            const int sign = side == 0 ? 1 : -1;
+            for (int q = 0; q < tb; q++)
+                for (int p = 0; p < ta; p++)
+                    for (int g = 0; g < bw[d]; g++) {
+                        const int cn = side == 0 ? g : g + ext[d] - bw[d];
+                        auto cell = [&](int c) {
+                            const int i = d == 0 ? c : p, j = d == 0 ? p : (d == 1 ? c : q), k = d == 2 ? c : q;
+                            return (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i;
+                        };
+                        const size_t id = cell(cn);
+                        long src = -1;
+                        R sgn = R(1.0);
+                        switch (BC) {
+                        case XFG_SYMMETRY: src = (long)cell(2 * (bw[d] + mirror_offset) - 1 - cn); break;
+                        case XFG_PERIODIC: src = (long)cell(cn + sign * inner[d]); break;
+                        case XFG_OUTFLOW: src = (long)cell(index_inner); break;
+                        case XFG_NSLIPWALL:
+                            // the mirror of X and Y; the reference's Z case indexes k - offset
+                            // (Visc_kernels.hpp:183), outside the array
+                            src = (long)cell(2 * (bw[d] + mirror_offset) - 1 - cn), sgn = R(-1.0);
+                            break;
+                        case XFG_INFLOW:
+                            for (int m = 0; m < 4; m++) f.Vde[comps[d][m] * n + id] = R(0.0);
+                            break;
+                        default: break;  // viscWall, slipWall, innerBlock: unchanged
+                        }
+                        if (src >= 0)
+                            for (int m = 0; m < 4; m++)
+                                f.Vde[comps[d][m] * n + id] = sgn == R(1.0) ? f.Vde[comps[d][m] * n + src]
+                                                                             : -f.Vde[comps[d][m] * n + src];
+                    }
+        }
+    }
+}
+
+// Gettransport_coeff_aver (Visc_kernels.hpp:226-245) with Get_transport_coeff_aver
+// (Visc_device.h:106-177) on every cell: mole fractions (get_xi), Wilke-averaged viscosity and
+// thermal conductivity, species enthalpies and mixture-averaged diffusion coefficients.
+template <class R>
+void transport(const Config &cf, Fields<R> &f) {
+    using std::ceil;
+    const xfg_transport &tr = cf.tr;
+    const ThermoTable tt = cf.table();
+    const int NS = cf.NS();
+    const bool heat = cf.sc.viscous & 2, diffu = cf.sc.viscous & 4;
+    const long n = (long)cf.ncell();
+#pragma omp parallel for schedule(static)
+    for (long id = 0; id < n; id++) {
+        const R T = f.T[id], rho = f.rho[id], p = f.p[id];
+        R X[kMaxE];
+        R C_total = R(0.0);
+        for (int i = 0; i < NS; i++) {
+            X[i] = f.y[NS * id + i] * R(cf.th._Wi[i]) * R(1e-3) * rho;
+            C_total = C_total + X[i];
+        }
+        const R _C = R(1.0) / C_total;
+        for (int i = 0; i < NS; i++) X[i] = X[i] * _C;
+        if (diffu)
+            for (int k = 0; k < NS; k++) f.hi[NS * id + k] = enthalpy(tt, T, tt.Ri[k], k);
+        R mu = R(0.0), kap = R(0.0);
+        for (int k = 0; k < NS; k++) {
+            R den = R(0.0);
+            for (int i = 0; i < NS; i++) den = den + X[i] * wilke_phi(tr, k, i, T);
+            const R _den = R(1.0) / den;
+            const int ik = (int)tr.species_chara[k * XFG_SPCH + 8];
+            mu = mu + X[k] * fit_exp(&tr.visc[ik * XFG_FIT_ORDER], T) * _den;
+            if (heat) kap = kap + X[k] * fit_exp(&tr.therm[ik * XFG_FIT_ORDER], T) * _den;
+        }
+        f.mu[id] = mu;
+        if (heat) f.kappa[id] = kap;
+        if (diffu) {
+            auto dkj = [&](int a, int c) {  // GetDkj: fit / p
+                const int ia = (int)tr.species_chara[a * XFG_SPCH + 8], ic = (int)tr.species_chara[c * XFG_SPCH + 8];
+                return fit_exp(&tr.dkj[(ia * NS + ic) * XFG_FIT_ORDER], T) / p;
+            };
+            for (int k = 0; k < NS; k++) {
+                R Dk;
+                if (NS > 1) {
+                    R t1 = R(0.0), t2 = R(1.0e-20);
+                    for (int i = 0; i < NS; i++)
+                        if (i != k) {
+                            t1 += (X[i] + R(1.0e-40)) * R(cf.th.Wi[i]);
+                            t2 += (X[i] + R(1.0e-40)) / (dkj(i, k) + R(1.0e-40));
+                        }
+                    if (!(R(0.0) < ceil(t1))) Dk = dkj(k, k);  // sycl::step(ceil(t1), 0) == 1
+                    else Dk = t1 / t2 / rho * C_total;
+                } else {
+                    Dk = dkj(0, 0);
+                }
+                Dk *= R(1.0e-1);
+                f.Dkm[NS * id + k] = Dk < R(1.0e-10) ? R(1.0e-10) : Dk;  // sycl::max(Dk, 1e-10)
+            }
+        }
+    }
+}
+
+// GetWallViscousFlux{X,Y,Z} (Fourth_Order/Visc_Order_kernels.hpp:74-342 with Flux_discrete.h) on
+// the faces i+1/2, i in [B-1, inner+B) along d: F_wall_v subtracted from the face flux.
+template <class R>
+void viscous_faces(const Config &cf, Fields<R> &f, int d, const R *yil_lim, const R *diffu_lim) {
+    const xfg_block &b = cf.bl;
+    const int E = cf.E(), NS = cf.NS();
+    const bool heat = cf.sc.viscous & 2, diffu = cf.sc.viscous & 4;
+    const size_t n = cf.ncell();
+    const size_t st = d == 0 ? 1 : (d == 1 ? (size_t)b.Xmax : (size_t)b.Xmax * b.Ymax);
+    const R _dl = R(d == 0 ? b._dx : (d == 1 ? b._dy : b._dz));
+    const R dt[3] = {R(b.DimX), R(b.DimY), R(b.DimZ)};
+    const int i0 = b.Bwidth_X - (d == 0 ? 1 : 0), j0 = b.Bwidth_Y - (d == 1 ? 1 : 0), k0 = b.Bwidth_Z - (d == 2 ? 1 : 0);
+    const int i1 = b.X_inner + b.Bwidth_X, j1 = b.Y_inner + b.Bwidth_Y, k1 = b.Z_inner + b.Bwidth_Z;
+    std::vector<R> &Fw = f.Fw[d];
+    const std::vector<R> *vel[3] = {&f.u, &f.v, &f.w};
+    // cross derivatives: in the momentum flux along c (c != d) the derivative of u_d along c; in the
+    // normal momentum flux the divergence terms of the other two directions
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = k0; k < k1; k++)
+        for (int j = j0; j < j1; j++)
+            for (int i = i0; i < i1; i++) {
+                const size_t id = (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i;
+                const size_t m1 = id - st, p1 = id + st, p2 = id + 2 * st;
+                auto half = [&](const std::vector<R> &a, size_t off = 0) {  // 4th-order face average
+                    return (R(9.0) * (a[off + p1] + a[off + id]) - (a[off + p2] + a[off + m1])) * R(kSxtn);
+                };
+                auto grad = [&](const std::vector<R> &a, size_t off = 0) {  // 4th-order face gradient
+                    return (R(27.0) * (a[off + p1] - a[off + id]) - (a[off + p2] - a[off + m1])) * _dl * R(kTwfr);
+                };
+                const R mue = half(f.mu);
+                const R lamada = -R(2.0) * R(kOT) * mue;
+                auto b27 = [&](const std::vector<R> &a) { return R(27.0) * (a[p1] - a[id]) - (a[p2] - a[m1]); };
+                auto vd = [&](int c, size_t q) { return f.Vde[(size_t)c * n + q]; };
+                R fv[3], hv[3];
+                for (int c = 0; c < 3; c++) {
+                    if (c == d) {
+                        // (2 mue + lambda) du_d/dx_d + lambda (the two other diagonal derivatives)
+                        const int oa = c == 0 ? DVCY : DUCX, ob = c == 2 ? DVCY : DWCZ;
+                        fv[c] = (R(2.0) * mue + lamada) * b27(*vel[c]) * _dl * R(kTwfr);
+                        fv[c] += lamada *
+                                 (R(9.0) * (vd(oa, p1) + vd(oa, id)) - (vd(oa, p2) + vd(oa, m1)) +
+                                  R(9.0) * (vd(ob, p1) + vd(ob, id)) - (vd(ob, p2) + vd(ob, m1))) *
+                                 R(kSxtn);
+                        hv[c] = half(*vel[c]);
+                    } else {
+                        // mue (du_c/dx_d + du_d/dx_c), the second from the cell-centre derivatives
+                        const int cr = 3 * c + d;  // derivative of u_d along x_c
+                        fv[c] = mue * b27(*vel[c]) * _dl * R(kTwfr) * dt[c];
+                        fv[c] += mue * (R(9.0) * (vd(cr, p1) + vd(cr, id)) - (vd(cr, p2) + vd(cr, m1))) * R(kSxtn) * dt[c];
+                        hv[c] = half(*vel[c]) * dt[c];
+                    }
+                }
+                R F[kMaxE];
+                F[0] = R(0.0), F[1] = fv[0], F[2] = fv[1], F[3] = fv[2];
+                F[4] = fv[0] * hv[0] + fv[1] * hv[1] + fv[2] * hv[2];
+                if (heat) {
+                    R kk = half(f.kappa);
+                    kk *= grad(f.T);
+                    F[4] += kk;
+                }
+                if (diffu) {
+                    const R rho_wall = half(f.rho);
+                    R CorrectTerm = R(0.0), Dim_Yil = R(1.0e-20);
+                    R Yi_wall[kMaxE];
+                    for (int l = 0; l < NS; l++) {
+                        auto yl = [&](size_t c) { return f.y[NS * c + l]; };
+                        auto hl = [&](size_t c) { return f.hi[NS * c + l]; };
+                        auto dl = [&](size_t c) { return f.Dkm[NS * c + l]; };
+                        const R hi_wall = (R(9.0) * (hl(p1) + hl(id)) - (hl(p2) + hl(m1))) * R(kSxtn);
+                        const R Dim_wall = (R(9.0) * (dl(p1) + dl(id)) - (dl(p2) + dl(m1))) * R(kSxtn);
+                        R Yil = (R(27.0) * (yl(p1) - yl(id)) - (yl(p2) - yl(m1))) * _dl * R(kTwfr);
+                        Yil = pp_min(pp_max(Yil, -yil_lim[l]), yil_lim[l]);
+                        R Yw = (R(9.0) * (yl(p1) + yl(id)) - (yl(p2) + yl(m1))) * R(kSxtn);
+                        Yi_wall[l] = pp_min(pp_max(Yw, R(1.0E-20)), R(1.0));
+                        Dim_Yil = pp_min(pp_max(Dim_wall * Yil, -diffu_lim[l]), diffu_lim[l]);
+                        CorrectTerm += Dim_Yil;
+                        F[4] += rho_wall * hi_wall * Dim_Yil;
+                    }
+                    CorrectTerm *= rho_wall;
+                    // every species takes the last species' Dim_Yil (MARCO_VIS_Diffu, Flux_discrete.h:57-61)
+                    for (int p = 5; p < E; p++) F[p] = rho_wall * Dim_Yil - Yi_wall[p - 5] * CorrectTerm;
+                } else {
+                    for (int p = 5; p < E; p++) F[p] = R(0.0);
+                }
+                for (int c = 0; c < E; c++) Fw[E * id + c] -= F[c];
+            }
+}
+
+template <class R>
+void viscous_lu(const Config &cf, Fields<R> &f) {
+    const xfg_block &b = cf.bl;
+    const int dims[3] = {b.DimX, b.DimY, b.DimZ};
+    const int NS = cf.NS();
+    velocity_derivatives(cf, f);
+    transport(cf, f);
+    // diffusion limiters (ConVenction_block.hpp:457-503) of a single block: the Y range of the
+    // inner cells (reductions seeded with 0) times Yil_limiter, and Dim_max = 0 * ... = 0 (the Dkm
+    // reduction is not taken; only the MPI build resets it to 1)
+    R yil[kMaxE], dlim[kMaxE];
+    for (int nn = 0; nn < NS; nn++) {
+        R ymin = R(0.0), ymax = R(0.0), Dmax = R(0.0);
+        if (cf.sc.viscous & 4) {
+            for (int k = b.Bwidth_Z; k < b.Z_inner + b.Bwidth_Z; k++)
+                for (int j = b.Bwidth_Y; j < b.Y_inner + b.Bwidth_Y; j++)
+                    for (int i = b.Bwidth_X; i < b.X_inner + b.Bwidth_X; i++) {
+                        const size_t id = (size_t)b.Xmax * b.Ymax * k + (size_t)b.Xmax * j + i;
+                        const R yv = f.y[NS * id + nn];
+                        ymin = pp_min(ymin, yv), ymax = pp_max(ymax, yv);
+                    }
+            ymax -= ymin;
+            ymax *= R(cf.tr.yil_limiter);
+            Dmax *= R(cf.tr.dim_limiter) * ymax;
+        }
+        yil[nn] = ymax, dlim[nn] = Dmax;
+    }
+    for (int d = 0; d < 3; d++)
+        if (dims[d]) viscous_faces(cf, f, d, yil, dlim);
+}
+
 template <class R>
 void compute_lu(const Config &cf, Fields<R> &f, const std::vector<R> &UI) {
     const int dims[3] = {cf.bl.DimX, cf.bl.DimY, cf.bl.DimZ};
@@ -972,6 +1274,7 @@ void compute_lu(const Config &cf, Fields<R> &f, const std::vector<R> &UI) {
     if (cf.sc.positivity)
         for (int d = 0; d < 3; d++)
             if (dims[d]) pp_limit(cf, f, UI, d);
+    if (cf.sc.viscous) viscous_lu(cf, f);
     lu_divergence(cf, f);
 }
 

@@ -19,7 +19,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
 import helpers as H  # noqa: E402
-from oracle.ref_runner import run_reference  # noqa: E402
+from oracle.ref_runner import read_transport, run_reference  # noqa: E402
 from xfluids_gb300 import cases  # noqa: E402
 from xfluids_gb300.abi import ROE, GLF, SYMMETRY  # noqa: E402
 
@@ -40,6 +40,13 @@ CASES = {
     "mixing5_12x8x6_janaf_cu6_roe": ("cop5_w6_roe_janaf",
                                      H.with_order(lambda: H.mixing_small((12, 8, 6), order=5, artificial=ROE), 6),
                                      (0.01, 0.01 * 8 / 12, 0.01 * 6 / 12)),
+    # viscous + heat conduction + diffusion (fourth order), fitted transport data of the reference
+    "visc_mixing5_12x8x6_janaf_w5": ("cop5_w5_llf_janaf_visc",
+                                     H.with_viscous(lambda: H.mixing_small((12, 8, 6), order=5)),
+                                     (0.01, 0.01 * 8 / 12, 0.01 * 6 / 12)),
+    "visc_mixing5_16x12_janaf_w5": ("cop5_w5_llf_janaf_visc",
+                                    H.with_viscous(lambda: H.mixing_small((16, 12, 0), order=5)),
+                                    (0.01, 0.01 * 12 / 16, 1.0)),
     # PositivityPreserving on: cases where the limiter acts (without it the first two go negative)
     "pp_riemann88_32_w5_llf": ("ncop_w5_llf_pp", H.with_positivity(lambda: H.riemann_member(88, 32)), None),
     "pp_riemann1d108_w5_llf": ("ncop_w5_llf_pp", H.with_positivity(H.riemann1d_strong), None),
@@ -59,7 +66,8 @@ def main(only=None):
         if only and name not in only:
             continue
         b, s, th, U, T = mk()
-        recs = run_reference(flav, b, U, T, steps=2, domain=domain)
+        tpath = os.path.join(HERE, ".transport.bin")
+        recs = run_reference(flav, b, U, T, steps=2, domain=domain, transport_out=tpath if s.viscous else None)
         E = s.Emax
         out = {
             "flavour": flav, "U0": U, "T0": T if T is not None else np.zeros(0),
@@ -74,6 +82,11 @@ def main(only=None):
             out["last_" + nm] = last[nm]
         if s.cop:
             out["species"] = np.array(cases.MIXING_SPECIES if s.num_species == 5 else ["H2", "O2", "AR", "N2"])
+        if s.viscous:  # the reference's fitted transport data, the input of the viscous fluxes
+            t = read_transport(tpath)
+            os.remove(tpath)
+            for k in ("visc", "therm", "dkj", "chara", "limits"):
+                out["tr_" + k] = t[k]
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **out)
         print(f"{path}: {len(recs)} stages, {os.path.getsize(path) / 1024:.0f} KB")

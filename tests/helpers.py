@@ -145,3 +145,19 @@ def with_order(mk, order):
         s.scheme_order = order
         return b, s, th, U, T
     return build
+
+
+def with_viscous(mk, flags=7):
+    def build():
+        b, s, th, U, T = mk()
+        s.viscous = flags
+        return b, s, th, U, T
+    return build
+
+
+def transport_of(z):
+    """xfg_transport from a fixture holding the reference's fitted transport data."""
+    if "tr_visc" not in z:
+        return None
+    ns = z["tr_chara"].size // 9
+    return thermo.transport_from_arrays(ns, z["tr_visc"], z["tr_therm"], z["tr_dkj"], z["tr_chara"], *z["tr_limits"])

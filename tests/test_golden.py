@@ -30,7 +30,7 @@ def load(path):
         setattr(s, k, v)
     th = H.thermal([str(x) for x in z["species"]], s.thermo) if s.cop else empty_thermal()
     T0 = z["T0"] if z["T0"].size else None
-    return z, b, s, th, z["U0"], T0
+    return z, b, s, th, z["U0"], T0, H.transport_of(z)
 
 
 def test_fixtures_present():
@@ -39,8 +39,8 @@ def test_fixtures_present():
 
 @pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[:-4] for f in FILES])
 def test_oracle_reproduces_reference_bitwise(path):
-    z, b, s, th, U0, T0 = load(path)
-    o = Oracle(b, s, th, U0, T0)
+    z, b, s, th, U0, T0, tr = load(path)
+    o = Oracle(b, s, th, U0, T0, transport=tr)
     o.initialize()
     E = s.Emax
     for q in range(len(z["dt"])):
@@ -61,9 +61,11 @@ def test_oracle_reproduces_reference_bitwise(path):
 @pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[:-4] for f in FILES])
 def test_cuda_matches_reference_fixture(path, precision, cuda_lib):
     from xfluids_gb300.fluid import Fluid
-    z, b, s, th, U0, T0 = load(path)
+    z, b, s, th, U0, T0, tr = load(path)
     s.precision = precision
     f = Fluid(b, s, th)
+    if tr is not None:
+        f.set_transport(tr)
     f.InitialU(U0, T0)
     f.initialize()
     E = s.Emax

@@ -78,12 +78,28 @@ class Scheme(C.Structure):
     _fields_ = [
         ("cop", C.c_int), ("num_species", C.c_int), ("scheme_order", C.c_int),
         ("artificial_type", C.c_int), ("thermo", C.c_int), ("ghost_species", C.c_int),
-        ("ncop_gamma", C.c_double), ("precision", C.c_int), ("positivity", C.c_int),
+        ("ncop_gamma", C.c_double), ("precision", C.c_int), ("positivity", C.c_int), ("viscous", C.c_int),
     ]
 
     @property
     def Emax(self) -> int:
         return self.num_species + 4 if self.cop else 5
+
+
+FIT_ORDER, SPCH = 4, 9
+VISC, VISC_HEAT, VISC_DIFFU = 1, 2, 4
+
+
+class Transport(C.Structure):
+    """xfg_transport: fitted transport coefficients and species characteristics."""
+    _fields_ = [
+        ("num_species", C.c_int),
+        ("visc", C.c_double * (MAX_SPECIES * FIT_ORDER)),
+        ("therm", C.c_double * (MAX_SPECIES * FIT_ORDER)),
+        ("dkj", C.c_double * (MAX_SPECIES * MAX_SPECIES * FIT_ORDER)),
+        ("species_chara", C.c_double * (MAX_SPECIES * SPCH)),
+        ("yil_limiter", C.c_double), ("dim_limiter", C.c_double),
+    ]
 
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -147,6 +163,7 @@ def lib():
         "xfg_ensemble_checkpoint_write": [P, I, C.c_char_p, C.c_float, P],
         "xfg_ensemble_add_checkpoint": [P, C.POINTER(Block), C.c_char_p, D, P, pi],
         "xfg_checkpoint_write": [P, C.c_char_p, I, D, C.c_float],
+        "xfg_set_transport": [P, C.POINTER(Transport)],
         "xfg_checkpoint_read": [P, C.c_char_p, pi, pd, C.POINTER(C.c_float)],
         "xfg_ensemble_get_option": [P, I, pi],
         "xfg_ensemble_active": [P],

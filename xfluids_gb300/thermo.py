@@ -108,3 +108,20 @@ def dump_tables(runtime_dir, sets, path):
         out[f"{'+'.join(species)}:{thermo}"] = read_tables(runtime_dir, species, thermo)
     with open(path, "w") as f:
         json.dump(out, f, indent=1)
+
+
+def transport_from_arrays(ns, visc, therm, dkj, chara, yil_limiter, dim_limiter):
+    """xfg_transport from the fitted coefficients (ns x 4, ns x 4, ns*ns x 4), the species
+    characteristics (ns x 9) and the two diffusion limiters."""
+    import numpy as np
+
+    from .abi import Transport
+    t = Transport()
+    t.num_species = int(ns)
+    for name, a in (("visc", visc), ("therm", therm), ("dkj", dkj), ("species_chara", chara)):
+        a = np.asarray(a, dtype=np.float64).reshape(-1)
+        dst = getattr(t, name)
+        for q, v in enumerate(a):
+            dst[q] = float(v)
+    t.yil_limiter, t.dim_limiter = float(yil_limiter), float(dim_limiter)
+    return t
