@@ -250,3 +250,85 @@ def test_mixed_single_gas_glf_and_primitives(cuda_lib):
         x, y = fmx.get(nm), f64.get(nm)
         assert np.abs(x - y).max() <= 1e-4 * np.abs(y).max(), nm
     f64.close(), fmx.close()
+
+
+def _visc_case(name):
+    """A viscous case and the reference's fitted transport data (from its golden fixture)."""
+    import os
+    z = np.load(os.path.join(H.GOLDEN, "visc_mixing5_12x8x6_janaf_w5.npz"))
+    tr = H.transport_of(z)
+    mk = {"visc3d": lambda: H.mixing_small((16, 12, 8), order=5),
+          "visc2d_weno7": lambda: H.mixing_small((24, 16, 0), order=7),
+          "visc3d_heat_only": lambda: H.mixing_small((12, 8, 6), order=5)}[name]
+    b, s, th, U, T = mk()
+    s.viscous = 3 if name == "visc3d_heat_only" else 7
+    return b, s, th, U, T, tr
+
+
+@pytest.mark.parametrize("precision", [FP64, FP64_STRICT], ids=["fp64", "strict"])
+@pytest.mark.parametrize("name", ["visc3d", "visc2d_weno7", "visc3d_heat_only"])
+def test_viscous_stagewise_parity(name, precision, cuda_lib):
+    """Viscous stress and heat conduction (and the diffusion terms, zero in a single block) agree
+    with the oracle per stage; exp / log / pow differ from the host's by an ulp, so the bound is
+    the parity bound, not bit equality."""
+    from xfluids_gb300.fluid import Fluid
+    b, s, th, U, T, tr = _visc_case(name)
+    s.precision = precision
+    f = Fluid(b, s, th)
+    f.set_transport(tr)
+    f.InitialU(U, T)
+    o = Oracle(b, s, th, U, T, transport=tr)
+    f.initialize(), o.initialize()
+    E = s.Emax
+    for step in range(2):
+        dt_g, dt_o = f.GetFluidDt(), o.get_dt()
+        assert abs(dt_g - dt_o) <= 1e-12 * dt_o
+        for flag in (1, 2, 3):
+            f.stage(flag, dt_o)
+            o.stage(flag, dt_o)
+            _compare_stage(b, f, o, E, f"{name} step {step} stage {flag}", True)
+    # the fused step and the graph replay of the same run
+    g = Fluid(b, s, th)
+    g.set_transport(tr)
+    g.InitialU(U, T)
+    g.initialize()
+    st, t, n = g.advance(2)
+    assert st == 0 and n == 2
+    _check("graph U", H.inner_aos(b, g.get("U"), E), H.inner_aos(b, o.get("U"), E), E)
+    f.close(), g.close()
+
+
+def test_viscous_needs_transport_and_a_mixture(cuda_lib):
+    from xfluids_gb300.abi import XfgError
+    from xfluids_gb300.fluid import Fluid
+    b, s, th, U, T, tr = _visc_case("visc3d")
+    f = Fluid(b, s, th)
+    f.InitialU(U, T)
+    f.initialize()
+    with pytest.raises(XfgError):
+        f.advance(1)                      # no transport data yet
+    f.close()
+    b2, s2, th2, U2, T2 = H.sod_like(64)
+    s2.viscous = 1
+    with pytest.raises(XfgError):
+        Fluid(b2, s2, th2)                # single gas: no temperature for the transport fits
+
+
+def test_mixed_viscous_close_to_fp64(cuda_lib):
+    from xfluids_gb300.fluid import Fluid
+    b, s, th, U, T, tr = _visc_case("visc3d")
+    runs = {}
+    for prec in (FP64, MIXED):
+        s.precision = prec
+        f = Fluid(b, s, th)
+        f.set_transport(tr)
+        f.InitialU(U, T)
+        f.initialize()
+        st, t, n = f.advance(3)
+        assert st == 0
+        runs[prec] = H.inner_aos(b, f.get("U"), 9)
+        f.close()
+    a, r = runs[MIXED], runs[FP64]
+    num, den = np.abs(a - r).mean(axis=0), np.abs(r).mean(axis=0)
+    rel = np.where(den > 0, num / np.where(den > 0, den, 1.0), num)
+    assert np.all(rel < 1e-4), rel

@@ -110,6 +110,7 @@ struct xfg_handle {
     int *host_err = nullptr;          // pinned mirror of err
     double t = 0.0;
     bool states_ready = false;
+    bool transport_ready = false;     // viscous schemes: xfg_set_transport called
     cudaGraphExec_t graph = nullptr;  // one fused step, replayed by xfg_advance
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
@@ -123,6 +124,10 @@ static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *
     if (s->artificial_type < 1 || s->artificial_type > 3) return fail(-1, "artificial_type must be 1..3");
     if (s->precision < 0 || s->precision > 2) return fail(-1, "precision must be 0 (fp64), 1 (mixed) or 2 (fp64 strict)");
     if (s->positivity != 0 && s->positivity != 1) return fail(-1, "positivity must be 0 or 1");
+    if (s->viscous < 0 || s->viscous > 7) return fail(-1, "viscous must be Visc | Visc_Heat << 1 | Visc_Diffu << 2");
+    if (s->viscous && !(s->viscous & 1)) return fail(-1, "Visc_Heat / Visc_Diffu need Visc (bit 0)");
+    if (s->viscous && !s->cop)
+        return fail(-1, "viscous fluxes need a mixture (cop = 1): the single-gas states compute no temperature");
     if (s->cop && (s->num_species < 2 || s->num_species > XFG_MAX_SPECIES))
         return fail(-1, "num_species %d out of range for COP", s->num_species);
     if (!s->cop && s->num_species != 1) return fail(-1, "num_species must be 1 without COP");
@@ -191,6 +196,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     // layout of the pool
     size_t nd = 3 * E + 12 + (scheme->cop ? NS : 0);           // U, U1, LU, primitives, y
     if (scheme->cop) nd += 3 + (NS - 1);                        // per-cell sound-speed terms
+    if (scheme->viscous) nd += 9 + 2;                           // velocity derivatives, mu, kappa
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;  // single-gas fast path extras
     if (fast1) nd += 2 + 3 * (block->DimX + block->DimY + block->DimZ);
     for (int d = 0; d < 3; d++)
@@ -202,7 +208,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
             if (dims[d]) nf += 2 * E;                             // Ff, Fwf
     }
     const size_t stage_elems = (size_t)h->N * (E > NS ? E : NS);
-    const size_t small = 4096;
+    const size_t small = 8192;                                  // small words; transport table at +4096
     size_t bytes = nd * arr8 + nf * arr4 + align_up(stage_elems * 8, 256) + small;
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->pool, bytes);
@@ -222,6 +228,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     f.rho = take8(1), f.u = take8(1), f.v = take8(1), f.w = take8(1), f.p = take8(1), f.H = take8(1);
     f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
     if (scheme->cop) f.y = take8(NS), f.xc = take8(3 + (NS - 1));
+    if (scheme->viscous) f.vde = take8(9), f.mu = take8(1), f.kappa = take8(1);
     if (fast1) {
         f.sr = take8(1), f.isr = take8(1);
         for (int d = 0; d < 3; d++)
@@ -241,6 +248,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     h->glf = (unsigned long long *)(p + 64);      // 9 x u64
     f.dtbuf = (double *)(p + 256);                // 8 doubles
     f.err = (int *)(p + 512);                     // 8 ints (+ NaN estimate scratch after)
+    if (scheme->viscous) f.tr = (const double *)(p + 4096);  // transport table (xfg_set_transport)
     // launch context
     Geo &g = h->ctx.g;
     g.Xmax = block->Xmax, g.Ymax = block->Ymax, g.Zmax = block->Zmax;
@@ -264,6 +272,8 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     h->ctx.glf = scheme->artificial_type == XFG_GLF ? (const double *)h->glf : nullptr;
     h->ctx.precision = scheme->precision;
     h->ctx.cfl = block->CFLnumber;
+    h->ctx.viscous = scheme->viscous;
+    for (int q = 0; q < 6; q++) g.bc[q] = block->Boundarys[q];
     e = cudaMallocHost(&h->host_dtbuf, 8 * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&h->host_err, 64 * sizeof(int));
     for (int q = 0; q < 4 && e == cudaSuccess; q++) e = cudaEventCreate(&h->ev[q]);
@@ -305,6 +315,38 @@ int xfg_set_state(xfg_handle *h, const double *U_aos, const double *T) {
     CK(cudaMemsetAsync(h->ctx.f.err, 0, 64 * sizeof(int), h->st));
     CK(cudaStreamSynchronize(h->st));
     h->states_ready = false;
+    return 0;
+}
+
+// Device transport table of a viscous handle: the fitted ln(mu) and ln(kappa) cubics, the two
+// species-pair factors of PHI (Visc_device.h:30-38) that depend on the molar masses only,
+// (W_i/W_k)^0.25 and (1 + W_k/W_i)^-0.5, computed here once, and the species ids (SID).
+int xfg_set_transport(xfg_handle *h, const xfg_transport *tr) {
+    if (!h || !tr) return fail(-1, "null argument");
+    if (!h->sc.viscous) return fail(-1, "the scheme has no viscous fluxes (xfg_scheme.viscous = 0)");
+    const int ns = h->NS;
+    if (tr->num_species != ns) return fail(-1, "transport data for %d species, the scheme has %d", tr->num_species, ns);
+    std::vector<double> t(8 * ns + 2 * ns * ns + ns);
+    for (int k = 0; k < ns; k++)
+        for (int q = 0; q < XFG_FIT_ORDER; q++) {
+            t[4 * k + q] = tr->visc[k * XFG_FIT_ORDER + q];
+            t[4 * ns + 4 * k + q] = tr->therm[k * XFG_FIT_ORDER + q];
+        }
+    for (int k = 0; k < ns; k++)
+        for (int i = 0; i < ns; i++) {
+            const double Wk = tr->species_chara[k * XFG_SPCH + 6], Wi = tr->species_chara[i * XFG_SPCH + 6];
+            t[8 * ns + k * ns + i] = std::pow(Wi / Wk, 0.25);
+            t[8 * ns + ns * ns + k * ns + i] = std::pow(1.0 + Wk / Wi, -0.5);
+        }
+    for (int k = 0; k < ns; k++) {
+        const double sid = tr->species_chara[k * XFG_SPCH + 8];
+        if (!(sid >= 0.0 && sid < ns)) return fail(-1, "species id %g out of range", sid);
+        t[8 * ns + 2 * ns * ns + k] = sid;
+    }
+    CK(cudaSetDevice(h->device));
+    CK(cudaMemcpyAsync((void *)h->ctx.f.tr, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    h->transport_ready = true;
     return 0;
 }
 
@@ -430,10 +472,12 @@ static void launch_lu(xfg_handle *h, double *UI, int guard) {
     if (h->sc.positivity)  // after all sweeps, ConVenction_block.hpp:328-410; lambda_0 in dtbuf[5..7]
         for (int d = 0; d < 3; d++)
             if (dims[d]) h->ops->pp(h->ctx, d, UI, h->ctx.f.dtbuf + 5, guard);
+    if (h->sc.viscous) h->ops->visc(h->ctx, guard);  // ConVenction_block.hpp:419-566
 }
 
 int xfg_compute_lu(xfg_handle *h, int flag, float *timers23) {
     if (!h) return fail(-1, "null handle");
+    if (h->sc.viscous && !h->transport_ready) return fail(-1, "viscous scheme: call xfg_set_transport first");
     CK(cudaSetDevice(h->device));
     CK(cudaEventRecord(h->ev[0], h->st));
     launch_lu(h, stage_U(h, flag), 0);
@@ -531,6 +575,7 @@ static int finish(xfg_handle *h, double *t, double *dt, int *steps) {
 int xfg_step(xfg_handle *h, double target_t, double *t, double *dt) {
     if (!h) return fail(-1, "null handle");
     if (!h->states_ready) return fail(-1, "xfg_step needs a preceding xfg_update_states (main.cpp:45-47)");
+    if (h->sc.viscous && !h->transport_ready) return fail(-1, "viscous scheme: call xfg_set_transport first");
     CK(cudaSetDevice(h->device));
     k_set_time<<<1, 1, 0, h->st>>>(h->ctx.f.dtbuf, h->t, target_t);
     launch_step(h);
@@ -551,6 +596,7 @@ int xfg_advance_timed(xfg_handle *h, int nsteps, double target_t, double *t, int
 static int advance_impl(xfg_handle *h, int nsteps, double target_t, double *t, int *steps_done, float *device_ms) {
     if (!h) return fail(-1, "null handle");
     if (!h->states_ready) return fail(-1, "xfg_advance needs a preceding xfg_update_states (main.cpp:45-47)");
+    if (h->sc.viscous && !h->transport_ready) return fail(-1, "viscous scheme: call xfg_set_transport first");
     CK(cudaSetDevice(h->device));
     k_set_time<<<1, 1, 0, h->st>>>(h->ctx.f.dtbuf, h->t, target_t);
     CK(cudaGetLastError());
@@ -596,6 +642,7 @@ int xfg_launches_per_step(xfg_handle *h, int *n) {
 int xfg_time_phases(xfg_handle *h, double target_t, float *ms_out) {
     if (!h || !ms_out) return fail(-1, "null argument");
     if (!h->states_ready) return fail(-1, "xfg_time_phases needs a preceding xfg_update_states");
+    if (h->sc.viscous && !h->transport_ready) return fail(-1, "viscous scheme: call xfg_set_transport first");
     CK(cudaSetDevice(h->device));
     DevFields &f = h->ctx.f;
     const int dims[3] = {h->bl.DimX, h->bl.DimY, h->bl.DimZ};

@@ -57,6 +57,7 @@ struct Geo {
     double _dx, _dy, _dz;
     long long pitch;  // elements between components of a SoA array
     double dx, dy, dz;  // cell sizes (the WENO-CU6 epsilon)
+    int bc[6];          // boundary kinds (the ghost layers of the viscous derivatives)
     __host__ __device__ long long ncell() const { return (long long)Xmax * Ymax * Zmax; }
 };
 
@@ -72,6 +73,9 @@ struct DevFields {
     float *Fwf[3];             // FP32 face fluxes (mixed form)
     double *sr, *isr;          // sqrt(rho) and 1/sqrt(rho) per cell (single-gas FP64 fast path)
     double *eab[3];            // |u_d - c|, |u_d|, |u_d + c| per cell and direction (same path)
+    double *vde;               // viscous: the 9 cell-centre velocity derivatives (ducx..dwcz)
+    double *mu, *kappa;        // viscous: mixture viscosity and thermal conductivity per cell
+    const double *tr;          // viscous: device transport table (see xfg_api.cu, pack_transport)
     double *xc;                // mixtures: per-cell terms of the interface sound speed (3 + NCOP
                                // components, see cop_cell_terms); null = the faces compute them
     unsigned long long *lam;   // dt wave-speed maxima (3 x bit patterns of non-negative doubles)

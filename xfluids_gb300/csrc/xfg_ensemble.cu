@@ -418,6 +418,7 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
         return efail(-1, "ensemble precision must be XFG_FP64 or XFG_MIXED%s");
     if (scheme->artificial_type == XFG_GLF) return efail(-1, "the ensemble engine supports Roe and LLF splitting%s");
     if (scheme->positivity) return efail(-1, "the ensemble engine has no positivity limiter%s");
+    if (scheme->viscous) return efail(-1, "the ensemble engine serves inviscid single-gas members%s");
     if (scheme->scheme_order != 5 && scheme->scheme_order != 7) return efail(-1, "scheme_order must be 5 or 7%s");
     ECK(cudaSetDevice(device));
     xfg_ensemble *e = new xfg_ensemble();

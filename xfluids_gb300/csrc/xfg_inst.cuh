@@ -10,6 +10,7 @@
 #include "xfg_kernels.cuh"
 #include "xfg_mixed.cuh"
 #include "xfg_ops.h"
+#include "xfg_viscous.cuh"
 
 namespace xfg {
 namespace XFG_KNS {
@@ -97,13 +98,37 @@ struct Inst {
         else pp_d<2>(c, UI, lam0, guard);
     }
 
+    static void visc(const LaunchCtx &c, int guard) {
+        if constexpr (COP) {
+            const Geo &g = c.g;
+            const int heat = (c.viscous & 2) ? 1 : 0;
+            const long long nd = (long long)(g.dimx ? g.Xi + 4 : 1) * (g.dimy ? g.Yi + 4 : 1) * (g.dimz ? g.Zi + 4 : 1);
+            k_vderiv<<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
+            if (g.dimx) k_vderiv_bc<0><<<grid_for((long long)g.Bx * g.Ymax * g.Zmax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
+            if (g.dimy) k_vderiv_bc<1><<<grid_for((long long)g.By * g.Xmax * g.Zmax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
+            if (g.dimz) k_vderiv_bc<2><<<grid_for((long long)g.Bz * g.Xmax * g.Ymax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
+            k_transport<NS><<<grid_for(g.ncell(), kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, heat, guard);
+            const long long nf[3] = {(long long)(g.Xi + 1) * g.Yi * g.Zi, (long long)g.Xi * (g.Yi + 1) * g.Zi,
+                                     (long long)g.Xi * g.Yi * (g.Zi + 1)};
+            if (MIXED) {
+                if (g.dimx) k_visc<0, E, float><<<grid_for(nf[0], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fwf[0], heat, guard);
+                if (g.dimy) k_visc<1, E, float><<<grid_for(nf[1], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fwf[1], heat, guard);
+                if (g.dimz) k_visc<2, E, float><<<grid_for(nf[2], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fwf[2], heat, guard);
+            } else {
+                if (g.dimx) k_visc<0, E, double><<<grid_for(nf[0], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fw[0], heat, guard);
+                if (g.dimy) k_visc<1, E, double><<<grid_for(nf[1], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fw[1], heat, guard);
+                if (g.dimz) k_visc<2, E, double><<<grid_for(nf[2], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fw[2], heat, guard);
+            }
+        }
+    }
+
     // tables for scheme orders 5 (WENO5-JS), 6 (WENO-CU6) and 7 (WENO7), registered under
     // precision id `prec`
     static const Ops *table(int order, int prec) {
         static Ops t[3][3];
         Ops &o = t[order - 5][prec];
         o = Ops{COP ? 1 : 0, NS, order, prec, bc, states, order == 7 ? faces<7> : (order == 6 ? faces<6> : faces<5>),
-                div_rk, glf, rk, estimate_nan, pp};
+                div_rk, glf, rk, estimate_nan, pp, visc};
         return &o;
     }
 };

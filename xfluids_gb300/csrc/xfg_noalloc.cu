@@ -76,6 +76,7 @@ extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *
     if (scheme->scheme_order < 5 || scheme->scheme_order > 7) return fail(-1, "scheme_order must be 5, 6 or 7");
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_FP64_STRICT)
         return fail(-1, "xfg_compute_lu_noalloc serves the FP64 forms (precision 0 or 2)");
+    if (scheme->viscous) return fail(-1, "xfg_compute_lu_noalloc has no viscous fluxes (they need transport data)");
     if (scheme->positivity)
         return fail(-1, "xfg_compute_lu_noalloc has no positivity limiter (it needs the step's GetDt maxima)");
     if (scheme->cop && !T) return fail(-1, "a mixture needs the temperature T (Newton warm start)");

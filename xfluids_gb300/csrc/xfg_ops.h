@@ -22,6 +22,7 @@ struct LaunchCtx {
     const double *glf;                 // GLF maxima per direction (9 doubles) or nullptr
     int precision;                     // xfg_precision
     double cfl;                        // CFLnumber (positivity limiter)
+    int viscous;                       // xfg_scheme.viscous
 };
 
 struct Ops {
@@ -35,6 +36,7 @@ struct Ops {
     void (*rk)(const LaunchCtx &, int flag, double dt);
     void (*estimate_nan)(const LaunchCtx &, const double *UI, int *pos);
     void (*pp)(const LaunchCtx &, int d, const double *UI, const double *lam0, int guard);
+    void (*visc)(const LaunchCtx &, int guard);   // viscous and heat-conduction fluxes (mixtures)
 };
 
 // Message returned by xfg_last_error() on this host thread.

@@ -55,6 +55,10 @@ class Fluid:
 
     set_state = InitialU
 
+    def set_transport(self, transport):
+        """Fitted transport data of a viscous scheme (xfg_transport, thermo.transport_from_arrays)."""
+        check(lib().xfg_set_transport(self._h, C.byref(transport)))
+
     # -- checkpoints (XFLUIDS::Output_Ubak / Read_Ubak, src/XFLUIDS.cpp:658-724) -------------------
     def write_checkpoint(self, path: str, step: int, time: float, duration: float = 0.0):
         check(lib().xfg_checkpoint_write(self._h, str(path).encode(), int(step), float(time), float(duration)))
