@@ -28,6 +28,9 @@ import numpy as np  # noqa: E402
 # DRAM bytes per face of the FP64 x-face kernel measured by ncu on a small case, scaled per face
 # (profiles/k_faces_fp64_vortex.md); None until a capture exists.
 THERMO_JSON = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "thermo_tables.json")
+# fitted transport coefficients of H2/O2/N2/H2O/AR (the reference's viscfit output, kept in a fixture)
+TRANSPORT_NPZ = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                             "visc_mixing5_12x8x6_janaf_w5.npz")
 # DRAM bytes per face of the FP64 x-face kernel: 674.2 MB read + 152.8 MB written in one ncu
 # capture of the 2048^2 vortex (4.196 M faces); traffic grows with the faces of a launch
 NCU_FACE_BYTES_FP64 = (674.218496e6 + 152.813568e6) / (2049 * 2048)
@@ -272,16 +275,21 @@ def bench_mixing_layer(args, local, steps):
     """3D inert temporal mixing layer (512 x 256 x 256, 5 species H2/O2/N2/H2O/AR, 7-coefficient
     thermo of the reference's runtime.dat, WENO7 LLF), FP64 and mixed from the same state: one
     warm-up step (graph capture), a reset, then `steps` timed steps; relative L1 / Linf of the
-    mixed state against the FP64 state at the same step count."""
+    mixed state against the FP64 state at the same step count. The same runs with viscous stress,
+    heat conduction and species diffusion (the reference's fitted transport data) give the share of
+    a step those terms add."""
     from xfluids_gb300 import thermo
     from xfluids_gb300.abi import MIXED
     from xfluids_gb300.fluid import Fluid
     th = thermo.load_thermal(cases_mod().MIXING_SPECIES, 0, tables_json=THERMO_JSON)
     b, s, th, U, T = cases_mod().mixing_layer((512, 256, 256), thermal=th)
     res, states = {}, {}
-    for prec in (0, MIXED):
-        s.precision = prec
+    tr = thermo.load_transport(TRANSPORT_NPZ)
+    for prec, visc in ((0, 0), (MIXED, 0), (0, 7), (MIXED, 7)):
+        s.precision, s.viscous = prec, visc
         f = Fluid(b, s, th, device=local)
+        if visc:
+            f.set_transport(tr)
         f.InitialU(U, T)
         f.initialize()
         f.advance(1)
@@ -290,10 +298,14 @@ def bench_mixing_layer(args, local, steps):
         f.time = 0.0
         st, t, k, ms = f.advance_timed(steps)
         cells = b.X_inner * b.Y_inner * b.Z_inner
-        res["fp64" if prec == 0 else "mixed"] = {"value": cells * k / (ms * 1e-3), "ms_per_step": ms / k,
-                                                 "steps": k, "status": st, "t": t}
-        states[prec] = f.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 9)[b.inner_slices()].reshape(-1, 9)
+        key = ("fp64" if prec == 0 else "mixed") + ("_viscous" if visc else "")
+        res[key] = {"value": cells * k / (ms * 1e-3), "ms_per_step": ms / k, "steps": k, "status": st, "t": t}
+        if not visc:
+            states[prec] = f.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 9)[b.inner_slices()].reshape(-1, 9)
         f.close()
+    s.viscous = 0
+    for p in ("fp64", "mixed"):  # share of a step the viscous, heat and diffusion terms add
+        res[p + "_viscous"]["viscous_share_of_step"] = 1.0 - res[p]["ms_per_step"] / res[p + "_viscous"]["ms_per_step"]
     d = np.abs(states[MIXED] - states[0])
     scale = np.abs(states[0]).mean(axis=0)
     live = scale > 0  # the H2O density is zero in this mixing layer (no reaction)

@@ -83,24 +83,30 @@ done
 # shows that the boundary compiles and links against the unmodified reference headers.
 LIBDIR=$(cd "$HERE/../.." && pwd)/xfluids_gb300/_build
 if [ -f "$LIBDIR/libxfluids_gb300.so" ] && { [ ${#want[@]} -eq 0 ] || [[ " ${want[*]} " =~ " dropin " ]]; }; then
-  base="$OUT/ncop_w5_llf"
-  d="$OUT/dropin_ncop_w5_llf"
-  mkdir -p "$d"
-  IFS='|' read -r name macros sample mixture <<< "${FLAVOURS[0]}"
-  dflags=(-std=c++17 -O2 -U_FORTIFY_SOURCE -ffp-contract=off -w -include cstdint -include memory -include cstring
-          -D__ACPP__ -DUSE_DOUBLE -DEIGEN_ALLOC=0 -DESTIM_NAN=1 -DESTIM_OUT=0 -D__SYNC_TIMER_=1 -DPOSP=0
-          -DCOP_CHEME=0 -DNUM_REA=1 -DVisc=0 $macros
-          "-DINI_SAMPLE=\"ini-dropin\"" "-DRFile=\"/$mixture\"" "-DIniFile=\"$d/case.json\"" "-DRPath=\"/runtime.dat\""
-          -I"$HERE/shim" -I"$REF/src" -I"$REF/src/include" -I"$REF/external" -I"$REF/$mixture"
-          -I"$REF/src/solver_Ini/sample/$sample" -I"$REF/src/solver_Reconstruction/viscosity/Fourth_Order"
-          -I"$REF/src/solver_Reconstruction/FDM_Method" -I"$REF/src/solver_Reconstruction/FDM_Method/positive-definite_eigen"
-          -I"$REF/src/solver_Reconstruction" -I"$HERE/../../include")
-  g++ "${dflags[@]}" -c "$HERE/../../xfluids_gb300/host/Fluids_gb300.cpp" -o "$d/Fluids_gb300.o"
-  g++ "${dflags[@]}" -c "$REF/src/main.cpp" -o "$d/main.o"
-  objs=()
-  for o in "$base"/obj/*.o; do
-    case "$(basename "$o")" in src_Fluids.cpp.o|ref_driver.o) ;; *) objs+=("$o") ;; esac
+  # a single gas and the viscous 5-species mixture (Visc, Visc_Heat, Visc_Diffu: xfg_set_transport)
+  for fl in "${FLAVOURS[@]}"; do
+    IFS='|' read -r name macros sample mixture <<< "$fl"
+    case "$name" in ncop_w5_llf|cop5_w5_llf_janaf_visc) ;; *) continue ;; esac
+    base="$OUT/$name"
+    d="$OUT/dropin_$name"
+    [ -d "$base/obj" ] || continue
+    mkdir -p "$d"
+    if [[ "$mixture" == runtime.dat/* ]]; then mixinc="$REF/$mixture"; else mixinc="$OUT/$mixture"; fi
+    dflags=(-std=c++17 -O2 -U_FORTIFY_SOURCE -ffp-contract=off -w -include cstdint -include memory -include cstring
+            -D__ACPP__ -DUSE_DOUBLE -DEIGEN_ALLOC=0 -DESTIM_NAN=1 -DESTIM_OUT=0 -D__SYNC_TIMER_=1 -DPOSP=0
+            -DCOP_CHEME=0 -DNUM_REA=1 -DVisc=0 $macros
+            "-DINI_SAMPLE=\"ini-dropin\"" "-DRFile=\"/$mixture\"" "-DIniFile=\"$d/case.json\"" "-DRPath=\"/runtime.dat\""
+            -I"$HERE/shim" -I"$REF/src" -I"$REF/src/include" -I"$REF/external" -I"$mixinc"
+            -I"$REF/src/solver_Ini/sample/$sample" -I"$REF/src/solver_Reconstruction/viscosity/Fourth_Order"
+            -I"$REF/src/solver_Reconstruction/FDM_Method" -I"$REF/src/solver_Reconstruction/FDM_Method/positive-definite_eigen"
+            -I"$REF/src/solver_Reconstruction" -I"$HERE/../../include")
+    g++ "${dflags[@]}" -c "$HERE/../../xfluids_gb300/host/Fluids_gb300.cpp" -o "$d/Fluids_gb300.o"
+    g++ "${dflags[@]}" -c "$REF/src/main.cpp" -o "$d/main.o"
+    objs=()
+    for o in "$base"/obj/*.o; do
+      case "$(basename "$o")" in src_Fluids.cpp.o|ref_driver.o) ;; *) objs+=("$o") ;; esac
+    done
+    g++ -o "$d/xfluids_gb300_dropin" "$d/Fluids_gb300.o" "$d/main.o" "${objs[@]}" -L"$LIBDIR" -lxfluids_gb300 -Wl,-rpath,"$LIBDIR"
+    echo "built $d/xfluids_gb300_dropin"
   done
-  g++ -o "$d/xfluids_gb300_dropin" "$d/Fluids_gb300.o" "$d/main.o" "${objs[@]}" -L"$LIBDIR" -lxfluids_gb300 -Wl,-rpath,"$LIBDIR"
-  echo "built $d/xfluids_gb300_dropin"
 fi

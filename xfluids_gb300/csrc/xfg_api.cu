@@ -248,7 +248,10 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     h->glf = (unsigned long long *)(p + 64);      // 9 x u64
     f.dtbuf = (double *)(p + 256);                // 8 doubles
     f.err = (int *)(p + 512);                     // 8 ints (+ NaN estimate scratch after)
-    if (scheme->viscous) f.tr = (const double *)(p + 4096);  // transport table (xfg_set_transport)
+    if (scheme->viscous) {  // transport tables (xfg_set_transport): FP64 at +4096, FP32 at +6144
+        f.tr = (const double *)(p + 4096);
+        f.trf = (const float *)(p + 6144);
+    }
     // launch context
     Geo &g = h->ctx.g;
     g.Xmax = block->Xmax, g.Ymax = block->Ymax, g.Zmax = block->Zmax;
@@ -343,7 +346,22 @@ int xfg_set_transport(xfg_handle *h, const xfg_transport *tr) {
         if (!(sid >= 0.0 && sid < ns)) return fail(-1, "species id %g out of range", sid);
         t[8 * ns + 2 * ns * ns + k] = sid;
     }
+    // FP32 table of the mixed form, species already resolved through SID: visc[4*ns], therm[4*ns],
+    // wa[ns*ns], wb[ns*ns] * 0.5 / sqrt(2)
+    std::vector<float> tf(8 * ns + 2 * ns * ns);
+    for (int k = 0; k < ns; k++) {
+        const int ik = (int)t[8 * ns + 2 * ns * ns + k];
+        for (int q = 0; q < XFG_FIT_ORDER; q++) {
+            tf[4 * k + q] = (float)t[4 * ik + q];
+            tf[4 * ns + 4 * k + q] = (float)t[4 * ns + 4 * ik + q];
+        }
+        for (int i = 0; i < ns; i++) {
+            tf[8 * ns + k * ns + i] = (float)t[8 * ns + k * ns + i];
+            tf[8 * ns + ns * ns + k * ns + i] = (float)(t[8 * ns + ns * ns + k * ns + i] * 0.5 / std::sqrt(2.0));
+        }
+    }
     CK(cudaSetDevice(h->device));
+    CK(cudaMemcpyAsync((void *)h->ctx.f.trf, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync((void *)h->ctx.f.tr, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
     CK(cudaStreamSynchronize(h->st));
     h->transport_ready = true;

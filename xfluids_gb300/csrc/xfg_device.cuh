@@ -76,6 +76,7 @@ struct DevFields {
     double *vde;               // viscous: the 9 cell-centre velocity derivatives (ducx..dwcz)
     double *mu, *kappa;        // viscous: mixture viscosity and thermal conductivity per cell
     const double *tr;          // viscous: device transport table (see xfg_api.cu, pack_transport)
+    const float *trf;          // viscous, mixed form: FP32 transport table (xfg_set_transport)
     double *xc;                // mixtures: per-cell terms of the interface sound speed (3 + NCOP
                                // components, see cop_cell_terms); null = the faces compute them
     unsigned long long *lam;   // dt wave-speed maxima (3 x bit patterns of non-negative doubles)

@@ -107,7 +107,10 @@ struct Inst {
             if (g.dimx) k_vderiv_bc<0><<<grid_for((long long)g.Bx * g.Ymax * g.Zmax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
             if (g.dimy) k_vderiv_bc<1><<<grid_for((long long)g.By * g.Xmax * g.Zmax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
             if (g.dimz) k_vderiv_bc<2><<<grid_for((long long)g.Bz * g.Xmax * g.Ymax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
-            k_transport<NS><<<grid_for(g.ncell(), kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, heat, guard);
+            if (MIXED)
+                k_transport_f32<NS><<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, heat, guard);
+            else
+                k_transport<NS><<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, heat, guard);
             const long long nf[3] = {(long long)(g.Xi + 1) * g.Yi * g.Zi, (long long)g.Xi * (g.Yi + 1) * g.Zi,
                                      (long long)g.Xi * g.Yi * (g.Zi + 1)};
             if (MIXED) {

@@ -27,13 +27,6 @@ struct TrView {
         : visc(t), therm(t + 4 * ns), wa(t + 8 * ns), wb(t + 8 * ns + ns * ns), sid(t + 8 * ns + 2 * ns * ns) {}
 };
 
-__device__ __forceinline__ double vfit_exp(const double *c, double T) {  // Viscosity / Thermal_conductivity
-    double v = c[3];
-#pragma unroll
-    for (int i = 2; i >= 0; i--) v = v * log(T) + c[i];
-    return exp(v);
-}
-
 // one thread per cell of [B-2, inner+B+2) in every active direction
 static __global__ void __launch_bounds__(kThreads) k_vderiv(Geo g, DevFields f, int guard) {
     if (guard && step_done(f)) return;
@@ -119,16 +112,25 @@ __global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, int 
     }
 }
 
-// mixture viscosity (Wilke) and thermal conductivity on every cell
+// mixture viscosity (Wilke) and thermal conductivity on the cells k_visc reads: [B-2, inner+B+2)
+// in every active direction. Per cell one ln T, NS viscosity fits, and the Wilke weights
+// PHI_ki = W_ki^a (mu_k / mu_i)^(1/2) ... (Visc_device.h:30-38) with (mu_k / mu_i)^(1/2) formed as
+// sqrt(mu_k) * (1 / sqrt(mu_i)): NS square roots and reciprocals instead of NS^2 pow calls, a
+// difference of a few ulp (the fits themselves go through exp and log).
 template <int NS>
 __global__ void __launch_bounds__(kThreads) k_transport(Geo g, DevFields f, DevThermo th, int heat, int guard) {
     if (guard && step_done(f)) return;
-    const long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= g.ncell()) return;
-    const long long P = g.pitch;
+    const int nx = g.dimx ? g.Xi + 4 : 1, ny = g.dimy ? g.Yi + 4 : 1, nz = g.dimz ? g.Zi + 4 : 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nx * ny * nz) return;
+    const int i0 = (int)(t % nx) + (g.dimx ? g.Bx - 2 : 0);
+    const long long r = t / nx;
+    const int j0 = (int)(r % ny) + (g.dimy ? g.By - 2 : 0), k0 = (int)(r / ny) + (g.dimz ? g.Bz - 2 : 0);
+    const long long P = g.pitch, id = (long long)g.Xmax * g.Ymax * k0 + (long long)g.Xmax * j0 + i0;
     const TrView tv(f.tr, NS);
     const double T = f.T[id], rho = f.rho[id];
-    double X[NS], mk[NS];
+    const double lT = log(T);
+    double X[NS], mk[NS], sq[NS], isq[NS];
     double C_total = 0.0;
 #pragma unroll
     for (int i = 0; i < NS; i++) {
@@ -139,25 +141,86 @@ __global__ void __launch_bounds__(kThreads) k_transport(Geo g, DevFields f, DevT
 #pragma unroll
     for (int i = 0; i < NS; i++) X[i] = X[i] * _C;
 #pragma unroll
-    for (int k = 0; k < NS; k++) mk[k] = vfit_exp(tv.visc + 4 * (int)tv.sid[k], T);
+    for (int k = 0; k < NS; k++) {
+        const double *c = tv.visc + 4 * (int)tv.sid[k];
+        mk[k] = exp(((c[3] * lT + c[2]) * lT + c[1]) * lT + c[0]);
+        sq[k] = sqrt(mk[k]);
+        isq[k] = 1.0 / sq[k];
+    }
     const double s2 = sqrt(2.0);
     double mu = 0.0, kap = 0.0;
 #pragma unroll
     for (int k = 0; k < NS; k++) {
         double den = 0.0;
 #pragma unroll
-        for (int i = 0; i < NS; i++) {  // PHI (Visc_device.h:30-38)
-            double phi = tv.wa[k * NS + i] * pow(mk[k] / mk[i], 0.5);
+        for (int i = 0; i < NS; i++) {
+            double phi = tv.wa[k * NS + i] * (sq[k] * isq[i]);
             phi = (phi + 1.0) * (phi + 1.0) * 0.5 / s2;
             phi = phi * tv.wb[k * NS + i];
             den = den + X[i] * phi;
         }
         const double _den = 1.0 / den;
         mu = mu + X[k] * mk[k] * _den;
-        if (heat) kap = kap + X[k] * vfit_exp(tv.therm + 4 * (int)tv.sid[k], T) * _den;
+        if (heat) {
+            const double *c = tv.therm + 4 * (int)tv.sid[k];
+            kap = kap + X[k] * exp(((c[3] * lT + c[2]) * lT + c[1]) * lT + c[0]) * _den;
+        }
     }
     f.mu[id] = mu;
     if (heat) f.kappa[id] = kap;
+}
+
+// The mixed form's transport: the same sums in FP32 (mu and kappa to ~1e-6 relative; the fits lose
+// about one decade to cancellation), from the FP32 table trf (species resolved, PHI's constant
+// 0.5 / sqrt(2) folded into wb).
+template <int NS>
+__global__ void __launch_bounds__(kThreads) k_transport_f32(Geo g, DevFields f, DevThermo th, int heat, int guard) {
+    if (guard && step_done(f)) return;
+    const int nx = g.dimx ? g.Xi + 4 : 1, ny = g.dimy ? g.Yi + 4 : 1, nz = g.dimz ? g.Zi + 4 : 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nx * ny * nz) return;
+    const int i0 = (int)(t % nx) + (g.dimx ? g.Bx - 2 : 0);
+    const long long r = t / nx;
+    const int j0 = (int)(r % ny) + (g.dimy ? g.By - 2 : 0), k0 = (int)(r / ny) + (g.dimz ? g.Bz - 2 : 0);
+    const long long P = g.pitch, id = (long long)g.Xmax * g.Ymax * k0 + (long long)g.Xmax * j0 + i0;
+    const float *visc = f.trf, *therm = f.trf + 4 * NS, *wa = f.trf + 8 * NS, *wb = f.trf + 8 * NS + NS * NS;
+    const float lT = logf((float)f.T[id]);
+    const double rho = f.rho[id];
+    float X[NS], mk[NS], sq[NS], isq[NS];
+    float C_total = 0.0f;
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+        X[i] = (float)(f.y[i * P + id] * rho) * (float)(th._Wi[i] * 1e-3);
+        C_total += X[i];
+    }
+    const float _C = 1.0f / C_total;
+#pragma unroll
+    for (int i = 0; i < NS; i++) X[i] *= _C;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        const float *c = visc + 4 * k;
+        mk[k] = expf(((c[3] * lT + c[2]) * lT + c[1]) * lT + c[0]);
+        sq[k] = sqrtf(mk[k]);
+        isq[k] = 1.0f / sq[k];
+    }
+    float mu = 0.0f, kap = 0.0f;
+#pragma unroll
+    for (int k = 0; k < NS; k++) {
+        float den = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NS; i++) {
+            const float q = wa[k * NS + i] * (sq[k] * isq[i]) + 1.0f;
+            den += X[i] * (q * q * wb[k * NS + i]);
+        }
+        const float _den = 1.0f / den;
+        mu += X[k] * mk[k] * _den;
+        if (heat) {
+            const float *c = therm + 4 * k;
+            kap += X[k] * expf(((c[3] * lT + c[2]) * lT + c[1]) * lT + c[0]) * _den;
+        }
+    }
+    f.mu[id] = (double)mu;
+    if (heat) f.kappa[id] = (double)kap;
 }
 
 // viscous stress and heat-conduction flux at the faces i+1/2 of direction D, subtracted from the

@@ -61,8 +61,31 @@ xfg_scheme to_scheme() {
 #endif
     s.precision = XFG_FP64;
     s.positivity = PositivityPreserving ? 1 : 0;  // read_json.cpp:68
+#if Visc
+    s.viscous = 1 | (Visc_Heat ? 2 : 0) | (Visc_Diffu ? 4 : 0);  // cmake/init_options.cmake:81-91
+#endif
     return s;
 }
+
+#if Visc
+// Setup's fitted transport coefficients (src/read_ini/src/viscfit.cpp:148-196, GetFitCoefficient) and the
+// diffusion limiters of the block, packed densely with the species count as stride.
+xfg_transport to_transport(const Setup &s) {
+    xfg_transport t{};
+    const int ns = NUM_SPECIES, m = XFG_FIT_ORDER;
+    t.num_species = ns;
+    for (int k = 0; k < ns; k++)
+        for (int i = 0; i < m; i++) {
+            t.visc[k * m + i] = s.h_thermal.fitted_coefficients_visc[k][i];
+            t.therm[k * m + i] = s.h_thermal.fitted_coefficients_therm[k][i];
+        }
+    for (int kj = 0; kj < ns * ns; kj++)
+        for (int i = 0; i < m; i++) t.dkj[kj * m + i] = s.h_thermal.Dkj_matrix[kj][i];
+    for (int q = 0; q < ns * XFG_SPCH; q++) t.species_chara[q] = s.h_thermal.species_chara[q];
+    t.yil_limiter = s.BlSz.Yil_limiter, t.dim_limiter = s.BlSz.Dim_limiter;
+    return t;
+}
+#endif
 
 xfg_thermal to_thermal(const Setup &s) {
     xfg_thermal t{};
@@ -127,6 +150,10 @@ void Fluid::AllocateFluidMemory(sycl::queue &q) {
     xfg_handle *h = nullptr;
     check(xfg_create(&b, &s, &t, Fs.DeviceSelect.size() > 2 ? Fs.DeviceSelect[2] : 0, &h), "xfg_create");
     g_handles[this] = h;
+#if Visc
+    xfg_transport tr = to_transport(Fs);
+    check(xfg_set_transport(h, &tr), "xfg_set_transport");
+#endif
 }
 
 void Fluid::InitialU(sycl::queue &q) {

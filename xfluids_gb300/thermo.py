@@ -125,3 +125,13 @@ def transport_from_arrays(ns, visc, therm, dkj, chara, yil_limiter, dim_limiter)
             dst[q] = float(v)
     t.yil_limiter, t.dim_limiter = float(yil_limiter), float(dim_limiter)
     return t
+
+
+def load_transport(path):
+    """xfg_transport from a file holding fitted transport data: an .npz with the arrays tr_visc
+    (ns x 4), tr_therm (ns x 4), tr_dkj (ns*ns x 4), tr_chara (ns x 9) and tr_limits (Yil_limiter,
+    Dim_limiter), as the golden fixtures of the viscous cases store the reference's fits."""
+    import numpy as np
+    z = np.load(path)
+    ns = z["tr_chara"].size // 9
+    return transport_from_arrays(ns, z["tr_visc"], z["tr_therm"], z["tr_dkj"], z["tr_chara"], *z["tr_limits"])

@@ -2,12 +2,14 @@
 
     python -m xfluids_gb300.workloads vortex   --size 1024 --steps 10 [--precision mixed]
     python -m xfluids_gb300.workloads sod      --size 1024 --steps 100
-    python -m xfluids_gb300.workloads mixing   --shape 256 128 64 --steps 2 [--precision mixed]
+    python -m xfluids_gb300.workloads mixing   --shape 256 128 64 --steps 2 [--precision mixed] [--viscous]
     python -m xfluids_gb300.workloads ensemble --members 32 --steps 4 [--precision mixed]
 
 Each run: initial state on the host, one warm-up step (captures the step graph), a reset to the
 initial state, then the timed steps (CUDA events around the graph replays). The mixing layer reads
-the thermo tables from a tables JSON (thermo.dump_tables), by default the one under tests/golden.
+the thermo tables from a tables JSON (thermo.dump_tables), by default the one under tests/golden;
+with --viscous it adds viscous stress, heat conduction and species diffusion with the fitted
+transport data of an .npz (thermo.load_transport), by default the viscous golden fixture's.
 """
 from __future__ import annotations
 
@@ -18,14 +20,17 @@ import os
 from . import cases, thermo
 from .abi import MIXED
 
-DEFAULT_TABLES = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
-                              "thermo_tables.json")
+_GOLDEN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden")
+DEFAULT_TABLES = os.path.join(_GOLDEN, "thermo_tables.json")
+DEFAULT_TRANSPORT = os.path.join(_GOLDEN, "visc_mixing5_12x8x6_janaf_w5.npz")
 
 
-def single_grid(b, s, th, U, T, steps, device=0):
+def single_grid(b, s, th, U, T, steps, device=0, transport=None):
     from .fluid import Fluid
     f = Fluid(b, s, th, device=device)
     try:
+        if transport is not None:
+            f.set_transport(transport)
         f.InitialU(U, T)
         f.initialize()
         f.advance(1)
@@ -67,6 +72,8 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--precision", choices=["fp64", "mixed", "strict"], default="fp64")
     ap.add_argument("--tables", default=DEFAULT_TABLES)
+    ap.add_argument("--viscous", action="store_true", help="mixing: viscous, heat and diffusion fluxes")
+    ap.add_argument("--transport", default=DEFAULT_TRANSPORT)
     ap.add_argument("--tune", action="store_true", help="ensemble: run the schedule autotuner first")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
@@ -81,8 +88,13 @@ def main(argv=None):
         else:
             th = thermo.load_thermal(cases.MIXING_SPECIES, 0, tables_json=a.tables)
             b, s, th, U, T = cases.mixing_layer(tuple(a.shape), thermal=th, precision=prec)
-        out = single_grid(b, s, th, U, T, a.steps, a.device)
-    out.update({"workload": a.workload, "precision": a.precision})
+        tr = None
+        if a.viscous:
+            if a.workload != "mixing":
+                raise SystemExit("--viscous needs a mixture (the mixing workload)")
+            s.viscous, tr = 7, thermo.load_transport(a.transport)
+        out = single_grid(b, s, th, U, T, a.steps, a.device, tr)
+    out.update({"workload": a.workload, "precision": a.precision, "viscous": bool(a.viscous)})
     print(json.dumps(out))
     return 0
 
