@@ -174,7 +174,8 @@ def mixing_layer(shape=(512, 256, 256), thermal=None, length=0.01, seed=1234, pr
     Domain [0, L] x [0, L*ny/nx] x [0, L*nz/nx]. Upper stream (y > mid): Y_O2 = 0.233,
     Y_N2 = 0.767 at 1200 K, Mach +0.6; lower stream: Y_H2 = 0.05, Y_N2 = 0.95 at 300 K,
     Mach -0.6; tanh blend of thickness 0.01 L; p = 1 atm; velocity perturbed by `noise` times
-    the local speed with a counter-based hash of (seed, i, j, k). Periodic in x and z.
+    the local speed with a counter-based hash of (seed, i, j, k). Periodic in x and z; in y
+    `ybc` (outflow by default; with PERIODIC the ghost rows start as the periodic images).
     """
     nx, ny, nz = shape
     dom = (length, length * ny / nx, length * nz / nx)
@@ -183,7 +184,12 @@ def mixing_layer(shape=(512, 256, 256), thermal=None, length=0.01, seed=1234, pr
                     ghost_species=False, precision=precision)
     # the mean state depends on y only: build it on the y column, then broadcast (same values as
     # evaluating every cell)
-    Y = (np.arange(b.Ymax) - b.Bwidth_Y + 0.5) * b.dy
+    jy = np.arange(b.Ymax) - b.Bwidth_Y
+    if ybc == PERIODIC:
+        # ghost rows hold their periodic images, so that the initial T (the warm start of the
+        # clamped temperature Newton iteration) agrees with the state the boundary fill puts there
+        jy = np.mod(jy, ny)
+    Y = (jy + 0.5) * b.dy
     ymid = 0.5 * dom[1]
     wgt = 0.5 * (1.0 + np.tanh((Y - ymid) / (0.01 * length)))  # 1 upper, 0 lower
     y_up = np.array([0.0, 0.233, 0.767, 0.0, 0.0])
