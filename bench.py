@@ -275,7 +275,9 @@ def bench_mixing_layer(args, local, steps):
     """3D inert temporal mixing layer (512 x 256 x 256, 5 species H2/O2/N2/H2O/AR, 7-coefficient
     thermo of the reference's runtime.dat, WENO7 LLF), FP64 and mixed from the same state: one
     warm-up step (graph capture), a reset, then `steps` timed steps; relative L1 / Linf of the
-    mixed state against the FP64 state at the same step count. The same runs with viscous stress,
+    mixed state against the FP64 state at the same step count; the strict form (no contraction,
+    the reference's operation order) beside the FP64 form (contracted face sweeps). The FP64 and
+    mixed runs with viscous stress,
     heat conduction and species diffusion (the reference's fitted transport data) give the share of
     a step those terms add."""
     from xfluids_gb300 import thermo
@@ -285,7 +287,7 @@ def bench_mixing_layer(args, local, steps):
     b, s, th, U, T = cases_mod().mixing_layer((512, 256, 256), thermal=th)
     res, states = {}, {}
     tr = thermo.load_transport(TRANSPORT_NPZ)
-    for prec, visc in ((0, 0), (MIXED, 0), (0, 7), (MIXED, 7)):
+    for prec, visc in ((0, 0), (MIXED, 0), (2, 0), (0, 7), (MIXED, 7)):
         s.precision, s.viscous = prec, visc
         f = Fluid(b, s, th, device=local)
         if visc:
@@ -298,9 +300,9 @@ def bench_mixing_layer(args, local, steps):
         f.time = 0.0
         st, t, k, ms = f.advance_timed(steps)
         cells = b.X_inner * b.Y_inner * b.Z_inner
-        key = ("fp64" if prec == 0 else "mixed") + ("_viscous" if visc else "")
+        key = {0: "fp64", MIXED: "mixed", 2: "fp64_strict"}[prec] + ("_viscous" if visc else "")
         res[key] = {"value": cells * k / (ms * 1e-3), "ms_per_step": ms / k, "steps": k, "status": st, "t": t}
-        if not visc:
+        if not visc and prec != 2:
             states[prec] = f.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 9)[b.inner_slices()].reshape(-1, 9)
         f.close()
     s.viscous = 0

@@ -144,6 +144,12 @@ int xfg_set_state(xfg_handle *h, const double *U_aos, const double *T);
  * buffers in XFLUIDS::Output / CopyDataFromDevice (src/XFLUIDS.cpp:644-656, :726-828). */
 int xfg_get_array(xfg_handle *h, int which, double *out);
 
+/* Copy one array in (host or device pointer), for which = XFG_U, XFG_U1 (AoS) or XFG_T: the
+ * writes a caller makes into Fluid's public device buffers d_U / d_U1 / d_fstate.T (e.g. the
+ * memcpy of XFLUIDS::Read_Ubak, src/XFLUIDS.cpp:689-724). T is the warm start of the next
+ * temperature Newton iteration. */
+int xfg_set_array(xfg_handle *h, int which, const double *in);
+
 /* Ghost-cell fill of U (flag 0) or U1 (flag != 0): replaces Fluid::BoundaryCondition
  * (src/Fluids.cpp:922-933) -> FluidBoundaryCondition (src/solver_BCs/BCs_block.cpp:4-218). */
 int xfg_boundary(xfg_handle *h, int flag);

@@ -131,6 +131,7 @@ def lib():
         "xfg_destroy": [P],
         "xfg_set_state": [P, P, P],
         "xfg_get_array": [P, I, P],
+        "xfg_set_array": [P, I, P],
         "xfg_boundary": [P, I],
         "xfg_update_states": [P, I, pi, C.POINTER(C.c_float)],
         "xfg_compute_lu": [P, I, C.POINTER(C.c_float)],

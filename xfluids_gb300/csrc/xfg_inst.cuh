@@ -48,7 +48,7 @@ struct Inst {
         const double *glf = c.glf ? c.glf + 3 * D : nullptr;
         (void)n;
         const dim3 grid = face_grid<D>(g), block(32, 4, 1);
-        if (MIXED)
+        if constexpr (MIXED)
             k_faces_mixed<D, COP, NS, ORDER><<<grid, block, 0, c.st>>>(g, c.f, c.th, c.artificial, glf, guard);
         else
             k_faces<D, COP, NS, ORDER><<<grid, block, 0, c.st>>>(g, c.f, c.th, UI, c.artificial, glf, guard);
@@ -142,6 +142,21 @@ struct Registrar {
     explicit Registrar(std::initializer_list<int> precisions) {
         for (int prec : precisions) {
             for (int order = 5; order <= 7; order++) register_ops(Inst<COP, NS, MIXED>::table(order, prec));
+        }
+    }
+};
+
+// Registers only the face-sweep launchers of one mixture size under the given precision ids,
+// replacing those of the tables another unit registered (this unit's compile flags apply to the
+// face kernels alone).
+template <bool COP, int NS>
+struct FacesRegistrar {
+    explicit FacesRegistrar(std::initializer_list<int> precisions) {
+        using I = Inst<COP, NS, false>;
+        for (int prec : precisions) {
+            register_faces_override(COP ? 1 : 0, NS, 5, prec, &I::template faces<5>);
+            register_faces_override(COP ? 1 : 0, NS, 6, prec, &I::template faces<6>);
+            register_faces_override(COP ? 1 : 0, NS, 7, prec, &I::template faces<7>);
         }
     }
 };

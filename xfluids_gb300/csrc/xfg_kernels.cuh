@@ -329,6 +329,17 @@ static __global__ void __launch_bounds__(kThreads) k_glf(Geo g, DevFields f, uns
 // WENO5-JS, WENO-CU6 (scheme order 6) or WENO7.
 // Local eigenvalues (GetLocalEigen) are formed on the fly from u_d and c of the window cells.
 // ---------------------------------------------------------------------------------------------
+// The mixture's Roe-linearised sound speed (ReconstructSoundSpeed) is ill-conditioned: in smooth
+// flow temp1 = dp - (dp/drho drho + dp/de de + sum dp/drho_i drho_i) is rounding noise divided by
+// a sum of squared small jumps, and it corrects dp/dE, dp/drho and c^2. Its result depends on the
+// rounding of every operation before it, so the mixture branch is written with round-to-nearest
+// operations the compiler never contracts into an FMA (pm / pa / ps), in the reference's operation
+// order; units built with --fmad=false get the same bits, and units that contract the rest of
+// the face (projections, WENO, back-projection) keep this state exact.
+__device__ __forceinline__ double pm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double pa(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ps(double a, double b) { return __dsub_rn(a, b); }
+
 template <bool COP, int NS>
 __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, const DevThermo &th, long long l,
                                            long long r, FaceState<NS> &F, double &Gamma0) {
@@ -339,102 +350,87 @@ __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, con
     const double D = sqrt(rr / rl);
     const double D1 = 1.0 / (D + 1.0);
     F.D = D, F.D1 = D1;
-    F._u = (ul + D * ur) * D1;
-    F._v = (vl + D * vr) * D1;
-    F._w = (wl + D * wr) * D1;
-    F._H = (Hl + D * Hr) * D1;
-    F._P = (pl + D * pr) * D1;
-    F._rho = sqrt(rr * rl);
-    if (!COP) {
+    if constexpr (!COP) {
+        F._u = (ul + D * ur) * D1;
+        F._v = (vl + D * vr) * D1;
+        F._w = (wl + D * wr) * D1;
+        F._H = (Hl + D * Hr) * D1;
+        F._P = (pl + D * pr) * D1;
+        F._rho = sqrt(rr * rl);
         Gamma0 = th.ncop_gamma;
         F.c2 = Gamma0 * F._P / F._rho;
         F.b1 = (Gamma0 - 1.0) / F.c2;
         F.b3 = 0.0;
         F._yi[0] = 1.0;
+        F.q2 = F._u * F._u + F._v * F._v + F._w * F._w;
+        F._c = sqrt(F.c2);
+        F.b2 = 1.0 + F.b1 * F.q2 - F.b1 * F._H;
+        F._c1 = 1.0 / F._c;
+        F.ent0 = (1.0 - F.b2 - F.b3) / F.b1;
     } else {
         constexpr int NCOP = NS - 1;
+        auto roe = [&](double a, double b) { return pm(pa(a, pm(D, b)), D1); };  // (a + D b) D1
+        F._u = roe(ul, ur), F._v = roe(vl, vr), F._w = roe(wl, wr);
+        F._H = roe(Hl, Hr), F._P = roe(pl, pr);
+        F._rho = sqrt(pm(rr, rl));
         double yl[NS], yr[NS];
 #pragma unroll
         for (int n = 0; n < NS; n++) {
             yl[n] = f.y[n * P + l];
             yr[n] = f.y[n * P + r];
-            F._yi[n] = (yl[n] + D * yr[n]) * D1;
+            F._yi[n] = roe(yl[n], yr[n]);
         }
-        // cell terms (cop_cell_terms): gamma, dp/drho, e, dp/drho_i of each side
-        double gl, gr, el, er, _dpdrho;
+        // cell terms (cop_cell_terms, written by the states kernel of every mixture path):
+        // gamma, dp/drho, e, dp/drho_i of each side
+        const double *xc = f.xc;
+        const double gl = xc[l], gr = xc[r];
+        const double _dpdrho = roe(xc[P + l], xc[P + r]);
+        const double el = xc[2 * P + l], er = xc[2 * P + r];
         double dpdrhoi[NCOP > 0 ? NCOP : 1], drhoi[NCOP > 0 ? NCOP : 1];
-        if (f.xc) {
-            const double *xc = f.xc;
-            gl = xc[l], gr = xc[r];
-            _dpdrho = (xc[P + l] + D * xc[P + r]) * D1;
-            el = xc[2 * P + l], er = xc[2 * P + r];
 #pragma unroll
-            for (int n = 0; n < NCOP; n++) {
-                dpdrhoi[n] = (xc[(3 + n) * P + l] + D * xc[(3 + n) * P + r]) * D1;
-                drhoi[n] = rr * yr[n] - rl * yl[n];
-            }
-        } else {
-            double hl[NS], hr[NS];
-            const double Tl = f.T[l], Tr = f.T[r];
-#pragma unroll
-            for (int n = 0; n < NS; n++) hl[n] = enthalpy(th, Tl, n), hr[n] = enthalpy(th, Tr, n);
-            const double Cpl = mix_Cp<NS>(th, yl, Tl), Cpr = mix_Cp<NS>(th, yr, Tr);
-            const double wl_ = mix_W_inv<NS>(th, yl), wr_ = mix_W_inv<NS>(th, yr);
-            gl = Cpl / (Cpl - kRu * wl_), gr = Cpr / (Cpr - kRu * wr_);  // get_CopGamma(yi, T)
-            const double q2l = ul * ul + vl * vl + wl * wl, q2r = ur * ur + vr * vr + wr * wr;
-            const double Rl = wl_ * kRu, Rr = wr_ * kRu;
-            el = Hl - 0.5 * q2l - pl / rl, er = Hr - 0.5 * q2r - pr / rr;
-            const double RN = th.Ri[NCOP];
-            auto dpdrho = [&](double hN, double q2, double Cp, double Rm, double T, double gm) {
-                double RNT = RN * T;
-                return (gm - 1.0) * (0.5 * q2 - hN + Cp * RNT / Rm);
-            };
-            _dpdrho = (dpdrho(hl[NCOP], q2l, Cpl, Rl, Tl, gl) + D * dpdrho(hr[NCOP], q2r, Cpr, Rr, Tr, gr)) * D1;
-#pragma unroll
-            for (int n = 0; n < NCOP; n++) {
-                const double Rin_RN = th.Ri[n] - RN;
-                const double a = (gl - 1.0) * ((-hl[n] + hl[NCOP]) + Cpl * Rin_RN * Tl / Rl);
-                const double b = (gr - 1.0) * ((-hr[n] + hr[NCOP]) + Cpr * Rin_RN * Tr / Rr);
-                dpdrhoi[n] = (a + D * b) * D1;
-                drhoi[n] = rr * yr[n] - rl * yl[n];
-            }
+        for (int n = 0; n < NCOP; n++) {
+            dpdrhoi[n] = roe(xc[(3 + n) * P + l], xc[(3 + n) * P + r]);
+            drhoi[n] = ps(pm(rr, yr[n]), pm(rl, yl[n]));
         }
-        Gamma0 = (gl + D * gr) * D1;
-        const double _prho = (pl / rl + D * (pr / rr)) * D1 +
-                             0.5 * D * D1 * D1 * ((ur - ul) * (ur - ul) + (vr - vl) * (vr - vl) + (wr - wl) * (wr - wl));
-        const double _dpdE = ((gl - 1.0) + D * (gr - 1.0)) * D1;
-        const double _dpde = ((gl - 1.0) * rl + D * ((gr - 1.0) * rr)) * D1;
-        const double dp = pr - pl, drho = rr - rl, de = er - el;
+        Gamma0 = roe(gl, gr);
+        const double du = ps(ur, ul), dv = ps(vr, vl), dw = ps(wr, wl);
+        const double _prho = pa(pm(pa(pl / rl, pm(D, pr / rr)), D1),
+                                pm(pm(pm(pm(0.5, D), D1), D1), pa(pa(pm(du, du), pm(dv, dv)), pm(dw, dw))));
+        const double _dpdE = roe(ps(gl, 1.0), ps(gr, 1.0));
+        const double _dpde = pm(pa(pm(ps(gl, 1.0), rl), pm(D, pm(ps(gr, 1.0), rr))), D1);
+        const double dp = ps(pr, pl), drho = ps(rr, rl), de = ps(er, el);
         double S1 = 0.0, S2 = 0.0, SY = 0.0;
 #pragma unroll
         for (int n = 0; n < NCOP; n++) {
-            S1 += dpdrhoi[n] * drhoi[n];
-            S2 += dpdrhoi[n] * drhoi[n] * dpdrhoi[n] * drhoi[n];
+            S1 = pa(S1, pm(dpdrhoi[n], drhoi[n]));
+            S2 = pa(S2, pm(pm(pm(dpdrhoi[n], drhoi[n]), dpdrhoi[n]), drhoi[n]));
         }
-        const double temp1 = dp - (_dpdrho * drho + _dpde * de + S1);
-        const double temp = temp1 / (_dpdrho * _dpdrho * drho * drho + _dpde * de * _dpde * de + S2 + 1e-19);
+        const double temp1 = ps(dp, pa(pa(pm(_dpdrho, drho), pm(_dpde, de)), S1));
+        const double den = pa(pa(pa(pm(pm(pm(_dpdrho, _dpdrho), drho), drho), pm(pm(pm(_dpde, de), _dpde), de)), S2),
+                              1e-19);
+        const double temp = temp1 / den;
 #pragma unroll
-        for (int n = 0; n < NCOP; n++) SY += F._yi[n] * dpdrhoi[n];
-        const double _dpdE_new = _dpdE + _dpdE * _dpdE * de * F._rho * temp;
-        const double _dpdrho_new = _dpdrho + _dpdrho * _dpdrho * drho * temp;
-        const double csqr = _dpdrho_new + _dpdE_new * _prho + SY;
+        for (int n = 0; n < NCOP; n++) SY = pa(SY, pm(F._yi[n], dpdrhoi[n]));
+        const double _dpdE_new = pa(_dpdE, pm(pm(pm(pm(_dpdE, _dpdE), de), F._rho), temp));
+        const double _dpdrho_new = pa(_dpdrho, pm(pm(pm(_dpdrho, _dpdrho), drho), temp));
+        const double csqr = pa(pa(_dpdrho_new, pm(_dpdE_new, _prho)), SY);
         F.b1 = _dpdE_new / csqr;
         double b3 = 0.0;
 #pragma unroll
         for (int n = 0; n < NCOP; n++) {
-            const double dn = dpdrhoi[n] + dpdrhoi[n] * dpdrhoi[n] * drhoi[n] * temp;
+            const double dn = pa(dpdrhoi[n], pm(pm(pm(dpdrhoi[n], dpdrhoi[n]), drhoi[n]), temp));
             F.z[n] = -dn / _dpdE_new;
-            b3 += F._yi[n] * F.z[n];
+            b3 = pa(b3, pm(F._yi[n], F.z[n]));
         }
-        F.b3 = b3 * F.b1;
+        F.b3 = pm(b3, F.b1);
         const double c2w = (0.0 < csqr) ? 0.0 : 1.0;
-        F.c2 = Gamma0 * F._P * F._rho * c2w + (1.0 - c2w) * csqr;
+        F.c2 = pa(pm(pm(pm(Gamma0, F._P), F._rho), c2w), pm(ps(1.0, c2w), csqr));
+        F.q2 = pa(pa(pm(F._u, F._u), pm(F._v, F._v)), pm(F._w, F._w));
+        F._c = sqrt(F.c2);
+        F.b2 = ps(pa(1.0, pm(F.b1, F.q2)), pm(F.b1, F._H));
+        F._c1 = 1.0 / F._c;
+        F.ent0 = ps(ps(1.0, F.b2), F.b3) / F.b1;
     }
-    F.q2 = F._u * F._u + F._v * F._v + F._w * F._w;
-    F._c = sqrt(F.c2);
-    F.b2 = 1.0 + F.b1 * F.q2 - F.b1 * F._H;
-    F._c1 = 1.0 / F._c;
-    F.ent0 = (1.0 - F.b2 - F.b3) / F.b1;
 }
 
 // Single-gas Roe state of the FP64 fast path from the per-cell sqrt(rho) and 1/sqrt(rho):

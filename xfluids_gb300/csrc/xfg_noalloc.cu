@@ -100,10 +100,12 @@ extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *
     const int E = scheme->cop ? scheme->num_species + 4 : 5, NS = scheme->cop ? scheme->num_species : 1;
     const long long N = (long long)block->Xmax * block->Ymax * block->Zmax;
     const long long P = (long long)up((size_t)N, 64);
-    // U, LU, 12 primitives, y, F and Fw per active direction, and for the single-gas FP64 fast
-    // kernels sqrt(rho), 1/sqrt(rho) and 3 |lambda| per direction; 1024 doubles of small words
+    // U, LU, 12 primitives, y and the per-cell sound-speed terms of a mixture (3 + NS - 1), F and
+    // Fw per active direction, and for the single-gas FP64 fast kernels sqrt(rho), 1/sqrt(rho) and
+    // 3 |lambda| per direction; 1024 doubles of small words
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;
-    const size_t arrays = 2 * E + 12 + (scheme->cop ? NS : 0) + 2 * E * ndim + (fast1 ? 2 + 3 * ndim : 0);
+    const size_t arrays =
+        2 * E + 12 + (scheme->cop ? NS + 3 + (NS - 1) : 0) + 2 * E * ndim + (fast1 ? 2 + 3 * ndim : 0);
     const size_t need_doubles = arrays * (size_t)P + 1024;
     if (need_doubles > kScratchDoubles)
         return fail(-2, "block too large for the fixed scratch of xfg_compute_lu_noalloc "
@@ -126,7 +128,7 @@ extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *
     f.LU = take(E);
     f.rho = take(1), f.u = take(1), f.v = take(1), f.w = take(1), f.p = take(1), f.H = take(1);
     f.c = take(1), f.T = take(1), f.gamma = take(1), f.e = take(1), f.Cp = take(1), f.R = take(1);
-    if (scheme->cop) f.y = take(NS);
+    if (scheme->cop) f.y = take(NS), f.xc = take(3 + (NS - 1));
     for (int d = 0; d < 3; d++)
         if (dims[d]) f.F[d] = take(E), f.Fw[d] = take(E);
     if (fast1) {

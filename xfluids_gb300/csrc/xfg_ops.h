@@ -45,6 +45,10 @@ void set_last_error(const char *msg);
 // Registry filled by the instantiation units.
 const Ops *find_ops(int cop, int ns, int order, int precision);
 void register_ops(const Ops *ops);
+// Face-sweep launcher from another instantiation unit (other compile flags) that replaces the
+// `faces` entry of the table registered under the same key.
+using FacesFn = void (*)(const LaunchCtx &, int d, const double *UI, int guard);
+void register_faces_override(int cop, int ns, int order, int precision, FacesFn faces);
 
 inline unsigned grid_for(long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 

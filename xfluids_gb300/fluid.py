@@ -81,6 +81,17 @@ class Fluid:
         check(lib().xfg_get_array(self._h, ARRAYS[name], out.ctypes.data_as(C.c_void_p)))
         return out
 
+    def set(self, name: str, arr: np.ndarray):
+        """Write U, U1 (reference AoS layout, ghosts included) or T into the handle."""
+        n = self.block.ncell
+        size = n * self.E if name in ("U", "U1") else n
+        if name not in ("U", "U1", "T"):
+            raise ValueError("set() takes U, U1 or T")
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        if a.size != size:
+            raise ValueError(f"{name} needs {size} values")
+        check(lib().xfg_set_array(self._h, ARRAYS[name], a.ctypes.data_as(C.c_void_p)))
+
     # -- the reference's stage methods -------------------------------------------------------
     def BoundaryCondition(self, flag: int = 0):
         check(lib().xfg_boundary(self._h, flag))
