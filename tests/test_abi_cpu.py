@@ -82,8 +82,10 @@ def test_ensemble_rejects_unsupported_schemes_before_touching_a_device(cuda_lib)
     from xfluids_gb300.ensemble import Ensemble
     from xfluids_gb300.mesh import make_scheme
     for kw in (dict(cop=True, num_species=2), dict(artificial_type=abi.GLF), dict(precision=2),
-               dict(scheme_order=6), dict(positivity=True)):
+               dict(scheme_order=6), dict(viscous=1)):
+        visc = kw.pop("viscous", 0)
         sc = make_scheme(**{"scheme_order": 5, "artificial_type": abi.LLF, **kw})
+        sc.viscous = visc
         with pytest.raises(abi.XfgError):
             Ensemble(sc, capacity=2, pool_bytes=1 << 20)
 

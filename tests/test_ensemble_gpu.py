@@ -81,6 +81,31 @@ def test_members_equal_single_grid_runs(cuda_lib, order, art, prec):
         e.close()
 
 
+@pytest.mark.parametrize("prec", [FP64, MIXED], ids=["fp64", "mixed"])
+def test_members_with_positivity_limiter_equal_single_grid_runs(cuda_lib, prec):
+    """With the positivity limiter on, every member (among them member 88 of the seeded ensemble,
+    whose first stage turns the density negative without the limiter) equals its single-grid run."""
+    from helpers import riemann_member
+    scheme = make_scheme(cop=False, scheme_order=5, artificial_type=LLF, precision=prec, positivity=True)
+    b88, _, _, U88, _ = riemann_member(88, 32)
+    ms = [(b88, U88)] + members()[:3]
+    nsteps = 6
+    e = Ensemble(scheme, capacity=len(ms), pool_bytes=pool_for([b for b, _ in ms], prec))
+    try:
+        slots = [e.add(b, U, 1e300) for b, U in ms]
+        st, _ = e.advance(nsteps)
+        assert st == 0
+        for (b, U), s in zip(ms, slots):
+            ref, t_ref, n_ref = alone(b, U, scheme, nsteps)
+            info = e.status(s)
+            assert info["error"] == 0 and info["steps"] == n_ref == nsteps
+            assert info["t"] == pytest.approx(t_ref, rel=1e-13 if prec == FP64 else MIXED_T_TOL, abs=0)
+            err = normwise(e.get_state(s), ref, 5).max()
+            assert err <= (PARITY_TOL if prec == FP64 else MIXED_TOL), (s, err)
+    finally:
+        e.close()
+
+
 def run_ensemble(scheme, ms, nsteps, use_graph, largest_first=1, chunks=1, **sched):
     e = Ensemble(scheme, capacity=len(ms), pool_bytes=pool_for([b for b, _ in ms], scheme.precision))
     try:

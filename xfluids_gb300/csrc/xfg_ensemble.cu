@@ -136,6 +136,33 @@ __global__ void __launch_bounds__(kThreads) kb_div_rk(const Member *__restrict__
         div_rk_body<5>(m.g, m.f, flag, m.f.dtbuf[0], 1, 0, t);
 }
 
+// positivity-preserving flux limiter (PositivityPreserving_kernels.hpp:5-76) on the face fluxes of
+// every active direction of every member, with the member's wave-speed maxima of this step
+// (written by kb_dt into dtbuf[5..7]); one thread per inner cell, as the divergence phase
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_pp(const Member *__restrict__ M, const int *__restrict__ off, int n, int flag) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    const double *UI = flag == 1 || flag == 0 ? m.f.U : m.f.U1;
+    const int dims[3] = {m.g.dimx, m.g.dimy, m.g.dimz};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        if (!dims[d]) continue;
+        const double l0 = m.f.dtbuf[5 + d];
+        if (MIXED) {
+            if (d == 0) pp_body<0, 5, 0, float>(m.g, UI, m.f.Ff[0], m.f.Fwf[0], l0, m.cfl / l0, t);
+            else if (d == 1) pp_body<1, 5, 0, float>(m.g, UI, m.f.Ff[1], m.f.Fwf[1], l0, m.cfl / l0, t);
+            else pp_body<2, 5, 0, float>(m.g, UI, m.f.Ff[2], m.f.Fwf[2], l0, m.cfl / l0, t);
+        } else {
+            if (d == 0) pp_body<0, 5, 0, double>(m.g, UI, m.f.F[0], m.f.Fw[0], l0, m.cfl / l0, t);
+            else if (d == 1) pp_body<1, 5, 0, double>(m.g, UI, m.f.F[1], m.f.Fw[1], l0, m.cfl / l0, t);
+            else pp_body<2, 5, 0, double>(m.g, UI, m.f.F[2], m.f.Fw[2], l0, m.cfl / l0, t);
+        }
+    }
+}
+
 __global__ void kb_dt(const Member *__restrict__ M, int n) {
     const int mi = blockIdx.x * blockDim.x + threadIdx.x;
     if (mi >= n) return;
@@ -400,6 +427,10 @@ void launch_step(xfg_ensemble *e) {
             XFG_FACES(2, PH_F2)
 #undef XFG_FACES
         }
+        if (e->sc.positivity) {
+            if (mixed) kb_pp<true><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
+            else kb_pp<false><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
+        }
         if (mixed) kb_div_rk<true><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
         else kb_div_rk<false><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
     }
@@ -417,7 +448,7 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_MIXED)
         return efail(-1, "ensemble precision must be XFG_FP64 or XFG_MIXED%s");
     if (scheme->artificial_type == XFG_GLF) return efail(-1, "the ensemble engine supports Roe and LLF splitting%s");
-    if (scheme->positivity) return efail(-1, "the ensemble engine has no positivity limiter%s");
+    if (scheme->positivity != 0 && scheme->positivity != 1) return efail(-1, "positivity must be 0 or 1%s");
     if (scheme->viscous) return efail(-1, "the ensemble engine serves inviscid single-gas members%s");
     if (scheme->scheme_order != 5 && scheme->scheme_order != 7) return efail(-1, "scheme_order must be 5 or 7%s");
     ECK(cudaSetDevice(device));

@@ -13,6 +13,80 @@
 namespace xfg {
 namespace XFG_KNS {
 
+// Mixture thermodynamics of the mixed form with the species folded into one polynomial.
+// h(T) = sum_n y_n h_n(T) and Cp(T) = sum_n y_n Cp_n(T) are linear in the species, and the
+// temperature ranges of both tables do not depend on the species (JANAF breaks at 1000 K, NASA-9
+// at 1000 / 6000 K), so within a range the mixture has coefficients
+// A_c = sum_n y_n R_n a_{n,c} (and the enthalpy constant B = sum_n y_n R_n b_n), folded once per
+// cell and range: each Newton iteration is one polynomial (and one log for NASA-9) instead of NS.
+// Below 200 K (the tables' linear extrapolation) the per-species functions are used. Same
+// mathematics as the reference's sums, different rounding: the mixed form only.
+template <int NS>
+struct FoldedThermo {
+    double A[7], B;
+    int rg = -9;
+    __device__ __forceinline__ bool fold(const DevThermo &t, const double *yi, double T) {
+        const int r = t.nasa ? nasa_range(T) : (T > 1000.0 ? 0 : 1);
+        if (r < 0) return false;
+        if (r == rg) return true;
+        rg = r;
+#pragma unroll
+        for (int c = 0; c < 7; c++) A[c] = 0.0;
+        B = 0.0;
+#pragma unroll
+        for (int n = 0; n < NS; n++) {
+            const double w = yi[n] * t.Ri[n];
+            const double *a = t.Hia + n * 21 + r;
+#pragma unroll
+            for (int c = 0; c < 7; c++) A[c] = fma(w, a[3 * c], A[c]);
+            B = fma(w, t.nasa ? t.Hib[n * 6 + r] : a[15], B);
+        }
+        return true;
+    }
+    // h and Cp of the mixture at T >= 200 K within the folded range
+    __device__ __forceinline__ void eval(bool nasa, double T, double &h, double &Cp) const {
+        if (nasa) {
+            const double iT = 1.0 / T;
+            Cp = fma(fma(A[0], iT, A[1]), iT, fma(fma(fma(fma(A[6], T, A[5]), T, A[4]), T, A[3]), T, A[2]));
+            h = fma(-A[0], iT, fma(A[1], log(T),
+                                   fma(fma(fma(fma(fma(A[6] * 0.2, T, A[5] * 0.25), T, A[4] * kOT), T, A[3] * 0.5), T,
+                                           A[2]),
+                                       T, B)));
+        } else {
+            Cp = fma(fma(fma(fma(A[4], T, A[3]), T, A[2]), T, A[1]), T, A[0]);
+            h = fma(fma(fma(fma(fma(A[4] * 0.2, T, A[3] * 0.25), T, A[2] * kOT), T, A[1] * 0.5), T, A[0]), T, B);
+        }
+    }
+};
+
+// get_T (Mixing_device.h:171-193): the same clamped Newton iteration and stopping test on the
+// folded mixture polynomials; returns T and the mixture Cp at T.
+template <int NS>
+__device__ double newton_T_folded(const DevThermo &t, const double *yi, double e, double T0, double &Cp_out) {
+    FoldedThermo<NS> ft;
+    double T = T0;
+    const double Rm = mix_R<NS>(t, yi);
+    for (int it = 1; it < 101; it++) {
+        double h, Cp;
+        if (T >= 200.0 && ft.fold(t, yi, T)) {
+            ft.eval(t.nasa, T, h, Cp);
+        } else {
+            h = mix_h<NS>(t, yi, T);
+            Cp = mix_Cp<NS>(t, yi, T);
+        }
+        double f = h - Rm * T - e;
+        double df_ = Cp - Rm;
+        double df = fmin(f / (df_ + 1.0e-30), 1e-3 * T);
+        df = fmax(df, -1e-2 * T);
+        T = T - df;
+        if (fabs(df) <= 1.0e-6) break;
+    }
+    double h;
+    if (T >= 200.0 && ft.fold(t, yi, T)) ft.eval(t.nasa, T, h, Cp_out);
+    else Cp_out = mix_Cp<NS>(t, yi, T);
+    return T;
+}
+
 // Primitive recovery of the mixed form. Single gas: from the FP64 state converted once to FP32.
 // Mixture: the FP64 recovery of k_states (Newton in FP64), followed by the FP32 copies.
 template <bool COP, int NS>
@@ -64,9 +138,9 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             const double ud = U[1] * rho1, vd = U[2] * rho1, wd = U[3] * rho1;
             const double tme = U[4] * rho1 - 0.5 * (ud * ud + vd * vd + wd * wd);
             const double Rm = mix_R<NS>(th, yi);
-            const double T = newton_T<NS>(th, yi, tme, f.T[id]);
+            double Cp;
+            const double T = newton_T_folded<NS>(th, yi, tme, f.T[id], Cp);
             const double pd = rhod * Rm * T;
-            const double Cp = mix_Cp<NS>(th, yi, T);
             const double CopW = 1.0 / mix_W_inv<NS>(th, yi);
             const double gmx = Cp / (Cp - kRu / CopW);
             const double gamma = gmx > 1.0 ? gmx : -1.0;
@@ -240,7 +314,7 @@ __device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &
     } else {
         FaceState<NS> Fd;
         double G0;
-        face_state<COP, NS>(g, f, th, idl, idr, Fd, G0);
+        face_state<COP, NS, false>(g, f, th, idl, idr, Fd, G0);
         F._u = (float)Fd._u, F._v = (float)Fd._v, F._w = (float)Fd._w, F._H = (float)Fd._H;
         F._P = (float)Fd._P, F._rho = (float)Fd._rho, F.c2 = (float)Fd.c2, F.b1 = (float)Fd.b1;
         F.b3 = (float)Fd.b3, F.q2 = (float)Fd.q2, F._c = (float)Fd._c, F.b2 = (float)Fd.b2, F._c1 = (float)Fd._c1;
