@@ -124,6 +124,30 @@ __global__ void __launch_bounds__(kThreads) kb_faces_all(const Member *__restric
     }
 }
 
+// The mixed WENO5 face sweeps with registers fitted to XFG_FACES_MIXED_MINB resident blocks per
+// SM, as k_faces_mixed_w5 of the single-grid path (the other forms stay unbounded).
+template <int D>
+__global__ void __launch_bounds__(kThreads, XFG_FACES_MIXED_MINB)
+    kb_faces_m5(const Member *__restrict__ M, const int *__restrict__ off, int n, DevThermo th, int flag, int artificial) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    member_face<D, 5, true>(m, blockIdx.x - off[mi], th, flag, artificial);
+}
+__global__ void __launch_bounds__(kThreads, XFG_FACES_MIXED_MINB)
+    kb_faces_all_m5(const Member *__restrict__ M, const int *__restrict__ off, int n3, DevThermo th, int flag,
+                    int artificial) {
+    const int e = member_of_block(off, n3, blockIdx.x);
+    const Member &m = M[e / 3];
+    if (member_done(m)) return;
+    const int lb = blockIdx.x - off[e];
+    switch (e % 3) {
+    case 0: member_face<0, 5, true>(m, lb, th, flag, artificial); break;
+    case 1: member_face<1, 5, true>(m, lb, th, flag, artificial); break;
+    default: member_face<2, 5, true>(m, lb, th, flag, artificial); break;
+    }
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(kThreads) kb_div_rk(const Member *__restrict__ M, const int *__restrict__ off, int n, int flag) {
     const int mi = member_of_block(off, n, blockIdx.x);
@@ -403,7 +427,7 @@ void launch_step(xfg_ensemble *e) {
             const int *t = tab(e, PH_FALL);
             if (nb) {
                 if (mixed) {
-                    if (order5) kb_faces_all<5, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                    if (order5) kb_faces_all_m5<<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
                     else kb_faces_all<7, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
                 } else {
                     if (order5) kb_faces_all<5, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
@@ -415,7 +439,7 @@ void launch_step(xfg_ensemble *e) {
             if (e->nblk[PH]) {                                                                                     \
                 const int *t = tab(e, PH);                                                                         \
                 if (mixed) {                                                                                       \
-                    if (order5) kb_faces<D, 5, true><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);  \
+                    if (order5) kb_faces_m5<D><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);        \
                     else kb_faces<D, 7, true><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);         \
                 } else {                                                                                           \
                     if (order5) kb_faces<D, 5, false><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art); \

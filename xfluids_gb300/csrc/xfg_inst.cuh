@@ -48,7 +48,9 @@ struct Inst {
         const double *glf = c.glf ? c.glf + 3 * D : nullptr;
         (void)n;
         const dim3 grid = face_grid<D>(g), block(32, 4, 1);
-        if constexpr (MIXED)
+        if constexpr (MIXED && !COP && ORDER == 5)
+            k_faces_mixed_w5<D><<<grid, block, 0, c.st>>>(g, c.f, c.th, c.artificial, glf, guard);
+        else if constexpr (MIXED)
             k_faces_mixed<D, COP, NS, ORDER><<<grid, block, 0, c.st>>>(g, c.f, c.th, c.artificial, glf, guard);
         else
             k_faces<D, COP, NS, ORDER><<<grid, block, 0, c.st>>>(g, c.f, c.th, UI, c.artificial, glf, guard);

@@ -411,6 +411,22 @@ __global__ void __launch_bounds__(kThreads) k_faces_mixed(Geo g, DevFields f, De
     faces_mixed_body<D, COP, NS, ORDER>(g, f, th, artificial, glf_d, i, j, k);
 }
 
+// The single-gas WENO5 kernel with its registers fitted to XFG_FACES_MIXED_MINB resident blocks
+// per SM: 5 blocks of 128 threads give 96 registers (120 unbounded) and an 84-byte spill, measured
+// +2.7 % on the 4096^2 vortex. Other orders and the mixtures stay unbounded (a bound spilled them
+// more and cost the mixture kernels 2 %).
+#ifndef XFG_FACES_MIXED_MINB
+#define XFG_FACES_MIXED_MINB 5
+#endif
+template <int D>
+__global__ void __launch_bounds__(kThreads, XFG_FACES_MIXED_MINB)
+    k_faces_mixed_w5(Geo g, DevFields f, DevThermo th, int artificial, const double *__restrict__ glf_d, int guard) {
+    if (guard && step_done(f)) return;
+    int i, j, k;
+    if (!face_of_thread<D>(g, i, j, k)) return;
+    faces_mixed_body<D, false, 1, 5>(g, f, th, artificial, glf_d, i, j, k);
+}
+
 // Divergence of the FP32 face fluxes, accumulated into the FP64 state by the RK stage.
 // Positivity limiter of the mixed form: the FP32 physical and face fluxes, the FP64 state.
 template <int D, bool COP, int NS>
