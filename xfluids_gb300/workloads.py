@@ -1,6 +1,6 @@
 """Run one workload of the convective path on the GPU and print its rate (one JSON line).
 
-    python -m xfluids_gb300.workloads vortex   --size 1024 --steps 10 [--precision mixed]
+    python -m xfluids_gb300.workloads vortex   --size 1024 --steps 10 [--precision mixed] [--positivity]
     python -m xfluids_gb300.workloads sod      --size 1024 --steps 100
     python -m xfluids_gb300.workloads mixing   --shape 256 128 64 --steps 2 [--precision mixed] [--viscous]
     python -m xfluids_gb300.workloads ensemble --members 32 --steps 4 [--precision mixed]
@@ -73,6 +73,7 @@ def main(argv=None):
     ap.add_argument("--precision", choices=["fp64", "mixed", "strict"], default="fp64")
     ap.add_argument("--tables", default=DEFAULT_TABLES)
     ap.add_argument("--viscous", action="store_true", help="mixing: viscous, heat and diffusion fluxes")
+    ap.add_argument("--positivity", action="store_true", help="vortex / sod / mixing: positivity-preserving limiter")
     ap.add_argument("--transport", default=DEFAULT_TRANSPORT)
     ap.add_argument("--tune", action="store_true", help="ensemble: run the schedule autotuner first")
     ap.add_argument("--device", type=int, default=0)
@@ -88,13 +89,15 @@ def main(argv=None):
         else:
             th = thermo.load_thermal(cases.MIXING_SPECIES, 0, tables_json=a.tables)
             b, s, th, U, T = cases.mixing_layer(tuple(a.shape), thermal=th, precision=prec)
+        s.positivity = int(a.positivity)
         tr = None
         if a.viscous:
             if a.workload != "mixing":
                 raise SystemExit("--viscous needs a mixture (the mixing workload)")
             s.viscous, tr = 7, thermo.load_transport(a.transport)
         out = single_grid(b, s, th, U, T, a.steps, a.device, tr)
-    out.update({"workload": a.workload, "precision": a.precision, "viscous": bool(a.viscous)})
+    out.update({"workload": a.workload, "precision": a.precision, "viscous": bool(a.viscous),
+                "positivity": bool(a.positivity)})
     print(json.dumps(out))
     return 0
 
