@@ -230,7 +230,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     // layout of the pool
     size_t nd = 3 * E + 12 + (scheme->cop ? NS : 0);           // U, U1, LU, primitives, y
     if (scheme->cop) nd += 3 + (NS - 1);                        // per-cell sound-speed terms
-    if (scheme->viscous) nd += 9 + 2;                           // velocity derivatives, mu, kappa
+    if (scheme->viscous && !mixed) nd += 9 + 2;                 // velocity derivatives, mu, kappa
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;  // single-gas fast path extras
     if (fast1) nd += 2 + 3 * (block->DimX + block->DimY + block->DimZ);
     for (int d = 0; d < 3; d++)
@@ -238,6 +238,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     size_t nf = 0;
     if (mixed) {
         nf = E + 7;
+        if (scheme->viscous) nf += 9 + 2 + 1;                    // FP32 derivatives, mu, kappa, T
         for (int d = 0; d < 3; d++)
             if (dims[d]) nf += 2 * E;                             // Ff, Fwf
     }
@@ -262,7 +263,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     f.rho = take8(1), f.u = take8(1), f.v = take8(1), f.w = take8(1), f.p = take8(1), f.H = take8(1);
     f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
     if (scheme->cop) f.y = take8(NS), f.xc = take8(3 + (NS - 1));
-    if (scheme->viscous) f.vde = take8(9), f.mu = take8(1), f.kappa = take8(1);
+    if (scheme->viscous && !mixed) f.vde = take8(9), f.mu = take8(1), f.kappa = take8(1);
     if (fast1) {
         f.sr = take8(1), f.isr = take8(1);
         for (int d = 0; d < 3; d++)
@@ -273,6 +274,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     if (mixed) {
         f.Uf = take4(E);
         f.primf = take4(7);
+        if (scheme->viscous) f.vdef = take4(9), f.muf = take4(1), f.kappaf = take4(1), f.Tf = take4(1);
         for (int d = 0; d < 3; d++)
             if (dims[d]) f.Ff[d] = take4(E), f.Fwf[d] = take4(E);
     }

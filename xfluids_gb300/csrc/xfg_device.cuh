@@ -75,6 +75,7 @@ struct DevFields {
     double *eab[3];            // |u_d - c|, |u_d|, |u_d + c| per cell and direction (same path)
     double *vde;               // viscous: the 9 cell-centre velocity derivatives (ducx..dwcz)
     double *mu, *kappa;        // viscous: mixture viscosity and thermal conductivity per cell
+    float *vdef, *muf, *kappaf, *Tf;  // viscous, mixed form: FP32 derivatives, mu, kappa and T
     const double *tr;          // viscous: device transport table (see xfg_api.cu, pack_transport)
     const float *trf;          // viscous, mixed form: FP32 transport table (xfg_set_transport)
     double *xc;                // mixtures: per-cell terms of the interface sound speed (3 + NCOP

@@ -105,20 +105,27 @@ struct Inst {
             const Geo &g = c.g;
             const int heat = (c.viscous & 2) ? 1 : 0;
             const long long nd = (long long)(g.dimx ? g.Xi + 4 : 1) * (g.dimy ? g.Yi + 4 : 1) * (g.dimz ? g.Zi + 4 : 1);
-            k_vderiv<<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
-            if (g.dimx) k_vderiv_bc<0><<<grid_for((long long)g.Bx * g.Ymax * g.Zmax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
-            if (g.dimy) k_vderiv_bc<1><<<grid_for((long long)g.By * g.Xmax * g.Zmax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
-            if (g.dimz) k_vderiv_bc<2><<<grid_for((long long)g.Bz * g.Xmax * g.Ymax, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
-            if (MIXED)
+            const long long nb[3] = {(long long)g.Bx * g.Ymax * g.Zmax, (long long)g.By * g.Xmax * g.Zmax,
+                                     (long long)g.Bz * g.Xmax * g.Ymax};
+            if constexpr (MIXED) {  // FP32 derivatives, transport and fluxes
+                k_vderiv_f32<<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
+                if (g.dimx) k_vderiv_bc<0, float><<<grid_for(nb[0], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.vdef, guard);
+                if (g.dimy) k_vderiv_bc<1, float><<<grid_for(nb[1], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.vdef, guard);
+                if (g.dimz) k_vderiv_bc<2, float><<<grid_for(nb[2], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.vdef, guard);
                 k_transport_f32<NS><<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, heat, guard);
-            else
+            } else {
+                k_vderiv<<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, guard);
+                if (g.dimx) k_vderiv_bc<0, double><<<grid_for(nb[0], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.vde, guard);
+                if (g.dimy) k_vderiv_bc<1, double><<<grid_for(nb[1], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.vde, guard);
+                if (g.dimz) k_vderiv_bc<2, double><<<grid_for(nb[2], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.vde, guard);
                 k_transport<NS><<<grid_for(nd, kThreads), kThreads, 0, c.st>>>(g, c.f, c.th, heat, guard);
+            }
             const long long nf[3] = {(long long)(g.Xi + 1) * g.Yi * g.Zi, (long long)g.Xi * (g.Yi + 1) * g.Zi,
                                      (long long)g.Xi * g.Yi * (g.Zi + 1)};
-            if (MIXED) {
-                if (g.dimx) k_visc<0, E, float><<<grid_for(nf[0], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fwf[0], heat, guard);
-                if (g.dimy) k_visc<1, E, float><<<grid_for(nf[1], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fwf[1], heat, guard);
-                if (g.dimz) k_visc<2, E, float><<<grid_for(nf[2], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fwf[2], heat, guard);
+            if constexpr (MIXED) {
+                if (g.dimx) k_visc_f32<0, E><<<grid_for(nf[0], kThreads), kThreads, 0, c.st>>>(g, c.f, heat, guard);
+                if (g.dimy) k_visc_f32<1, E><<<grid_for(nf[1], kThreads), kThreads, 0, c.st>>>(g, c.f, heat, guard);
+                if (g.dimz) k_visc_f32<2, E><<<grid_for(nf[2], kThreads), kThreads, 0, c.st>>>(g, c.f, heat, guard);
             } else {
                 if (g.dimx) k_visc<0, E, double><<<grid_for(nf[0], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fw[0], heat, guard);
                 if (g.dimy) k_visc<1, E, double><<<grid_for(nf[1], kThreads), kThreads, 0, c.st>>>(g, c.f, c.f.Fw[1], heat, guard);

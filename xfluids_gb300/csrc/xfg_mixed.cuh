@@ -148,6 +148,7 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             const double cd = sqrt(gamma * pd * rho1);
             f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd, f.c[id] = cd;
             f.e[id] = tme, f.gamma[id] = gamma, f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
+            if (f.Tf) f.Tf[id] = (float)T;  // viscous schemes: the heat flux's FP32 temperature
             if (f.xc) cop_cell_terms<NS>(th, yi, T, Cp, ud, vd, wd, Hd, pd, rhod, f.xc, P, id);
 #pragma unroll
             for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = (float)yi[s];

@@ -58,9 +58,37 @@ static __global__ void __launch_bounds__(kThreads) k_vderiv(Geo g, DevFields f, 
         }
 }
 
+// The mixed form's derivatives: the same fourth-order differences in FP32 from the form's FP32
+// velocities (primf components 1..3), written as FP32.
+static __global__ void __launch_bounds__(kThreads) k_vderiv_f32(Geo g, DevFields f, int guard) {
+    if (guard && step_done(f)) return;
+    const int r0[3] = {g.dimx ? g.Bx - 2 : 0, g.dimy ? g.By - 2 : 0, g.dimz ? g.Bz - 2 : 0};
+    const int nx = g.dimx ? g.Xi + 4 : 1, ny = g.dimy ? g.Yi + 4 : 1, nz = g.dimz ? g.Zi + 4 : 1;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nx * ny * nz) return;
+    const int i = (int)(t % nx) + r0[0];
+    const long long r = t / nx;
+    const int j = (int)(r % ny) + r0[1], k = (int)(r / ny) + r0[2];
+    const long long P = g.pitch, id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    const long long st[3] = {1, (long long)g.Xmax, (long long)g.Xmax * g.Ymax};
+    const int dims[3] = {g.dimx, g.dimy, g.dimz};
+    const float inv[3] = {(float)(g._dx * kVTwle), (float)(g._dy * kVTwle), (float)(g._dz * kVTwle)};
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float val = 0.f;
+            if (dims[d] && (c == d || dims[c])) {
+                const float *q = f.primf + (1 + c) * P;
+                val = (8.f * (q[id + st[d]] - q[id - st[d]]) - (q[id + 2 * st[d]] - q[id - 2 * st[d]])) * inv[d];
+            }
+            f.vdef[(3 * d + c) * P + id] = val;
+        }
+}
+
 // ghost layers of direction D: the four derivative components its flux reads
-template <int D>
-__global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, int guard) {
+template <int D, class VT>
+__global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, VT *__restrict__ vde, int guard) {
     if (guard && step_done(f)) return;
     const int bw = D == 0 ? g.Bx : (D == 1 ? g.By : g.Bz);
     const int inner = D == 0 ? g.Xi : (D == 1 ? g.Yi : g.Zi);
@@ -99,15 +127,15 @@ __global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, int 
             break;
         case XFG_INFLOW:
 #pragma unroll
-            for (int m = 0; m < 4; m++) f.vde[comps[m] * P + id] = 0.0;
+            for (int m = 0; m < 4; m++) vde[comps[m] * P + id] = VT(0);
             break;
         default: break;
         }
         if (src >= 0)
 #pragma unroll
             for (int m = 0; m < 4; m++) {
-                const double v = f.vde[comps[m] * P + src];
-                f.vde[comps[m] * P + id] = neg ? -v : v;
+                const VT v = vde[comps[m] * P + src];
+                vde[comps[m] * P + id] = neg ? -v : v;
             }
     }
 }
@@ -172,7 +200,7 @@ __global__ void __launch_bounds__(kThreads) k_transport(Geo g, DevFields f, DevT
 
 // The mixed form's transport: the same sums in FP32 (mu and kappa to ~1e-6 relative; the fits lose
 // about one decade to cancellation), from the FP32 table trf (species resolved, PHI's constant
-// 0.5 / sqrt(2) folded into wb).
+// 0.5 / sqrt(2) folded into wb), written as FP32 for k_visc_f32.
 template <int NS>
 __global__ void __launch_bounds__(kThreads) k_transport_f32(Geo g, DevFields f, DevThermo th, int heat, int guard) {
     if (guard && step_done(f)) return;
@@ -219,8 +247,8 @@ __global__ void __launch_bounds__(kThreads) k_transport_f32(Geo g, DevFields f, 
             kap += X[k] * expf(((c[3] * lT + c[2]) * lT + c[1]) * lT + c[0]) * _den;
         }
     }
-    f.mu[id] = (double)mu;
-    if (heat) f.kappa[id] = (double)kap;
+    f.muf[id] = mu;
+    if (heat) f.kappaf[id] = kap;
 }
 
 // viscous stress and heat-conduction flux at the faces i+1/2 of direction D, subtracted from the
@@ -274,6 +302,56 @@ __global__ void __launch_bounds__(kThreads) k_visc(Geo g, DevFields f, FT *__res
     Fw[3 * P + id] = (FT)((double)Fw[3 * P + id] - fv[2]);
     Fw[4 * P + id] = (FT)((double)Fw[4 * P + id] - F4);
     // component 0 and the species: minus zero (the reference subtracts 0.0 and the zero diffusion)
+}
+
+// The mixed form's viscous and heat-conduction face flux: k_visc's terms in FP32 from the form's
+// FP32 velocities (primf), derivatives, mu, kappa and T, subtracted from the FP32 face fluxes.
+// FP32 rounding of u (~6e-8 |u|) moves the stress by far less than the FP32 convective flux's own
+// rounding.
+template <int D, int E>
+__global__ void __launch_bounds__(kThreads) k_visc_f32(Geo g, DevFields f, int heat, int guard) {
+    if (guard && step_done(f)) return;
+    const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)nfx * nfy * nfz) return;
+    const int i = (int)(t % nfx) + g.Bx - (D == 0 ? 1 : 0);
+    const long long r = t / nfx;
+    const int j = (int)(r % nfy) + g.By - (D == 1 ? 1 : 0), k = (int)(r / nfy) + g.Bz - (D == 2 ? 1 : 0);
+    const long long P = g.pitch, id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
+    const long long st = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
+    const long long m1 = id - st, p1 = id + st, p2 = id + 2 * st;
+    const float _dl24 = (float)((D == 0 ? g._dx : (D == 1 ? g._dy : g._dz)) * kVTwfr);
+    const float dt[3] = {(float)g.dimx, (float)g.dimy, (float)g.dimz};
+    const float *vel[3] = {f.primf + P, f.primf + 2 * P, f.primf + 3 * P};
+    constexpr float s16 = (float)kVSxtn;
+    auto half = [&](const float *a) { return (9.f * (a[p1] + a[id]) - (a[p2] + a[m1])) * s16; };
+    auto b27 = [&](const float *a) { return 27.f * (a[p1] - a[id]) - (a[p2] - a[m1]); };
+    auto vh = [&](int c) {  // 16 x the face value of derivative component c
+        const float *a = f.vdef + c * P;
+        return 9.f * (a[p1] + a[id]) - (a[p2] + a[m1]);
+    };
+    const float mue = half(f.muf);
+    const float lamada = -2.f * (float)kOT * mue;
+    float fv[3], hv[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        if (c == D) {
+            const int oa = c == 0 ? V_DVCY : V_DUCX, ob = c == 2 ? V_DVCY : V_DWCZ;
+            fv[c] = (2.f * mue + lamada) * b27(vel[c]) * _dl24 + lamada * (vh(oa) + vh(ob)) * s16;
+            hv[c] = half(vel[c]);
+        } else {
+            const int cr = 3 * c + D;  // derivative of u_D along x_c
+            fv[c] = (mue * b27(vel[c]) * _dl24 + mue * vh(cr) * s16) * dt[c];
+            hv[c] = half(vel[c]) * dt[c];
+        }
+    }
+    float F4 = fv[0] * hv[0] + fv[1] * hv[1] + fv[2] * hv[2];
+    if (heat) F4 += half(f.kappaf) * b27(f.Tf) * _dl24;
+    float *Fw = f.Fwf[D];
+    Fw[1 * P + id] -= fv[0];
+    Fw[2 * P + id] -= fv[1];
+    Fw[3 * P + id] -= fv[2];
+    Fw[4 * P + id] -= F4;
 }
 
 }  // namespace XFG_KNS
