@@ -81,8 +81,7 @@ def test_ensemble_rejects_unsupported_schemes_before_touching_a_device(cuda_lib)
     """xfg_ensemble_create checks the scheme first (no device call is made for these)."""
     from xfluids_gb300.ensemble import Ensemble
     from xfluids_gb300.mesh import make_scheme
-    for kw in (dict(cop=True, num_species=2), dict(artificial_type=abi.GLF), dict(precision=2),
-               dict(scheme_order=6), dict(viscous=1)):
+    for kw in (dict(cop=True, num_species=2), dict(precision=2), dict(scheme_order=8), dict(viscous=1)):
         visc = kw.pop("viscous", 0)
         sc = make_scheme(**{"scheme_order": 5, "artificial_type": abi.LLF, **kw})
         sc.viscous = visc

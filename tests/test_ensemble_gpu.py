@@ -10,7 +10,7 @@ import pytest
 
 from helpers import PARITY_TOL, blast3d, normwise, riemann_small, sod_like
 from xfluids_gb300 import cases
-from xfluids_gb300.abi import LLF, PERIODIC, ROE
+from xfluids_gb300.abi import GLF, LLF, PERIODIC, ROE
 from xfluids_gb300.ensemble import Ensemble
 from xfluids_gb300.fluid import Fluid
 from xfluids_gb300.mesh import empty_thermal, make_scheme
@@ -51,7 +51,8 @@ def pool_for(blocks, precision, extra=0):
 
 
 @pytest.mark.parametrize("order,art,prec", [(5, LLF, FP64), (7, ROE, FP64), (5, ROE, FP64), (5, LLF, MIXED),
-                                            (7, LLF, MIXED)])
+                                            (7, LLF, MIXED), (6, LLF, FP64), (6, ROE, MIXED), (5, GLF, FP64),
+                                            (7, GLF, FP64), (5, GLF, MIXED)])
 def test_members_equal_single_grid_runs(cuda_lib, order, art, prec):
     scheme = make_scheme(cop=False, scheme_order=order, artificial_type=art, precision=prec)
     ms = members()

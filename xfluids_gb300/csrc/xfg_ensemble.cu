@@ -38,6 +38,7 @@ struct Member {
     int bc[6];
     int active;
     int ltx;  // face tile of this member: 2^ltx faces along x by kThreads >> ltx across
+    unsigned long long *glf;  // GLF running maxima (9 words in the member's small-word area)
 };
 
 // phases with a block table; PH_FALL holds three entries per member (x, y, z face sweeps of the
@@ -93,10 +94,11 @@ __device__ __forceinline__ void member_face(const Member &m, int lb, const DevTh
     const int bx = lb % gd.x, by = (lb / gd.x) % gd.y, bz = lb / (gd.x * gd.y);
     int i, j, k;
     if (!face_of_tile<D>(m.g, bx, by, bz, m.ltx, i, j, k)) return;
+    const double *glf = artificial == XFG_GLF ? (const double *)m.glf + 3 * D : nullptr;
     if (MIXED)
-        faces_mixed_body<D, false, 1, ORDER>(m.g, m.f, th, artificial, nullptr, i, j, k);
+        faces_mixed_body<D, false, 1, ORDER>(m.g, m.f, th, artificial, glf, i, j, k);
     else
-        faces_body<D, false, 1, ORDER>(m.g, m.f, th, flag == 1 || flag == 0 ? m.f.U : m.f.U1, artificial, nullptr, i, j, k);
+        faces_body<D, false, 1, ORDER>(m.g, m.f, th, flag == 1 || flag == 0 ? m.f.U : m.f.U1, artificial, glf, i, j, k);
 }
 
 // one face sweep (direction D) of every member
@@ -184,6 +186,34 @@ __global__ void __launch_bounds__(kThreads) kb_pp(const Member *__restrict__ M, 
             else if (d == 1) pp_body<1, 5, 0, double>(m.g, UI, m.f.F[1], m.f.Fw[1], l0, m.cfl / l0, t);
             else pp_body<2, 5, 0, double>(m.g, UI, m.f.F[2], m.f.Fw[2], l0, m.cfl / l0, t);
         }
+    }
+}
+
+// GLF maxima (ConVenction_block.hpp:115-215) of every member, folded into its running maxima as
+// k_glf / k_glf_mixed do for a single grid: |u_d - c|, |u_d|, |u_d + c| over all cells
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_glf(const Member *__restrict__ M, const int *__restrict__ off, int n) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    const long long id = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    const long long N = m.g.ncell(), P = m.g.pitch;
+    double mx[9];
+    for (int q = 0; q < 9; q++) mx[q] = 0.0;
+    if (id < N) {
+        const double c = MIXED ? (double)m.f.primf[6 * P + id] : m.f.c[id];
+        for (int d = 0; d < 3; d++) {
+            const double v = MIXED ? (double)m.f.primf[(1 + d) * P + id] : (d == 0 ? m.f.u[id] : (d == 1 ? m.f.v[id] : m.f.w[id]));
+            mx[3 * d + 0] = fabs(v - c);
+            mx[3 * d + 1] = fabs(v);
+            mx[3 * d + 2] = fabs(v + c);
+        }
+    }
+    // a block belongs to one member, so a warp's maxima are one member's
+    for (int q = 0; q < 9; q++) {
+        double x = mx[q];
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&m.glf[q], x);
     }
 }
 
@@ -331,6 +361,7 @@ void carve(Member &m, char *base, const xfg_block &b, bool mixed) {
             if (dims[d]) f.Ff[d] = t4(5), f.Fwf[d] = t4(5);
     }
     f.lam = (unsigned long long *)p;
+    m.glf = (unsigned long long *)(p + 64);
     Geo &g = m.g;
     g.Xmax = b.Xmax, g.Ymax = b.Ymax, g.Zmax = b.Zmax, g.Xi = b.X_inner, g.Yi = b.Y_inner, g.Zi = b.Z_inner;
     g.Bx = b.Bwidth_X, g.By = b.Bwidth_Y, g.Bz = b.Bwidth_Z, g.dimx = b.DimX, g.dimy = b.DimY, g.dimz = b.DimZ;
@@ -412,7 +443,7 @@ void launch_step(xfg_ensemble *e) {
     const int n = (int)e->order.size();
     if (!n) return;
     const bool mixed = e->sc.precision == XFG_MIXED;
-    const int order5 = e->sc.scheme_order == 5;
+    const int order = e->sc.scheme_order;
     cudaStream_t st = e->st;
     kb_dt<<<(n + 127) / 128, 128, 0, st>>>(e->dm, n);
     for (int flag = 1; flag <= 3; flag++) {
@@ -422,15 +453,21 @@ void launch_step(xfg_ensemble *e) {
         if (mixed) kb_states<true><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
         else kb_states<false><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
         const int art = e->sc.artificial_type;
+        if (art == XFG_GLF) {
+            if (mixed) kb_glf<true><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n);
+            else kb_glf<false><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n);
+        }
         if (e->fused_faces) {
             const int nb = e->nblk[PH_FALL];
             const int *t = tab(e, PH_FALL);
             if (nb) {
                 if (mixed) {
-                    if (order5) kb_faces_all_m5<<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                    if (order == 5) kb_faces_all_m5<<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                    else if (order == 6) kb_faces_all<6, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
                     else kb_faces_all<7, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
                 } else {
-                    if (order5) kb_faces_all<5, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                    if (order == 5) kb_faces_all<5, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
+                    else if (order == 6) kb_faces_all<6, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
                     else kb_faces_all<7, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
                 }
             }
@@ -438,12 +475,15 @@ void launch_step(xfg_ensemble *e) {
 #define XFG_FACES(D, PH)                                                                                           \
             if (e->nblk[PH]) {                                                                                     \
                 const int *t = tab(e, PH);                                                                         \
+                const unsigned nb = e->nblk[PH];                                                                   \
                 if (mixed) {                                                                                       \
-                    if (order5) kb_faces_m5<D><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);        \
-                    else kb_faces<D, 7, true><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);         \
+                    if (order == 5) kb_faces_m5<D><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);         \
+                    else if (order == 6) kb_faces<D, 6, true><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art); \
+                    else kb_faces<D, 7, true><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);             \
                 } else {                                                                                           \
-                    if (order5) kb_faces<D, 5, false><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art); \
-                    else kb_faces<D, 7, false><<<e->nblk[PH], kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);        \
+                    if (order == 5) kb_faces<D, 5, false><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);  \
+                    else if (order == 6) kb_faces<D, 6, false><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art); \
+                    else kb_faces<D, 7, false><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);            \
                 }                                                                                                  \
             }
             XFG_FACES(0, PH_F0)
@@ -471,10 +511,9 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
     if (scheme->cop) return efail(-1, "the ensemble engine serves single-gas members (cop = 0)%s");
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_MIXED)
         return efail(-1, "ensemble precision must be XFG_FP64 or XFG_MIXED%s");
-    if (scheme->artificial_type == XFG_GLF) return efail(-1, "the ensemble engine supports Roe and LLF splitting%s");
     if (scheme->positivity != 0 && scheme->positivity != 1) return efail(-1, "positivity must be 0 or 1%s");
     if (scheme->viscous) return efail(-1, "the ensemble engine serves inviscid single-gas members%s");
-    if (scheme->scheme_order != 5 && scheme->scheme_order != 7) return efail(-1, "scheme_order must be 5 or 7%s");
+    if (scheme->scheme_order < 5 || scheme->scheme_order > 7) return efail(-1, "scheme_order must be 5, 6 or 7%s");
     ECK(cudaSetDevice(device));
     xfg_ensemble *e = new xfg_ensemble();
     e->device = device, e->sc = *scheme, e->capacity = capacity;
