@@ -244,8 +244,9 @@ int xfg_checkpoint_read(xfg_handle *h, const char *path, int *step, double *time
 typedef struct xfg_ensemble xfg_ensemble;
 
 /* Create an ensemble with `capacity` member slots and a device pool of pool_bytes from which the
- * members are sub-allocated (admission by HBM budget). scheme: single gas (cop = 0), ROE or LLF,
- * WENO5/7, precision XFG_FP64 or XFG_MIXED. */
+ * members are sub-allocated (admission by HBM budget). scheme: single gas (cop = 0), inviscid,
+ * ROE, LLF or GLF (running maxima per member), WENO5 / WENO-CU6 / WENO7, positivity limiter on or
+ * off, precision XFG_FP64 or XFG_MIXED. */
 int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *scheme, const xfg_thermal *thermal,
                         int device, xfg_ensemble **out);
 int xfg_ensemble_destroy(xfg_ensemble *e);
