@@ -119,3 +119,37 @@ def test_random_case_matches_oracle(seed, precision, cuda_lib):
     worst = run_stagewise((b, s, th, U, T), steps=2, precision=precision)
     print(f"seed {seed}: dims {b.DimX}{b.DimY}{b.DimZ} cop {s.cop} order {s.scheme_order} art {s.artificial_type} "
           f"pos {s.positivity} bc {list(b.Boundarys)}: worst {worst:.2e}")
+
+
+def _advance(case, precision, steps):
+    from xfluids_gb300.fluid import Fluid
+    b, s, th, U, T = case
+    s.precision = precision
+    f = Fluid(b, s, th)
+    try:
+        f.InitialU(U, T)
+        f.initialize()
+        st, t, n = f.advance(steps)
+        assert st == 0 and n == steps, (st, n)
+        return H.inner_aos(b, f.get("U"), s.Emax), t
+    finally:
+        f.close()
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_case_mixed_close_to_fp64(seed, cuda_lib):
+    """The mixed form on the same random cases: L1 of the state after 2 steps against the FP64
+    form, per component over its state scale (density for the density and the species, the mean
+    momentum magnitude for the momenta, the mean energy), within 1e-5."""
+    from xfluids_gb300.abi import MIXED
+    case = random_case(seed)
+    ref, t64 = _advance(case, FP64, 2)
+    got, tmx = _advance(random_case(seed), MIXED, 2)
+    assert abs(tmx - t64) <= 1e-5 * t64
+    d = np.abs(got - ref).mean(axis=0)
+    rho = np.abs(ref[:, 0]).mean()
+    mom = np.sqrt((ref[:, 1:4] ** 2).sum(axis=1)).mean()
+    scale = np.array([rho, mom, mom, mom, np.abs(ref[:, 4]).mean()] + [rho] * (ref.shape[1] - 5))
+    rel = d / scale
+    print(f"seed {seed}: mixed vs FP64 state-scaled L1 {rel.max():.2e}")
+    assert np.all(rel <= 1e-5), rel
