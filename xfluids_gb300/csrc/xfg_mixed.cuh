@@ -358,6 +358,12 @@ __device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &
     float acc[E];
 #pragma unroll
     for (int n = 0; n < E; n++) {
+        // Mixtures across the sweep (strided stencil): the stencil addresses are the same for every
+        // field, and computed once they would stay live through the field loop (8 points x E
+        // components x 2 arrays of 64-bit addresses, 255 registers). An opaque copy of the stride
+        // per field makes them cheap integer work recomputed per field instead.
+        long long stride_n = stride;
+        if constexpr (!PRELOAD && D != 0) asm volatile("mov.b64 %0, %0;" : "+l"(stride_n));
         const float ev = n == 0 ? fabsf(un - F._c) : (n == E - 1 ? fabsf(un + F._c) : fabsf(un));
         float av;
         if (artificial == XFG_ROE || ORDER == 7) {
@@ -379,7 +385,7 @@ __device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &
                 uf = project_r<D, E>(lrow, n, Us[m - M0]);
                 ff = project_r<D, E>(lrow, n, Fs[m - M0]);
             } else {
-                const long long q = idl + m * stride;
+                const long long q = idl + m * stride_n;
                 uf = project_f<D, E>(lrow, n, Ua, P, q);
                 ff = project_f<D, E>(lrow, n, Fl, P, q);
             }
