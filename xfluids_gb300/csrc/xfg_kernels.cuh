@@ -703,6 +703,10 @@ __device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, con
     double acc[E];
 #pragma unroll
     for (int n = 0; n < E; n++) {
+        // mixtures across the sweep: an opaque copy of the stride per field keeps the strided
+        // stencil addresses (the same for every field) from being computed once and held live
+        long long stride_n = stride;
+        if constexpr (COP && D != 0) asm volatile("mov.b64 %0, %0;" : "+l"(stride_n));
         const double ev = n == 0 ? fabs(un - F._c) : (n == E - 1 ? fabs(un + F._c) : fabs(un));
         double av;
         if (artificial == XFG_ROE || ORDER == 7) {
@@ -720,7 +724,7 @@ __device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, con
         const double hav = 0.5 * av;
 #pragma unroll
         for (int m = M0; m <= M1; m++) {
-            const long long q = idl + m * stride;
+            const long long q = idl + m * stride_n;
             const double uf = project<D, E>(lrow, n, UI, P, q);
             const double ff = project<D, E>(lrow, n, Fl, P, q);
             if constexpr (FAST_BUILD) {  // 0.5 (ff +- av uf) with one rounding, as the contracted form
