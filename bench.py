@@ -28,9 +28,9 @@ import numpy as np  # noqa: E402
 # DRAM bytes per face of the FP64 x-face kernel measured by ncu on a small case, scaled per face
 # (profiles/k_faces_fp64_vortex.md); None until a capture exists.
 THERMO_JSON = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "thermo_tables.json")
-# fitted transport coefficients of H2/O2/N2/H2O/AR (the reference's viscfit output, kept in a fixture)
-TRANSPORT_NPZ = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
-                             "visc_mixing5_12x8x6_janaf_w5.npz")
+# Lennard-Jones data and collision integrals of runtime.dat for the transport fits of the mixture
+TRANSPORT_TABLES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                                "transport_tables.json")
 # DRAM bytes per face of the FP64 x-face kernel: 674.2 MB read + 152.8 MB written in one ncu
 # capture of the 2048^2 vortex (4.196 M faces); traffic grows with the faces of a launch
 NCU_FACE_BYTES_FP64 = (674.218496e6 + 152.813568e6) / (2049 * 2048)
@@ -286,7 +286,9 @@ def bench_mixing_layer(args, local, steps):
     th = thermo.load_thermal(cases_mod().MIXING_SPECIES, 0, tables_json=THERMO_JSON)
     b, s, th, U, T = cases_mod().mixing_layer((512, 256, 256), thermal=th)
     res, states = {}, {}
-    tr = thermo.load_transport(TRANSPORT_NPZ)
+    from xfluids_gb300 import transport
+    tr = transport.fit_transport(cases_mod().MIXING_SPECIES, th, 0, tables_json=TRANSPORT_TABLES,
+                                 inv_spacing=(b._dx, b._dy, b._dz))
     for prec, visc in ((0, 0), (MIXED, 0), (2, 0), (0, 7), (MIXED, 7)):
         s.precision, s.viscous = prec, visc
         f = Fluid(b, s, th, device=local)

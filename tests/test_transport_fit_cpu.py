@@ -1,0 +1,47 @@
+"""The transport fits of xfluids_gb300.transport (a restatement of Setup::GetFitCoefficient,
+src/read_ini/src/viscfit.cpp:148-196) against the fitted data the reference produced for the
+viscous golden fixtures: bit for bit, every coefficient, including the H2 fits whose 3000 K node
+reads past the reference's T_star table."""
+import os
+
+import numpy as np
+import pytest
+
+import helpers as H
+from xfluids_gb300 import cases, transport
+
+TABLES = os.path.join(H.GOLDEN, "transport_tables.json")
+
+
+@pytest.mark.parametrize("name", ["visc_mixing5_12x8x6_janaf_w5", "visc_mixing5_16x12_janaf_w5"])
+def test_fit_matches_reference_fixture_bitwise(name):
+    z = np.load(os.path.join(H.GOLDEN, name + ".npz"))
+    th = H.thermal(cases.MIXING_SPECIES, 0)
+    ref = H.transport_of(z)
+    inv = (ref.yil_limiter,)  # max(1/dx, 1/dy, 1/dz) x clamp(1e10, 0, 1) = max(1/d)
+    tr = transport.fit_transport(cases.MIXING_SPECIES, th, 0, tables_json=TABLES, inv_spacing=inv)
+    ns = 5
+    for field, n in (("visc", ns * 4), ("therm", ns * 4), ("dkj", ns * ns * 4), ("species_chara", ns * 9)):
+        got = np.array(list(getattr(tr, field))[:n])
+        want = np.array(list(getattr(ref, field))[:n])
+        assert np.array_equal(got, want), (field, np.nonzero(got != want))
+    assert (tr.yil_limiter, tr.dim_limiter) == (ref.yil_limiter, ref.dim_limiter)
+
+
+def test_fit_from_runtime_dat_equals_fit_from_tables():
+    rt = os.path.join(os.environ.get("XF_REFERENCE", "/root/reference"), "runtime.dat")
+    if not os.path.isdir(rt):
+        pytest.skip("reference runtime.dat not present")
+    th = H.thermal(cases.MIXING_SPECIES, 1)
+    a = transport.fit_transport(cases.MIXING_SPECIES, th, 1, runtime_dir=rt, inv_spacing=(100.0,))
+    b = transport.fit_transport(cases.MIXING_SPECIES, th, 1, tables_json=TABLES, inv_spacing=(100.0,))
+    assert bytes(a) == bytes(b)
+
+
+def test_least_squares_recovers_an_exact_cubic():
+    xs = [1.0, 2.0, 3.0, 4.5, 5.0, 7.0]
+    coef = [0.5, -1.25, 0.75, -0.0625]
+    AA = [[x ** j for j in range(4)] for x in xs]
+    b = [sum(c * x ** j for j, c in enumerate(coef)) for x in xs]
+    got = transport._solve_overdetermined(AA, b)
+    assert np.allclose(got, coef, rtol=1e-10, atol=1e-10)

@@ -8,8 +8,8 @@
 Each run: initial state on the host, one warm-up step (captures the step graph), a reset to the
 initial state, then the timed steps (CUDA events around the graph replays). The mixing layer reads
 the thermo tables from a tables JSON (thermo.dump_tables), by default the one under tests/golden;
-with --viscous it adds viscous stress, heat conduction and species diffusion with the fitted
-transport data of an .npz (thermo.load_transport), by default the viscous golden fixture's.
+with --viscous it adds viscous stress, heat conduction and species diffusion with transport data
+fitted by transport.fit_transport from a tables JSON, by default the one under tests/golden.
 """
 from __future__ import annotations
 
@@ -22,7 +22,7 @@ from .abi import MIXED
 
 _GOLDEN = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden")
 DEFAULT_TABLES = os.path.join(_GOLDEN, "thermo_tables.json")
-DEFAULT_TRANSPORT = os.path.join(_GOLDEN, "visc_mixing5_12x8x6_janaf_w5.npz")
+DEFAULT_TRANSPORT_TABLES = os.path.join(_GOLDEN, "transport_tables.json")
 
 
 def single_grid(b, s, th, U, T, steps, device=0, transport=None):
@@ -74,7 +74,8 @@ def main(argv=None):
     ap.add_argument("--tables", default=DEFAULT_TABLES)
     ap.add_argument("--viscous", action="store_true", help="mixing: viscous, heat and diffusion fluxes")
     ap.add_argument("--positivity", action="store_true", help="vortex / sod / mixing: positivity-preserving limiter")
-    ap.add_argument("--transport", default=DEFAULT_TRANSPORT)
+    ap.add_argument("--transport-tables", default=DEFAULT_TRANSPORT_TABLES,
+                    help="Lennard-Jones rows and collision integrals (transport.dump_transport_tables)")
     ap.add_argument("--tune", action="store_true", help="ensemble: run the schedule autotuner first")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
@@ -94,7 +95,10 @@ def main(argv=None):
         if a.viscous:
             if a.workload != "mixing":
                 raise SystemExit("--viscous needs a mixture (the mixing workload)")
-            s.viscous, tr = 7, thermo.load_transport(a.transport)
+            from . import transport
+            s.viscous = 7
+            tr = transport.fit_transport(cases.MIXING_SPECIES, th, 0, tables_json=a.transport_tables,
+                                         inv_spacing=(b._dx, b._dy, b._dz))
         out = single_grid(b, s, th, U, T, a.steps, a.device, tr)
     out.update({"workload": a.workload, "precision": a.precision, "viscous": bool(a.viscous),
                 "positivity": bool(a.positivity)})
