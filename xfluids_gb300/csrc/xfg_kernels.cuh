@@ -429,11 +429,13 @@ __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, con
         const double _dpdrho_new = pa<Q>(_dpdrho, pm<Q>(pm<Q>(pm<Q>(_dpdrho, _dpdrho), drho), temp));
         const double csqr = pa<Q>(pa<Q>(_dpdrho_new, pm<Q>(_dpdE_new, _prho)), SY);
         F.b1 = _dpdE_new / csqr;
+        // the mixed form (PIN = false) divides by dp/dE once: z_n = -d_n (1 / dp/dE)
+        const double inv_dpdE = PIN ? 0.0 : 1.0 / _dpdE_new;
         double b3 = 0.0;
 #pragma unroll
         for (int n = 0; n < NCOP; n++) {
             const double dn = pa<Q>(dpdrhoi[n], pm<Q>(pm<Q>(pm<Q>(dpdrhoi[n], dpdrhoi[n]), drhoi[n]), temp));
-            F.z[n] = -dn / _dpdE_new;
+            F.z[n] = PIN ? -dn / _dpdE_new : -dn * inv_dpdE;
             b3 = pa<Q>(b3, pm<Q>(F._yi[n], F.z[n]));
         }
         F.b3 = pm<Q>(b3, F.b1);
@@ -443,7 +445,7 @@ __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, con
         F._c = sqrt(F.c2);
         F.b2 = ps<Q>(pa<Q>(1.0, pm<Q>(F.b1, F.q2)), pm<Q>(F.b1, F._H));
         F._c1 = 1.0 / F._c;
-        F.ent0 = ps<Q>(ps<Q>(1.0, F.b2), F.b3) / F.b1;
+        F.ent0 = PIN ? ps<Q>(ps<Q>(1.0, F.b2), F.b3) / F.b1 : ((1.0 - F.b2) - F.b3) * (csqr * inv_dpdE);
     }
 }
 
