@@ -23,7 +23,7 @@ namespace XFG_KNS {
 // mathematics as the reference's sums, different rounding: the mixed form only.
 template <int NS>
 struct FoldedThermo {
-    double A[7], B;
+    double A[7], Hs[7], B;  // Cp coefficients; enthalpy coefficients A_c / (power of T they multiply)
     int rg = -9;
     __device__ __forceinline__ bool fold(const DevThermo &t, const double *yi, double T) {
         const int r = t.nasa ? nasa_range(T) : (T > 1000.0 ? 0 : 1);
@@ -41,6 +41,12 @@ struct FoldedThermo {
             for (int c = 0; c < 7; c++) A[c] = fma(w, a[3 * c], A[c]);
             B = fma(w, t.nasa ? t.Hib[n * 6 + r] : a[15], B);
         }
+        if (t.nasa) {
+            Hs[0] = A[0], Hs[1] = A[1], Hs[2] = A[2], Hs[3] = A[3] * 0.5, Hs[4] = A[4] * kOT;
+            Hs[5] = A[5] * 0.25, Hs[6] = A[6] * 0.2;
+        } else {
+            Hs[0] = A[0], Hs[1] = A[1] * 0.5, Hs[2] = A[2] * kOT, Hs[3] = A[3] * 0.25, Hs[4] = A[4] * 0.2;
+        }
         return true;
     }
     // h and Cp of the mixture at T >= 200 K within the folded range
@@ -48,16 +54,34 @@ struct FoldedThermo {
         if (nasa) {
             const double iT = 1.0 / T;
             Cp = fma(fma(A[0], iT, A[1]), iT, fma(fma(fma(fma(A[6], T, A[5]), T, A[4]), T, A[3]), T, A[2]));
-            h = fma(-A[0], iT, fma(A[1], log(T),
-                                   fma(fma(fma(fma(fma(A[6] * 0.2, T, A[5] * 0.25), T, A[4] * kOT), T, A[3] * 0.5), T,
-                                           A[2]),
-                                       T, B)));
+            h = fma(-Hs[0], iT, fma(Hs[1], log(T), fma(fma(fma(fma(fma(Hs[6], T, Hs[5]), T, Hs[4]), T, Hs[3]), T, Hs[2]), T, B)));
         } else {
             Cp = fma(fma(fma(fma(A[4], T, A[3]), T, A[2]), T, A[1]), T, A[0]);
-            h = fma(fma(fma(fma(fma(A[4] * 0.2, T, A[3] * 0.25), T, A[2] * kOT), T, A[1] * 0.5), T, A[0]), T, B);
+            h = fma(fma(fma(fma(fma(Hs[4], T, Hs[3]), T, Hs[2]), T, Hs[1]), T, Hs[0]), T, B);
         }
     }
 };
+
+// cop_cell_terms for the mixed form (the same terms, no reference rounding to keep): gamma and 1/rho
+// from the caller, one reciprocal of the mixture R instead of a division per term.
+template <int NS>
+__device__ __forceinline__ void cop_cell_terms_mixed(const DevThermo &th, double T, double Cp, double gm, double wi,
+                                                     double u, double v, double w, double H, double p, double rho1,
+                                                     double *xc, long long P, long long id) {
+    constexpr int NCOP = NS - 1;
+    double h[NS];
+#pragma unroll
+    for (int n = 0; n < NS; n++) h[n] = enthalpy(th, T, n);
+    const double q2 = u * u + v * v + w * w;
+    const double CpT_R = Cp * T / (wi * kRu);
+    const double RN = th.Ri[NCOP];
+    const double g1 = gm - 1.0;
+    xc[id] = gm;
+    xc[P + id] = g1 * (0.5 * q2 - h[NCOP] + RN * CpT_R);
+    xc[2 * P + id] = H - 0.5 * q2 - p * rho1;
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) xc[(3 + n) * P + id] = g1 * ((h[NCOP] - h[n]) + (th.Ri[n] - RN) * CpT_R);
+}
 
 // get_T (Mixing_device.h:171-193): the same clamped Newton iteration and stopping test on the
 // folded mixture polynomials; returns T and the mixture Cp at T.
@@ -141,15 +165,15 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             double Cp;
             const double T = newton_T_folded<NS>(th, yi, tme, f.T[id], Cp);
             const double pd = rhod * Rm * T;
-            const double CopW = 1.0 / mix_W_inv<NS>(th, yi);
-            const double gmx = Cp / (Cp - kRu / CopW);
+            const double wi = mix_W_inv<NS>(th, yi);
+            const double gmx = Cp / (Cp - kRu * wi);
             const double gamma = gmx > 1.0 ? gmx : -1.0;
             const double Hd = (U[4] + pd) * rho1;
             const double cd = sqrt(gamma * pd * rho1);
             f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd, f.c[id] = cd;
             f.e[id] = tme, f.gamma[id] = gamma, f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
             if (f.Tf) f.Tf[id] = (float)T;  // viscous schemes: the heat flux's FP32 temperature
-            if (f.xc) cop_cell_terms<NS>(th, yi, T, Cp, ud, vd, wd, Hd, pd, rhod, f.xc, P, id);
+            if (f.xc) cop_cell_terms_mixed<NS>(th, T, Cp, gmx, wi, ud, vd, wd, Hd, pd, rho1, f.xc, P, id);
 #pragma unroll
             for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = (float)yi[s];
 #pragma unroll
