@@ -75,6 +75,11 @@ def test_create_rejects_bad_arguments(cuda_lib):
     b.Bwidth_X = 2
     rc = cuda_lib.xfg_create(C.byref(b), C.byref(s), C.byref(th), 0, C.byref(h))
     assert rc == -1 and "Bwidth" in cuda_lib.xfg_last_error().decode()
+    from xfluids_gb300.abi import OUTFLOW
+    from xfluids_gb300.mesh import make_block
+    long3d = make_block((8, 70000, 8), (1.0, 1.0, 1.0), [OUTFLOW] * 6)
+    rc = cuda_lib.xfg_create(C.byref(long3d), C.byref(s), C.byref(th), 0, C.byref(h))
+    assert rc == -1 and "elongated" in cuda_lib.xfg_last_error().decode()
 
 
 def test_ensemble_rejects_unsupported_schemes_before_touching_a_device(cuda_lib):

@@ -176,6 +176,10 @@ static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *
         }
     }
     if (!(dims[0] || dims[1] || dims[2])) return fail(-1, "no active direction");
+    // face launches: 32 x 4 threads per block, grid (x/32, y/4, z) for the x and y sweeps and
+    // (x/32, y, z/4) for the z sweep; grid y and z are limited to 65535 blocks
+    if (inner[2] + 1 > 65535 || (dims[2] && inner[1] + 1 > 65535) || (inner[1] + 4) / 4 > 65535)
+        return fail(-1, "block too elongated for the face launches (Z_inner or, in 3D, Y_inner above 65534)");
     return 0;
 }
 
