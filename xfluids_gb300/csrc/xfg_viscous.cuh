@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kThreads) k_transport_f32(Geo g, DevFields f, 
 }
 
 // viscous stress and heat-conduction flux at the faces i+1/2 of direction D, subtracted from the
-// face flux (FP64 face fluxes, or the FP32 ones of the mixed form)
+// FP64 face fluxes (the mixed form runs k_visc_f32)
 template <int D, int E, class FT>
 __global__ void __launch_bounds__(kThreads) k_visc(Geo g, DevFields f, FT *__restrict__ Fw, int heat, int guard) {
     if (guard && step_done(f)) return;
