@@ -153,3 +153,51 @@ def test_random_case_mixed_close_to_fp64(seed, cuda_lib):
     rel = d / scale
     print(f"seed {seed}: mixed vs FP64 state-scaled L1 {rel.max():.2e}")
     assert np.all(rel <= 1e-5), rel
+
+
+def _tiny_case(res, dom, bc, order, cop=False):
+    rng = np.random.default_rng(sum(res) * 31 + order)
+    b = make_block(res, dom, bc, cfl=0.5)
+    X, Y, Z = cases.cell_centres(b)
+    vel = [_field(rng, b, X, Y, Z, 1.0, 0.3, 0.0) - 1.0 for _ in range(3)]
+    u, v, w = [0.4 * vv if d else 0.0 * vv for vv, d in zip(vel, (b.DimX, b.DimY, b.DimZ))]
+    if not cop:
+        s = make_scheme(cop=False, scheme_order=order)
+        rho = _field(rng, b, X, Y, Z, 1.0, 0.1, 0.2)
+        p = _field(rng, b, X, Y, Z, 1.0, 0.1, -0.2)
+        return b, s, empty_thermal(), cases.conserved_ideal(rho, u, v, w, p), None
+    th = H.thermal(cases.MIXING_SPECIES, 0)
+    s = make_scheme(cop=True, num_species=5, scheme_order=order, thermo=0, ghost_species=False)
+    T = fill_ghosts_like_bc(b, _field(rng, b, X, Y, Z, 700.0, 0.1, 0.2))
+    p = _field(rng, b, X, Y, Z, 1.0e5, 0.05, 0.1)
+    Ys = np.stack([_field(rng, b, X, Y, Z, 0.2 + 0.1 * q, 0.1, 0.1) for q in range(5)], axis=-1)
+    Ys = Ys / Ys.sum(-1, keepdims=True)
+    R = thermo.RU * sum(Ys[..., q] / th.Wi[q] for q in range(5))
+    rho = p / (R * T)
+    h = sum(Ys[..., q] * cases.species_cp_h(th, q, T, nasa=False)[1] for q in range(5))
+    E = rho * (h - R * T + 0.5 * (3600 * (u * u + v * v + w * w)))
+    U = np.concatenate([np.stack([rho, 60 * rho * u, 60 * rho * v, 60 * rho * w, E], axis=-1),
+                        rho[..., None] * Ys[..., :4]], axis=-1)
+    return b, s, th, np.ascontiguousarray(U.reshape(-1, 9)), np.ascontiguousarray(T.reshape(-1))
+
+
+TINY = {
+    "1d_min_periodic_w7": ((4, 0, 0), (1.0, 1.0, 1.0), [PERIODIC] * 6, 7, False),
+    "1d_min_outflow_w5": ((4, 0, 0), (1.0, 1.0, 1.0), [OUTFLOW] * 6, 5, False),
+    "2d_min_walls_w7": ((4, 4, 0), (1.0, 3.0, 1.0), [SYMMETRY, NSLIPWALL, SLIPWALL, OUTFLOW, 0, 0], 7, False),
+    "2d_ragged_w6": ((5, 7, 0), (0.7, 1.9, 1.0), [PERIODIC, PERIODIC, OUTFLOW, SYMMETRY, 0, 0], 6, False),
+    "3d_min_w5": ((4, 4, 4), (1.0, 2.0, 0.5), [PERIODIC, PERIODIC, OUTFLOW, OUTFLOW, SYMMETRY, NSLIPWALL], 5, False),
+    "3d_ragged_w7": ((5, 6, 7), (1.0, 1.3, 0.4), [OUTFLOW, SLIPWALL, PERIODIC, PERIODIC, INFLOW, OUTFLOW], 7, False),
+    "3d_min_mixture_w7": ((4, 4, 4), (0.01, 0.02, 0.01), [PERIODIC, PERIODIC, OUTFLOW, NSLIPWALL, SYMMETRY, OUTFLOW], 7, True),
+    "2d_ragged_mixture_w5": ((5, 9, 0), (0.01, 0.013, 1.0), [SLIPWALL, OUTFLOW, PERIODIC, PERIODIC, 0, 0], 5, True),
+}
+
+
+@pytest.mark.parametrize("precision", [FP64, FP64_STRICT], ids=["fp64", "strict"])
+@pytest.mark.parametrize("name", list(TINY))
+def test_smallest_and_ragged_blocks_match_oracle(name, precision, cuda_lib):
+    """Blocks at the minimum size (inner = Bwidth = 4 per active direction), odd and unequal sizes,
+    unequal spacings."""
+    res, dom, bc, order, cop = TINY[name]
+    worst = run_stagewise(_tiny_case(res, dom, bc, order, cop), steps=2, precision=precision)
+    print(f"{name}: worst {worst:.2e}")
