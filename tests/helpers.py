@@ -6,7 +6,7 @@ import os
 import numpy as np
 
 from xfluids_gb300 import cases, thermo
-from xfluids_gb300.abi import OUTFLOW, PERIODIC, SYMMETRY, SLIPWALL, ROE, LLF, GLF
+from xfluids_gb300.abi import OUTFLOW, PERIODIC, SYMMETRY, SLIPWALL, LLF
 from xfluids_gb300.mesh import make_block, make_scheme, empty_thermal
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")

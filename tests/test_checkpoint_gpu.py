@@ -7,7 +7,7 @@ from helpers import riemann_small, sod_like
 from xfluids_gb300 import cases, checkpoint
 from xfluids_gb300.ensemble import Ensemble
 from xfluids_gb300.fluid import Fluid
-from xfluids_gb300.mesh import empty_thermal, make_scheme
+from xfluids_gb300.mesh import make_scheme
 from xfluids_gb300.serve import Server, poisson_trace
 
 pytestmark = pytest.mark.gpu

@@ -17,7 +17,7 @@ import pytest
 
 import helpers as H
 from oracle.xfo import Oracle
-from xfluids_gb300.abi import ROE, LLF, GLF, MIXED, FP64, FP64_STRICT
+from xfluids_gb300.abi import ROE, GLF, MIXED, FP64, FP64_STRICT
 
 pytestmark = pytest.mark.gpu
 

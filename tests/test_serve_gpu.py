@@ -1,7 +1,6 @@
 """Continuous-batching server (xfluids_gb300/serve.py): every request served in the mix, with
 others arriving, running and leaving around it, gives the same result as the same solve run
 alone through the single-grid path (Fluid.advance to its end time)."""
-import numpy as np
 import pytest
 
 from helpers import PARITY_TOL, normwise

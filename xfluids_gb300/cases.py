@@ -10,7 +10,7 @@ import math
 
 import numpy as np
 
-from .abi import OUTFLOW, PERIODIC, SYMMETRY, LLF
+from .abi import OUTFLOW, PERIODIC, LLF
 from .mesh import make_block, make_scheme, empty_thermal
 from .thermo import RU
 
