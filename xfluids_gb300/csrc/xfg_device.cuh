@@ -531,6 +531,46 @@ __device__ __forceinline__ T weno7(const T *pp, const T *mm) {
     return tp + tm;
 }
 
+// WENO7 of the contracted FP64 forms: the same indicators, candidates and weights, the weights in
+// the product form W_k = C_k prod_{j != k} (eps + S_j)^2 / sum (one division instead of eight; the
+// products stay far inside the FP64 range: (eps + S)^2 is at least 1e-14, three of them of large
+// indicators ~1e144 at the steepest jumps met here). Not for FP32, where they would overflow.
+__device__ __forceinline__ double weno7_prod_body(double v1, double v2, double v3, double v4, double v5, double v6,
+                                                  double v7) {
+    const double ep = 1.0e-7;
+    const double C0 = 1.0 / 35.0, C1 = 12.0 / 35.0, C2 = 18.0 / 35.0, C3 = 4.0 / 35.0;
+    const double S10 = (-2.0 / 6.0) * v1 + (9.0 / 6.0) * v2 - (18.0 / 6.0) * v3 + (11.0 / 6.0) * v4;
+    const double S11 = (1.0 / 6.0) * v2 - v3 + (3.0 / 6.0) * v4 + (2.0 / 6.0) * v5;
+    const double S12 = (-2.0 / 6.0) * v3 - (3.0 / 6.0) * v4 + v5 - (1.0 / 6.0) * v6;
+    const double S13 = (-11.0 / 6.0) * v4 + (18.0 / 6.0) * v5 - (9.0 / 6.0) * v6 + (2.0 / 6.0) * v7;
+    const double S20 = -v1 + 4.0 * v2 - 5.0 * v3 + 2.0 * v4;
+    const double S21 = v3 - 2.0 * v4 + v5;
+    const double S22 = v4 - 2.0 * v5 + v6;
+    const double S23 = 2.0 * v4 - 5.0 * v5 + 4.0 * v6 - v7;
+    const double S30 = -v1 + 3.0 * v2 - 3.0 * v3 + v4;
+    const double S31 = -v2 + 3.0 * v3 - 3.0 * v4 + v5;
+    const double S32 = -v3 + 3.0 * v4 - 3.0 * v5 + v6;
+    const double S33 = -v4 + 3.0 * v5 - 3.0 * v6 + v7;
+    const double k13 = 13.0 / 12.0, k1043 = 1043.0 / 960.0, k112 = 1.0 / 12.0;
+    const double S0 = S10 * S10 + k13 * S20 * S20 + k1043 * S30 * S30 + k112 * S10 * S30;
+    const double S1 = S11 * S11 + k13 * S21 * S21 + k1043 * S31 * S31 + k112 * S11 * S31;
+    const double S2 = S12 * S12 + k13 * S22 * S22 + k1043 * S32 * S32 + k112 * S12 * S32;
+    const double S3 = S13 * S13 + k13 * S23 * S23 + k1043 * S33 * S33 + k112 * S13 * S33;
+    const double d0 = (ep + S0) * (ep + S0), d1 = (ep + S1) * (ep + S1);
+    const double d2 = (ep + S2) * (ep + S2), d3 = (ep + S3) * (ep + S3);
+    const double d01 = d0 * d1, d23 = d2 * d3;
+    const double p0 = C0 * d1 * d23, p1 = C1 * d0 * d23, p2 = C2 * d01 * d3, p3 = C3 * d01 * d2;
+    const double q0 = (-3.0 / 12.0) * v1 + (13.0 / 12.0) * v2 - (23.0 / 12.0) * v3 + (25.0 / 12.0) * v4;
+    const double q1 = (1.0 / 12.0) * v2 - (5.0 / 12.0) * v3 + (13.0 / 12.0) * v4 + (3.0 / 12.0) * v5;
+    const double q2 = (-1.0 / 12.0) * v3 + (7.0 / 12.0) * v4 + (7.0 / 12.0) * v5 - (1.0 / 12.0) * v6;
+    const double q3 = (3.0 / 12.0) * v4 + (13.0 / 12.0) * v5 - (5.0 / 12.0) * v6 + (1.0 / 12.0) * v7;
+    return (p0 * q0 + p1 * q1 + p2 * q2 + p3 * q3) / (p0 + p1 + p2 + p3);
+}
+__device__ __forceinline__ double weno7_prod(const double *pp, const double *mm) {
+    return weno7_prod_body(pp[0], pp[1], pp[2], pp[3], pp[4], pp[5], pp[6]) +
+           weno7_prod_body(mm[7], mm[6], mm[5], mm[4], mm[3], mm[2], mm[1]);
+}
+
 // atomic max of a non-negative double through its bit pattern (monotone for x >= 0)
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long *addr, double v) {
     if (!(v >= 0.0)) v = __longlong_as_double(0x7ff0000000000000LL);  // NaN -> +inf (flags the step)

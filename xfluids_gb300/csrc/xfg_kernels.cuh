@@ -739,7 +739,7 @@ __device__ __forceinline__ void faces_body(const Geo &g, const DevFields &f, con
             }
         }
         double fl;
-        if constexpr (ORDER == 7) fl = weno7(pp, mm);
+        if constexpr (ORDER == 7) fl = XFG_STRICT_BUILD ? weno7(pp, mm) : weno7_prod(pp, mm);
         else if constexpr (ORDER == 6) fl = wenocu6(pp, mm, D == 0 ? g.dx : (D == 1 ? g.dy : g.dz));
         else fl = FAST_BUILD ? weno5_fast(pp, mm) : weno5(pp, mm);
 #pragma unroll
