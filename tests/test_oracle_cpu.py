@@ -78,46 +78,6 @@ def test_vortex_translates():
     assert err < 2e-3, err
 
 
-def _sod_exact(x, t, g=1.4):
-    """Exact Sod solution (rho) from the two-rarefaction/shock Newton iteration."""
-    rl, pl, rr, pr = 1.0, 1.0, 0.125, 0.1
-    cl, cr = math.sqrt(g * pl / rl), math.sqrt(g * pr / rr)
-
-    def f(p, rk, pk, ck):
-        if p > pk:
-            A, B = 2 / ((g + 1) * rk), (g - 1) / (g + 1) * pk
-            return (p - pk) * math.sqrt(A / (p + B))
-        return 2 * ck / (g - 1) * ((p / pk) ** ((g - 1) / (2 * g)) - 1)
-
-    p = 0.3
-    for _ in range(100):
-        F = f(p, rl, pl, cl) + f(p, rr, pr, cr)
-        dp = 1e-7
-        dF = (f(p + dp, rl, pl, cl) + f(p + dp, rr, pr, cr) - F) / dp
-        p -= F / dF
-    u = 0.5 * (f(p, rr, pr, cr) - f(p, rl, pl, cl))
-    rstar_l = rl * (p / pl) ** (1 / g)
-    rstar_r = rr * ((p / pr + (g - 1) / (g + 1)) / ((g - 1) / (g + 1) * p / pr + 1))
-    S = u + 0.0  # contact speed
-    Ss = math.sqrt((g + 1) / (2 * g) * p / pr + (g - 1) / (2 * g)) * cr  # shock speed
-    cstar = cl * (p / pl) ** ((g - 1) / (2 * g))
-    out = np.empty_like(x)
-    for q, xq in enumerate(x):
-        s = (xq - 0.5) / t
-        if s < -cl:
-            out[q] = rl
-        elif s < u - cstar:
-            c = 2 / (g + 1) * (cl - (g - 1) / 2 * s)
-            out[q] = rl * (c / cl) ** (2 / (g - 1))
-        elif s < S:
-            out[q] = rstar_l
-        elif s < Ss:
-            out[q] = rstar_r
-        else:
-            out[q] = rr
-    return out
-
-
 @pytest.mark.parametrize("order", [5, 7])
 def test_sod_against_exact(order):
     b, s, th, U, T = cases.sod(256, order=order)
@@ -130,7 +90,7 @@ def test_sod_against_exact(order):
     X, _, _ = cases.cell_centres(b)
     sl = b.inner_slices()
     rho = o.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 5)[..., 0][sl].ravel()
-    ex = _sod_exact(X[sl].ravel(), 0.2)
+    ex = cases.sod_exact_density(X[sl].ravel(), 0.2)
     assert np.abs(rho - ex).mean() < 6e-3
 
 

@@ -72,6 +72,37 @@ def sod(n=1024, cfl=0.5, precision=0, order=5):
     return b, s, empty_thermal(), U, None
 
 
+def sod_exact_density(x, t, gamma=1.4):
+    """Exact density of the Sod problem at time t (interface at x = 0.5): the star pressure from
+    Newton's method on the pressure functions of the exact Riemann solver (Toro, ch. 4), then a
+    left rarefaction, the contact and a right shock."""
+    rl, pl, rr, pr = 1.0, 1.0, 0.125, 0.1
+    g = gamma
+    cl, cr = math.sqrt(g * pl / rl), math.sqrt(g * pr / rr)
+
+    def f(p, rk, pk, ck):
+        if p > pk:
+            A, B = 2 / ((g + 1) * rk), (g - 1) / (g + 1) * pk
+            return (p - pk) * math.sqrt(A / (p + B))
+        return 2 * ck / (g - 1) * ((p / pk) ** ((g - 1) / (2 * g)) - 1)
+
+    p = 0.3
+    for _ in range(100):
+        F = f(p, rl, pl, cl) + f(p, rr, pr, cr)
+        dp = 1e-7
+        dF = (f(p + dp, rl, pl, cl) + f(p + dp, rr, pr, cr) - F) / dp
+        p -= F / dF
+    u = 0.5 * (f(p, rr, pr, cr) - f(p, rl, pl, cl))
+    rstar_l = rl * (p / pl) ** (1 / g)
+    rstar_r = rr * ((p / pr + (g - 1) / (g + 1)) / ((g - 1) / (g + 1) * p / pr + 1))
+    shock = math.sqrt((g + 1) / (2 * g) * p / pr + (g - 1) / (2 * g)) * cr
+    cstar = cl * (p / pl) ** ((g - 1) / (2 * g))
+    s = (np.asarray(x, dtype=np.float64) - 0.5) / t
+    c_fan = 2 / (g + 1) * (cl - (g - 1) / 2 * s)
+    fan = rl * np.maximum(c_fan / cl, 0.0) ** (2 / (g - 1))
+    return np.select([s < -cl, s < u - cstar, s < u, s < shock], [rl, fan, rstar_l, rstar_r], rr)
+
+
 def riemann_states(rng):
     """Four quadrant states (rho, u, v, p): rho in U[0.1,2], u,v in U[-1,1], p in U[0.05,2]."""
     q = np.empty((4, 4))

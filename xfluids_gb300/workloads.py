@@ -4,6 +4,10 @@
     python -m xfluids_gb300.workloads sod      --size 1024 --steps 100
     python -m xfluids_gb300.workloads mixing   --shape 256 128 64 --steps 2 [--precision mixed] [--viscous]
     python -m xfluids_gb300.workloads ensemble --members 32 --steps 4 [--precision mixed]
+    python -m xfluids_gb300.workloads horizon  --size 1024 --periods 10
+
+The horizon workload runs the 2D vortex for whole periods (t = 10 per period) in FP64 and in the
+mixed form and reports the error of each against the exact vortex and of mixed against FP64.
 
 Each run: initial state on the host, one warm-up step (captures the step graph), a reset to the
 initial state, then the timed steps (CUDA events around the graph replays). The mixing layer reads
@@ -16,6 +20,8 @@ from __future__ import annotations
 import argparse
 import json
 import os
+
+import numpy as np
 
 from . import cases, thermo
 from .abi import MIXED
@@ -63,9 +69,62 @@ def ensemble(members, steps, precision, device=0, tune=False):
             "schedule": sched}
 
 
+def _rel_l1(a, r):
+    """L1 of a - r per conserved component, relative to the mean |r| of the density (rho, rho*E
+    scaled by their own means; the momenta by the mean momentum magnitude)."""
+    d = np.abs(a - r).mean(axis=0)
+    scale = np.abs(r).mean(axis=0)
+    mom = float(np.sqrt((r[:, 1:4] ** 2).sum(axis=1)).mean())
+    scale[1:4] = mom
+    return [float(x) for x in d / scale]
+
+
+def vortex_horizon(n, periods=10, precisions=(0, MIXED), device=0, chunk=4096):
+    """The 2D vortex n^2 advanced to t = 10 * periods (whole periods: the exact solution is the
+    initial state) in each precision; per precision the steps, the device time, the L1 and Linf
+    error of rho against the exact vortex and the drift of the total mass; for the mixed form the
+    L1 of each component against the FP64 run (relative as in _rel_l1) and the normwise Linf."""
+    from .fluid import Fluid
+    t_end = 10.0 * periods
+    out = {"workload": f"2D isentropic vortex {n}^2, {periods} periods (t = {t_end:g})"}
+    finals = {}
+    for prec in precisions:
+        b, s, th, U, T = cases.isentropic_vortex(n, precision=prec)
+        sl = b.inner_slices()
+        inner = lambda a: a.reshape(b.Zmax, b.Ymax, b.Xmax, 5)[sl].reshape(-1, 5)
+        f = Fluid(b, s, th, device=device)
+        try:
+            f.InitialU(U, T)
+            f.initialize()
+            t, k, ms, st = 0.0, 0, 0.0, 0
+            while t < t_end and st == 0:
+                st, t, kk, dms = f.advance_timed(chunk, t_end)
+                k += kk
+                ms += dms
+            g = inner(f.get("U"))
+        finally:
+            f.close()
+        u0 = inner(np.asarray(U, dtype=np.float64).reshape(-1))
+        rho_ex = cases.isentropic_vortex_exact(b, t_end)[sl].reshape(-1)
+        mass0, mass = np.ascontiguousarray(u0[:, 0]).sum(), np.ascontiguousarray(g[:, 0]).sum()
+        finals[prec] = g
+        out["fp64" if prec == 0 else ("mixed" if prec == MIXED else "strict")] = {
+            "status": st, "t": t, "steps": k, "ms": ms,
+            "cell_updates_per_s": n * n * k / (ms * 1e-3) if ms > 0 else 0.0,
+            "l1_rho_vs_exact": float(np.abs(g[:, 0] - rho_ex).mean()),
+            "linf_rho_vs_exact": float(np.abs(g[:, 0] - rho_ex).max()),
+            "mass_drift_rel": float((mass - mass0) / mass0)}
+    if 0 in finals and MIXED in finals:
+        a, r = finals[MIXED], finals[0]
+        out["mixed_vs_fp64"] = {
+            "l1_rel": _rel_l1(a, r),
+            "linf_normwise": float(max(np.abs(a[:, q] - r[:, q]).max() / np.abs(r[:, q]).max() for q in range(4)))}
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    ap.add_argument("workload", choices=["vortex", "sod", "mixing", "ensemble"])
+    ap.add_argument("workload", choices=["vortex", "sod", "mixing", "ensemble", "horizon"])
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--shape", type=int, nargs=3, default=[256, 128, 64])
     ap.add_argument("--members", type=int, default=32)
@@ -77,9 +136,13 @@ def main(argv=None):
     ap.add_argument("--transport-tables", default=DEFAULT_TRANSPORT_TABLES,
                     help="Lennard-Jones rows and collision integrals (transport.dump_transport_tables)")
     ap.add_argument("--tune", action="store_true", help="ensemble: run the schedule autotuner first")
+    ap.add_argument("--periods", type=int, default=10, help="horizon: vortex periods (t = 10 per period)")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     prec = {"fp64": 0, "mixed": MIXED, "strict": 2}[a.precision]
+    if a.workload == "horizon":
+        print(json.dumps(vortex_horizon(a.size, a.periods, device=a.device)))
+        return 0
     if a.workload == "ensemble":
         out = ensemble(a.members, a.steps, prec, a.device, a.tune)
     else:
