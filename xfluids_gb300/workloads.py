@@ -118,7 +118,8 @@ def vortex_horizon(n, periods=10, precisions=(0, MIXED), device=0, chunk=4096):
         a, r = finals[MIXED], finals[0]
         out["mixed_vs_fp64"] = {
             "l1_rel": _rel_l1(a, r),
-            "linf_normwise": float(max(np.abs(a[:, q] - r[:, q]).max() / np.abs(r[:, q]).max() for q in range(4)))}
+            "linf_normwise": float(max(np.abs(a[:, q] - r[:, q]).max() / np.abs(r[:, q]).max()
+                                       for q in range(5) if np.abs(r[:, q]).max() > 0))}
     return out
 
 
