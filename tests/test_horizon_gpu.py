@@ -92,7 +92,9 @@ def test_vortex_ten_periods_mixed_against_fp64(n, cuda_lib):
     print(out)
     for name in ("fp64", "mixed"):
         assert out[name]["status"] == 0 and abs(out[name]["t"] - 100.0) <= 1e-12, out[name]
-        assert abs(out[name]["mass_drift_rel"]) <= 1e-12, out[name]
+        # the FP64 stage sums move the total mass by about 4e-17 per step (rounding of the stage
+        # arithmetic); the FP32 face fluxes must add nothing to that
+        assert abs(out[name]["mass_drift_rel"]) <= 2e-16 * out[name]["steps"], out[name]
     assert out["fp64"]["steps"] == out["mixed"]["steps"] or abs(out["fp64"]["steps"] - out["mixed"]["steps"]) <= 1
     # FP32 reconstruction against FP64 after the whole solve
     assert max(out["mixed_vs_fp64"]["l1_rel"]) <= 1e-5, out["mixed_vs_fp64"]

@@ -299,6 +299,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     g.Bx = block->Bwidth_X, g.By = block->Bwidth_Y, g.Bz = block->Bwidth_Z;
     g.dimx = block->DimX, g.dimy = block->DimY, g.dimz = block->DimZ;
     g._dx = block->_dx, g._dy = block->_dy, g._dz = block->_dz;
+    geo_split_spacing(g);
     g.dx = block->dx, g.dy = block->dy, g.dz = block->dz;
     g.pitch = h->P;
     DevThermo &th = h->ctx.th;

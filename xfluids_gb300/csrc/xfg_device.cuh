@@ -58,8 +58,20 @@ struct Geo {
     long long pitch;  // elements between components of a SoA array
     double dx, dy, dz;  // cell sizes (the WENO-CU6 epsilon)
     int bc[6];          // boundary kinds (the ghost layers of the viscous derivatives)
+    float idh[3], idl[3];  // 1/dx, 1/dy, 1/dz as float pairs, hi + lo (the mixed divergence)
     __host__ __device__ long long ncell() const { return (long long)Xmax * Ymax * Zmax; }
 };
+
+// Fills Geo::idh / idl from _dx, _dy, _dz: hi = the nearest float, lo = the nearest float to the
+// remainder, so hi + lo carries the inverse spacing to about 2^-48 relative.
+inline void geo_split_spacing(Geo &g) {
+    const double v[3] = {g._dx, g._dy, g._dz};
+    for (int d = 0; d < 3; d++) {
+        const bool ok = v[d] == v[d] && v[d] <= 3.0e38 && v[d] >= -3.0e38;   // finite, in float range
+        g.idh[d] = ok ? (float)v[d] : 0.f;
+        g.idl[d] = ok ? (float)(v[d] - (double)g.idh[d]) : 0.f;
+    }
+}
 
 // Device arrays of one block. All SoA with the block pitch.
 struct DevFields {

@@ -366,6 +366,7 @@ void carve(Member &m, char *base, const xfg_block &b, bool mixed) {
     g.Xmax = b.Xmax, g.Ymax = b.Ymax, g.Zmax = b.Zmax, g.Xi = b.X_inner, g.Yi = b.Y_inner, g.Zi = b.Z_inner;
     g.Bx = b.Bwidth_X, g.By = b.Bwidth_Y, g.Bz = b.Bwidth_Z, g.dimx = b.DimX, g.dimy = b.DimY, g.dimz = b.DimZ;
     g._dx = b._dx, g._dy = b._dy, g._dz = b._dz, g.pitch = (long long)P;
+    geo_split_spacing(g);
     g.dx = b.dx, g.dy = b.dy, g.dz = b.dz;
     m.cfl = b.CFLnumber;
     for (int q = 0; q < 6; q++) m.bc[q] = b.Boundarys[q];

@@ -458,7 +458,6 @@ __global__ void __launch_bounds__(kThreads, XFG_FACES_MIXED_MINB)
     faces_mixed_body<D, false, 1, 5>(g, f, th, artificial, glf_d, i, j, k);
 }
 
-// Divergence of the FP32 face fluxes, accumulated into the FP64 state by the RK stage.
 // Positivity limiter of the mixed form: the FP32 physical and face fluxes, the FP64 state.
 template <int D, bool COP, int NS>
 __global__ void __launch_bounds__(kThreads) k_pp_mixed(Geo g, DevFields f, const double *__restrict__ UI,
@@ -470,6 +469,45 @@ __global__ void __launch_bounds__(kThreads) k_pp_mixed(Geo g, DevFields f, const
                                      (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// Knuth's TwoSum: a + b = s + e exactly (round to nearest, no overflow). The _rn intrinsics keep
+// the compiler from contracting or reordering the steps.
+__device__ __forceinline__ float two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b);
+    const float bv = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bv)), __fsub_rn(b, bv));
+    return s;
+}
+
+// float -> double through the bit patterns of IEEE 754 binary32 and binary64 (exponent rebias
+// 127 -> 1023, mantissa shifted by 29), exact for zeros and normal floats and off the FP64 pipe;
+// subnormals, infinities and NaNs take the conversion instruction.
+__device__ __forceinline__ double f2d_bits(float x) {
+    const unsigned u = __float_as_uint(x), mag = u & 0x7fffffffu;
+    if (mag != 0u && mag - 0x00800000u >= 0x7f000000u) return (double)x;
+    const unsigned hi = (u & 0x80000000u) | (mag ? (mag >> 3) + (896u << 20) : 0u);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// One direction's share of the divergence of component q, added to the float pair (s, c):
+// (Fa - Fb) * (1/dx) with the difference taken exactly (TwoSum) and the product with the float
+// pair 1/dx = sh + sl to about 2^-48, so that every face flux enters its two cells with equal and
+// opposite weight up to that level and the sum over cells telescopes.
+__device__ __forceinline__ void div_acc(float a, float b, float sh, float sl, float &s, float &c) {
+    float e;
+    const float d = two_sum(a, -b, e);
+    const float p = __fmul_rn(d, sh);
+    const float pe = fmaf(e, sh, fmaf(d, sl, fmaf(d, sh, -p)));
+    float e2;
+    s = two_sum(s, p, e2);
+    c = __fadd_rn(c, __fadd_rn(e2, pe));
+}
+
+// Divergence of the FP32 face fluxes and the SSP-RK3 stage in FP64 (a12, a13: the reference's
+// UpdateFluidLU, Reconstruction_kernels.hpp:201-234, and UpdateURK3rdKernel, Update_kernels.hpp:64-94).
+// The divergence is accumulated as an unevaluated float pair (s + c, compensated summation) and
+// enters the FP64 stage sum as two exactly converted doubles, so the FP32 fluxes' rounding stays in
+// the fluxes, where it cancels between neighbouring cells, and the conserved sums of U move only by
+// the FP64 stage arithmetic.
 template <int E>
 __device__ __forceinline__ void div_rk_mixed_body(const Geo &g, const DevFields &f, int flag, double dt, int do_rk,
                                                   int store_lu, long long t) {
@@ -480,19 +518,18 @@ __device__ __forceinline__ void div_rk_mixed_body(const Geo &g, const DevFields 
     const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
     const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long sy = g.Xmax, sz = (long long)g.Xmax * g.Ymax;
-    const float fdx = (float)g._dx, fdy = (float)g._dy, fdz = (float)g._dz;
     int code = 0;
 #pragma unroll
     for (int n = 0; n < E; n++) {
-        float L = 0.f;
-        if (g.dimx) L += (f.Fwf[0][n * P + id - 1] - f.Fwf[0][n * P + id]) * fdx;
-        if (g.dimy) L += (f.Fwf[1][n * P + id - sy] - f.Fwf[1][n * P + id]) * fdy;
-        if (g.dimz) L += (f.Fwf[2][n * P + id - sz] - f.Fwf[2][n * P + id]) * fdz;
-        const double LU0 = (double)L;
-        if (store_lu) f.LU[n * P + id] = LU0;
-        if (!isfinite(L)) code = 1;
+        const long long q = n * P + id;
+        float s = 0.f, c = 0.f;
+        if (g.dimx) div_acc(f.Fwf[0][q - 1], f.Fwf[0][q], g.idh[0], g.idl[0], s, c);
+        if (g.dimy) div_acc(f.Fwf[1][q - sy], f.Fwf[1][q], g.idh[1], g.idl[1], s, c);
+        if (g.dimz) div_acc(f.Fwf[2][q - sz], f.Fwf[2][q], g.idh[2], g.idl[2], s, c);
+        const double LU0 = f2d_bits(s) + f2d_bits(c);
+        if (store_lu) f.LU[q] = LU0;
+        if (!isfinite(s)) code = 1;
         if (do_rk) {
-            const long long q = n * P + id;
             double out;
             if (flag == 1) {
                 out = f.U[q] + dt * LU0;

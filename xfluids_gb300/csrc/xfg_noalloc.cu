@@ -146,6 +146,7 @@ extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *
     c.g.Bx = block->Bwidth_X, c.g.By = block->Bwidth_Y, c.g.Bz = block->Bwidth_Z;
     c.g.dimx = block->DimX, c.g.dimy = block->DimY, c.g.dimz = block->DimZ;
     c.g._dx = block->_dx, c.g._dy = block->_dy, c.g._dz = block->_dz;
+    geo_split_spacing(c.g);
     c.g.dx = block->dx, c.g.dy = block->dy, c.g.dz = block->dz;
     c.g.pitch = P;
     for (int n = 0; n < XFG_MAX_SPECIES; n++) c.th.Ri[n] = thermal->Ri[n], c.th._Wi[n] = thermal->_Wi[n];

@@ -138,11 +138,13 @@ def main(argv=None):
                     help="Lennard-Jones rows and collision integrals (transport.dump_transport_tables)")
     ap.add_argument("--tune", action="store_true", help="ensemble: run the schedule autotuner first")
     ap.add_argument("--periods", type=int, default=10, help="horizon: vortex periods (t = 10 per period)")
+    ap.add_argument("--only", choices=["fp64", "mixed"], help="horizon: run one precision only")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     prec = {"fp64": 0, "mixed": MIXED, "strict": 2}[a.precision]
     if a.workload == "horizon":
-        print(json.dumps(vortex_horizon(a.size, a.periods, device=a.device)))
+        precs = (0, MIXED) if a.only is None else ((0,) if a.only == "fp64" else (MIXED,))
+        print(json.dumps(vortex_horizon(a.size, a.periods, precisions=precs, device=a.device)))
         return 0
     if a.workload == "ensemble":
         out = ensemble(a.members, a.steps, prec, a.device, a.tune)
