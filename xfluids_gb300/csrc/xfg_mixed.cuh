@@ -479,13 +479,15 @@ __device__ __forceinline__ float two_sum(float a, float b, float &e) {
 }
 
 // float -> double through the bit patterns of IEEE 754 binary32 and binary64 (exponent rebias
-// 127 -> 1023, mantissa shifted by 29), exact for zeros and normal floats and off the FP64 pipe;
-// subnormals, infinities and NaNs take the conversion instruction.
+// 127 -> 1023, mantissa shifted by 29), integer operations only, so nothing of it runs on the FP64
+// pipe: exact for zeros, normal floats, infinities and NaNs (payload kept); subnormal floats
+// (|x| < 2^-126) become zero.
 __device__ __forceinline__ double f2d_bits(float x) {
-    const unsigned u = __float_as_uint(x), mag = u & 0x7fffffffu;
-    if (mag != 0u && mag - 0x00800000u >= 0x7f000000u) return (double)x;
-    const unsigned hi = (u & 0x80000000u) | (mag ? (mag >> 3) + (896u << 20) : 0u);
-    return __hiloint2double((int)hi, (int)(u << 29));
+    const unsigned u = __float_as_uint(x), mag = u & 0x7fffffffu, sign = u & 0x80000000u;
+    const bool normal = mag - 0x00800000u < 0x7f000000u, special = mag >= 0x7f800000u;
+    const unsigned hi = sign | (normal ? (mag >> 3) + (896u << 20) : special ? 0x7ff00000u | ((mag & 0x7fffffu) >> 3) : 0u);
+    const unsigned lo = (normal || special) ? u << 29 : 0u;
+    return __hiloint2double((int)hi, (int)lo);
 }
 
 // One direction's share of the divergence of component q, added to the float pair (s, c):
