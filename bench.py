@@ -25,8 +25,14 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-# DRAM bytes per face of the FP64 x-face kernel measured by ncu on a small case, scaled per face
-# (profiles/k_faces_fp64_vortex.md); None until a capture exists.
+# Algorithmic flops of the vortex workload (WENO5-JS LLF, single gas), counted once by running the
+# oracle restatement with a counting scalar (+,-,*,/,sqrt,exp,log = 1; max/abs/compare = 0) on the
+# 64^2 vortex: per x face, and per cell-update over all kernels of one SSP-RK3 step.
+# tests/test_bench_cpu.py recounts both on the oracle and checks them.
+FLOPS_PER_FACE_X = 1378.0
+FLOPS_PER_CELL_UPDATE = 8711.78271484375
+FLOP_COUNT_SIZE = 64
+# Thermodynamic tables of the mixture workloads (NASA-9 / JANAF coefficients)
 THERMO_JSON = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "thermo_tables.json")
 # Lennard-Jones data and collision integrals of runtime.dat for the transport fits of the mixture
 TRANSPORT_TABLES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
@@ -126,17 +132,6 @@ class ClockSampler:
         reasons = sorted({names[q] for r in self.rows for q in range(4) if len(r) > 5 + q and r[5 + q] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
-
-
-def flops_per_face(size=64):
-    """Algorithmic flops of one x face of the vortex workload, counted on the oracle restatement
-    with a counting scalar (+,-,*,/,sqrt,exp,log = 1), per face and per cell-update."""
-    from oracle import xfo
-    from xfluids_gb300 import cases
-    b, s, th, U, T = cases.isentropic_vortex(size)
-    c = xfo.count_flops(b, s, th, U, T, 1)
-    nfx = (size + 1) * size
-    return c["faces_x"] / 3.0 / nfx, sum(c.values()) / float(size * size)
 
 
 def cpu_baseline(size, threads, min_seconds=10.0):
@@ -334,14 +329,36 @@ def bench_mixing_layer(args, local, steps):
     return res
 
 
-def bench_accuracy(local, n=192, t_end=0.5):
-    """Free-running drift of the FP64 path against the oracle (same steps, no resynchronisation)
-    and the error of FP64 and mixed against the exact vortex, 2D vortex n^2 to t_end."""
-    from oracle import xfo
+def accuracy_gpu(local, n=192, t_end=0.5):
+    """FP64 and mixed runs of the 2D vortex n^2 to t_end on the GPU, free running (no
+    resynchronisation); the inner-cell states are compared in the CPU leg (accuracy_vs_oracle)."""
     from xfluids_gb300.abi import MIXED
     from xfluids_gb300.fluid import Fluid
     cs = cases_mod()
-    xfo.set_threads(os.cpu_count() or 1)
+    b, s, th, U, T = cs.isentropic_vortex(n)
+    sl = b.inner_slices()
+    runs = {"n": n, "t_end": t_end}
+    for name, prec in (("fp64", 0), ("mixed", MIXED)):
+        s.precision = prec
+        f = Fluid(b, s, th, device=local)
+        f.InitialU(U, T)
+        f.initialize()
+        tg, k = 0.0, 0
+        while tg < t_end:
+            _, tg, kk = f.advance(64, t_end)
+            k += kk
+        runs[name] = (k, f.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 5)[sl].reshape(-1, 5))
+        f.close()
+    return runs
+
+
+def accuracy_vs_oracle(runs, threads):
+    """CPU leg, as the checker: the oracle advances the same vortex to the same time; returns the
+    drift of each GPU run against it and the density error of each against the exact vortex."""
+    from oracle import xfo
+    cs = cases_mod()
+    n, t_end = runs["n"], runs["t_end"]
+    xfo.set_threads(threads)
     b, s, th, U, T = cs.isentropic_vortex(n)
     o = xfo.Oracle(b, s, th, U, T)
     o.initialize()
@@ -353,17 +370,8 @@ def bench_accuracy(local, n=192, t_end=0.5):
     ref = o.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 5)[sl].reshape(-1, 5)
     rho_ex = cs.isentropic_vortex_exact(b, t_end)[sl].reshape(-1)
     out = {"workload": f"2D isentropic vortex {n}^2 to t = {t_end}", "steps": n_o}
-    for name, prec in (("fp64", 0), ("mixed", MIXED)):
-        s.precision = prec
-        f = Fluid(b, s, th, device=local)
-        f.InitialU(U, T)
-        f.initialize()
-        tg, k = 0.0, 0
-        while tg < t_end:
-            _, tg, kk = f.advance(64, t_end)
-            k += kk
-        g = f.get("U").reshape(b.Zmax, b.Ymax, b.Xmax, 5)[sl].reshape(-1, 5)
-        f.close()
+    for name in ("fp64", "mixed"):
+        k, g = runs[name]
         d = np.abs(g - ref)
         out[name] = {"steps": k, "l1_vs_oracle": float(d.mean()),
                      "max_normwise_vs_oracle": float(max(d[:, q].max() / np.abs(ref[:, q]).max()
@@ -372,6 +380,15 @@ def bench_accuracy(local, n=192, t_end=0.5):
                      "linf_rho_vs_exact": float(np.abs(g[:, 0] - rho_ex).max())}
     out["oracle_l1_rho_vs_exact"] = float(np.abs(ref[:, 0] - rho_ex).mean())
     return out
+
+
+def cpu_leg(threads, accuracy_runs=None):
+    """The CPU leg of the GPU arm (rank 0): the oracle restatement timed on the host cores
+    (cpu_baseline: steps of the 1024^2 vortex for about 10 s) and, when accuracy runs were made,
+    the oracle as their checker."""
+    val, steps, el = cpu_baseline(1024, threads, min_seconds=10.0)
+    acc = None if accuracy_runs is None else accuracy_vs_oracle(accuracy_runs, threads)
+    return val, steps, el, acc
 
 
 def cases_mod():
@@ -386,7 +403,7 @@ def run_gpu_arm(args, world, rank, local):
     d = Dist(world, local)
     n = args.size
     peaks = measure_pipe_peaks(local)
-    fpf, flops_per_cu = flops_per_face()
+    fpf, flops_per_cu = FLOPS_PER_FACE_X, FLOPS_PER_CELL_UPDATE
 
     def setup(precision):
         b, s, th, U, T = cases.isentropic_vortex(n, precision=precision)
@@ -484,7 +501,7 @@ def run_gpu_arm(args, world, rank, local):
         del s64, smx, diff
     serving = bench_serving(local, args.serve_requests, MIXED) if args.serve_requests > 0 else None
     mixing = bench_mixing_layer(args, local, args.mixing_steps) if args.mixing_steps > 0 else None
-    accuracy = bench_accuracy(local) if args.accuracy else None
+    accuracy_runs = accuracy_gpu(local) if args.accuracy else None
     d.close()
     if rank != 0:
         return 0
@@ -492,7 +509,7 @@ def run_gpu_arm(args, world, rank, local):
     fp64_peak = peaks["fp64_flops"] / 1e12
     traffic = None if NCU_FACE_BYTES_FP64 is None else NCU_FACE_BYTES_FP64 * faces_per_launch
     cpu_threads = os.cpu_count() or 1
-    cpu_val, cpu_steps, cpu_el = cpu_baseline(1024, cpu_threads, min_seconds=10.0)
+    cpu_val, cpu_steps, cpu_el, accuracy = cpu_leg(cpu_threads, accuracy_runs)
     line = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
         "steps": k, "warmup": args.warmup, "ms_per_step": ms_total_fp64, "higher_is_better": True,

@@ -1,0 +1,60 @@
+"""Host logic of bench.py on CPU: the committed algorithmic flop counts against a recount on the
+oracle, and the accuracy leg (GPU runs + oracle checker) driven by an oracle-backed stand-in for the
+CUDA handle on a small vortex."""
+import numpy as np
+import pytest
+
+import bench
+from oracle import xfo
+from xfluids_gb300 import cases
+
+
+def test_flop_constants_match_oracle_count():
+    n = bench.FLOP_COUNT_SIZE
+    b, s, th, U, T = cases.isentropic_vortex(n)
+    c = xfo.count_flops(b, s, th, U, T, 1)
+    per_face_x = c["faces_x"] / 3.0 / ((n + 1) * n)   # three RK stages, (n+1) x faces per row
+    per_cell_update = sum(c.values()) / float(n * n)
+    assert per_face_x == bench.FLOPS_PER_FACE_X
+    assert per_cell_update == bench.FLOPS_PER_CELL_UPDATE
+
+
+class _OracleFluid:
+    """The subset of Fluid that bench.accuracy_gpu uses, run by the oracle (precision ignored)."""
+
+    def __init__(self, b, s, th, device=0):
+        self.b, self.s, self.th = b, s, th
+
+    def InitialU(self, U, T):
+        self.o = xfo.Oracle(self.b, self.s, self.th, U, T)
+
+    def initialize(self):
+        self.o.initialize()
+        self.t = 0.0
+
+    def advance(self, nsteps, target_t):
+        k = 0
+        while k < nsteps and self.t < target_t:
+            self.t, _ = self.o.step(target_t)
+            k += 1
+        return 0, self.t, k
+
+    def get(self, name):
+        return self.o.get(name)
+
+    def close(self):
+        pass
+
+
+def test_accuracy_leg_with_oracle_stand_in(monkeypatch):
+    from xfluids_gb300 import fluid
+    monkeypatch.setattr(fluid, "Fluid", _OracleFluid)
+    runs = bench.accuracy_gpu(0, n=24, t_end=0.05)
+    acc = bench.accuracy_vs_oracle(runs, threads=2)
+    assert acc["steps"] > 0
+    for name in ("fp64", "mixed"):
+        r = acc[name]
+        assert r["steps"] == acc["steps"]
+        assert r["l1_vs_oracle"] == 0.0 and r["max_normwise_vs_oracle"] == 0.0
+        assert r["l1_rho_vs_exact"] == pytest.approx(acc["oracle_l1_rho_vs_exact"])
+        assert np.isfinite(r["linf_rho_vs_exact"]) and r["linf_rho_vs_exact"] > 0.0
