@@ -70,7 +70,9 @@ def fill_ghosts_like_bc(b, A):
     return A
 
 
-def random_case(seed):
+def random_case(seed, cop=None, order=None, art=None, pos=None, thermo_kind=None):
+    """Seeded random block, boundary kinds, scheme and state. The keyword arguments, when given,
+    replace the drawn choice after it was drawn, so the other draws of a seed stay the same."""
     rng = np.random.default_rng(7000 + seed)
     ndim = int(rng.choice([1, 2, 3], p=[0.3, 0.4, 0.3]))
     res = {1: lambda: (int(rng.integers(16, 65)), 0, 0), 2: lambda: (int(rng.integers(12, 41)), int(rng.integers(12, 41)), 0),
@@ -81,10 +83,9 @@ def random_case(seed):
             bc += [PERIODIC, PERIODIC]
         else:
             bc += [int(rng.choice(SIDES)), int(rng.choice(SIDES))]
-    cop = rng.random() < 0.35
-    order = int(rng.choice([5, 6, 7]))
-    art = int(rng.choice([LLF, ROE, GLF]))
-    pos = bool(rng.random() < 0.3)
+    drawn = (rng.random() < 0.35, int(rng.choice([5, 6, 7])), int(rng.choice([LLF, ROE, GLF])),
+             bool(rng.random() < 0.3))
+    cop, order, art, pos = (d if o is None else o for d, o in zip(drawn, (cop, order, art, pos)))
     b = make_block(res, (1.0, 1.0, 1.0), bc, cfl=float(rng.uniform(0.3, 0.6)))
     X, Y, Z = cases.cell_centres(b)
     vel = [_field(rng, b, X, Y, Z, 1.0, 0.3, 0.0) - 1.0 for _ in range(3)]
@@ -95,6 +96,7 @@ def random_case(seed):
         u, v, w = [0.5 * vv if d else 0.0 * vv for vv, d in zip(vel, (b.DimX, b.DimY, b.DimZ))]
         return b, s, empty_thermal(), cases.conserved_ideal(rho, u, v, w, p), None
     tk = int(rng.integers(0, 2))
+    tk = tk if thermo_kind is None else thermo_kind
     th = H.thermal(cases.MIXING_SPECIES, tk)
     s = make_scheme(cop=True, num_species=5, scheme_order=order, artificial_type=art, thermo=tk,
                     ghost_species=False, positivity=pos)
