@@ -17,6 +17,8 @@ its work-group size. The oracle and the CUDA path take the inner range as it is,
 reference whenever the work-group size divides the inner size. The random cases replace such a
 high side by Outflow where the size would expose it; the last test pins the behaviour itself.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -24,7 +26,8 @@ import helpers as H
 from oracle import ref_runner
 from oracle.xfo import Oracle
 from test_fuzz_gpu import random_case
-from xfluids_gb300.abi import GLF, INFLOW, LLF, OUTFLOW, ROE, SLIPWALL, VISCWALL
+from xfluids_gb300 import thermo
+from xfluids_gb300.abi import GLF, INFLOW, LLF, NSLIPWALL, OUTFLOW, ROE, SLIPWALL, VISCWALL
 
 # flavour -> scheme choices (cop, order, splitting, positivity limiter); mixtures are the
 # 5-species JANAF mixture of the random cases
@@ -61,7 +64,9 @@ def without_overhang_exposure(b):
     return replaced
 SEEDS = range(6 * len(NAMES))
 
-pytestmark = pytest.mark.skipif(not all(ref_runner.available(f) for f in NAMES),
+VISCOUS = "cop5_w5_llf_janaf_visc"
+
+pytestmark = pytest.mark.skipif(not all(ref_runner.available(f) for f in NAMES + [VISCOUS]),
                                 reason="reference flavours not built (oracle/ref/build_ref.sh)")
 
 
@@ -88,6 +93,40 @@ def test_oracle_equals_reference_on_random_case(seed):
     if cop:
         assert np.array_equal(o.get("T"), last["T"])
         assert np.array_equal(o.get("y"), last["y"])
+
+
+def _compare_stages(b, s, th, U, T, recs, transport=None):
+    o = Oracle(b, s, th, U, T, transport=transport)
+    o.initialize()
+    E = s.Emax
+    for q, r in enumerate(recs):
+        if r["flag"] == 1:
+            assert o.get_dt() == r["dt"], f"dt stage {q}"
+        o.stage(int(r["flag"]), float(r["dt"]))
+        assert np.array_equal(H.inner_aos(b, o.get("U"), E), H.inner_aos(b, r["U"], E)), f"U stage {q}"
+        assert np.array_equal(H.inner_aos(b, o.get("LU"), E), H.inner_aos(b, r["LU"], E)), f"LU stage {q}"
+    last = recs[-1]
+    for nm in ("rho", "p", "u", "v", "w", "c", "H", "T", "y"):
+        assert np.array_equal(o.get(nm), last[nm]), nm
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_oracle_equals_reference_on_random_viscous_case(seed, tmp_path):
+    """Viscous stress, heat conduction and diffusion (the 5-species JANAF mixture, WENO5 LLF) on
+    random cases, with the reference's own fitted transport data fed to the oracle. A z side of
+    kind nslipWall is replaced by Outflow: there the reference's velocity-derivative ghost fill
+    indexes outside the block (CenterDerivativeBCKernelZ, Visc_kernels.hpp:147-200)."""
+    b, s, th, U, T = random_case(200 + seed, cop=True, order=5, art=LLF, pos=False, thermo_kind=0)
+    s.viscous = 7
+    without_overhang_exposure(b)
+    for q in (4, 5):
+        if b.DimZ and b.Boundarys[q] == NSLIPWALL:
+            b.Boundarys[q] = OUTFLOW
+    tpath = os.path.join(tmp_path, "transport.bin")
+    recs = ref_runner.run_reference(VISCOUS, b, U, T, steps=2, transport_out=tpath)
+    t = ref_runner.read_transport(tpath)
+    tr = thermo.transport_from_arrays(5, t["visc"], t["therm"], t["dkj"], t["chara"], *t["limits"])
+    _compare_stages(b, s, th, U, T, recs, transport=tr)
 
 
 def test_reference_work_group_overhang_at_a_high_side_inflow():
