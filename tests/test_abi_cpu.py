@@ -109,3 +109,28 @@ def test_checkpoint_format_is_the_references(tmp_path):
     assert (step, t, dur) == (17, 0.125, 3.5) and np.array_equal(U, V)
     with pytest.raises(ValueError):
         checkpoint.read(p, 41)
+
+
+def test_noalloc_rejects_bad_arguments_before_touching_a_device(cuda_lib):
+    """xfg_compute_lu_noalloc checks its arguments and the block's scratch need against the fixed
+    scratch size before any CUDA call; these calls return there (the state pointers are never
+    dereferenced)."""
+    from xfluids_gb300 import cases
+    from xfluids_gb300.abi import MIXED
+    fake = C.c_void_p(256)
+    f = cuda_lib.xfg_compute_lu_noalloc
+
+    def call(b, s, th, U=fake, LU=fake):
+        return f(C.byref(b), C.byref(s), C.byref(th), U, None, LU, None)
+
+    b, s, th, _, _ = cases.isentropic_vortex(32)
+    assert call(b, s, th, U=None) == -1 and "null" in cuda_lib.xfg_last_error().decode()
+    s.precision = MIXED
+    assert call(b, s, th) == -1 and "FP64" in cuda_lib.xfg_last_error().decode()
+    s.precision = 0
+    s.positivity = 1
+    assert call(b, s, th) == -1 and "positivity" in cuda_lib.xfg_last_error().decode()
+    s.positivity = 0
+    big, s2, th2, _, _ = cases.isentropic_vortex(512)
+    assert call(big, s2, th2) == -2
+    assert "XFG_NOALLOC_MAX_SCRATCH_BYTES" in cuda_lib.xfg_last_error().decode()
