@@ -42,6 +42,20 @@ TRANSPORT_TABLES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tes
 NCU_FACE_BYTES_FP64 = (674.218496e6 + 152.813568e6) / (2049 * 2048)
 
 
+def hbm_context(traffic_bytes, launch_ms, peaks_path=os.path.join(ROOT, "MEASURED_PEAKS.json")):
+    """DRAM throughput of one launch of the dominant kernel (ncu traffic per launch over its
+    CUDA-event time) against the measured HBM copy bandwidth of this GPU model, else 6.8 TB/s."""
+    if traffic_bytes is None or not launch_ms:
+        return None
+    try:
+        with open(peaks_path) as f:
+            peak, src = float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, ValueError, KeyError, TypeError):
+        peak, src = 6800.0, "of fallback (6.8 TB/s)"
+    gbs = traffic_bytes / (launch_ms * 1e-3) / 1e9
+    return {"dram_gbs": gbs, "hbm_peak_gbs": peak, "frac": gbs / peak, "peak_source": src}
+
+
 def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -527,6 +541,7 @@ def run_gpu_arm(args, world, rank, local):
                      "traffic_note": "DRAM bytes per launch, ncu capture of the 2048^2 vortex scaled by faces",
                      "algorithmic_flops_per_face": fpf, "faces_per_launch": faces_per_launch,
                      "launch_ms": face_launch_ms,
+                     "hbm": hbm_context(traffic, face_launch_ms),
                      "peak_source": "measured FP64 FMA chain on this GPU (xfg_measure_pipe_peaks); MEASURED_PEAKS.json has no FP64 figure"},
         "phases_ms_per_step": ph,
         "mixed": {"value": value_mixed, "unit": "cell-updates/s", "speedup_vs_fp64": value_mixed / value,

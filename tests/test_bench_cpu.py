@@ -58,3 +58,14 @@ def test_accuracy_leg_with_oracle_stand_in(monkeypatch):
         assert r["l1_vs_oracle"] == 0.0 and r["max_normwise_vs_oracle"] == 0.0
         assert r["l1_rho_vs_exact"] == pytest.approx(acc["oracle_l1_rho_vs_exact"])
         assert np.isfinite(r["linf_rho_vs_exact"]) and r["linf_rho_vs_exact"] > 0.0
+
+
+def test_hbm_context_reads_the_measured_peak_or_falls_back(tmp_path):
+    peaks = tmp_path / "peaks.json"
+    peaks.write_text('{"hbm_gbs": 6000.0}')
+    h = bench.hbm_context(3.0e9, 20.0, peaks_path=str(peaks))
+    assert h["dram_gbs"] == pytest.approx(150.0) and h["hbm_peak_gbs"] == 6000.0
+    assert h["frac"] == pytest.approx(0.025) and h["peak_source"].startswith("of measured")
+    h = bench.hbm_context(3.0e9, 20.0, peaks_path=str(tmp_path / "absent.json"))
+    assert h["hbm_peak_gbs"] == 6800.0 and h["peak_source"].startswith("of fallback")
+    assert bench.hbm_context(None, 20.0) is None
