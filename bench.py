@@ -396,11 +396,11 @@ def accuracy_vs_oracle(runs, threads):
     return out
 
 
-def cpu_leg(threads, accuracy_runs=None):
+def cpu_leg(threads, accuracy_runs=None, size=1024, min_seconds=10.0):
     """The CPU leg of the GPU arm (rank 0): the oracle restatement timed on the host cores
-    (cpu_baseline: steps of the 1024^2 vortex for about 10 s) and, when accuracy runs were made,
-    the oracle as their checker."""
-    val, steps, el = cpu_baseline(1024, threads, min_seconds=10.0)
+    (cpu_baseline: steps of the size^2 vortex for about min_seconds) and, when accuracy runs were
+    made, the oracle as their checker."""
+    val, steps, el = cpu_baseline(size, threads, min_seconds=min_seconds)
     acc = None if accuracy_runs is None else accuracy_vs_oracle(accuracy_runs, threads)
     return val, steps, el, acc
 

@@ -50,7 +50,8 @@ def test_accuracy_leg_with_oracle_stand_in(monkeypatch):
     from xfluids_gb300 import fluid
     monkeypatch.setattr(fluid, "Fluid", _OracleFluid)
     runs = bench.accuracy_gpu(0, n=24, t_end=0.05)
-    acc = bench.accuracy_vs_oracle(runs, threads=2)
+    val, steps, el, acc = bench.cpu_leg(2, runs, size=32, min_seconds=0.2)
+    assert val > 0 and steps >= 1 and el >= 0.2
     assert acc["steps"] > 0
     for name in ("fp64", "mixed"):
         r = acc[name]
