@@ -323,6 +323,14 @@ int xfg_ensemble_active(xfg_ensemble *e);
  * applies the boundary conditions to its own copy of U, recovers the primitives and computes LU
  * as xfg_boundary + xfg_update_states + xfg_compute_lu do, on `stream` (a cudaStream_t, 0 = legacy
  * default stream), without synchronising. FP64 forms only (precision XFG_FP64 or XFG_FP64_STRICT).
+ * Unlike xfg_update_states, the call reports no non-physical state (negative or NaN density,
+ * pressure or temperature in an inner cell): it returns 0 once the launches are queued, and such a
+ * state leaves NaN or Inf in LU, which the caller checks.
+ *
+ * The scratch holds 8 Mi doubles; a block needs (arrays) x (cells rounded up to 64) of them, with
+ * 37 arrays for a 1D single gas (about 226 k cells at most), 50 for a 2D single gas (about 167 k
+ * cells), 63 for a 3D single gas (about 133 k cells) and more for mixtures (96 for a 3D 5-species
+ * mixture, about 87 k cells).
  *
  * Every intermediate array lives in one file-scope device array of XFG_NOALLOC_MAX_SCRATCH_BYTES,
  * which every GPU that loads the library holds until the process exits; blocks that need more are

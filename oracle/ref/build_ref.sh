@@ -6,8 +6,11 @@
 # would set for these flavours. Used only to pin the oracle (test infrastructure).
 #
 # usage: bash oracle/ref/build_ref.sh [flavour ...]   (default: all flavours)
+#        bash oracle/ref/build_ref.sh --root           (print the reference location and exit)
+# The reference location is $XF_REFERENCE, by default the read-only checkout of this container.
 set -euo pipefail
 REF=${XF_REFERENCE:-/root/reference}
+if [ "${1:-}" = "--root" ]; then echo "$REF"; exit 0; fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$(cd "$HERE/.." && pwd)/_ref
 [ -d "$REF/src" ] || { echo "reference sources not found at $REF" >&2; exit 1; }

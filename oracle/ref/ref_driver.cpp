@@ -8,10 +8,13 @@
 //                U, U1, LU (E*ncell each), rho, p, u, v, w, c, H, T (ncell each), y (NUM_SPECIES*ncell)
 //   XFREF_STEPS  number of time steps
 //   XFREF_TEND   end time (the dt clip of XFLUIDS::Evolution)
+//   XFREF_TIMING if set: no per-stage records; the time-step loop is timed (steady clock) and one
+//                line "xfref_time <seconds> <steps>" is printed, the output file gets the final U
 //   XFREF_TRANSPORT (viscous builds) file for the fitted transport coefficients of Setup: int32 NS,
 //                int32 order, visc (NS*order), therm (NS*order), Dkj (NS*NS*order), species_chara
 //                (NS*SPCH_Sz), Yil_limiter, Dim_limiter (doubles)
 // The sequence mirrors main.cpp:36-49 and the loop body of XFLUIDS::Evolution (src/XFLUIDS.cpp:172-214).
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -71,9 +74,12 @@ int main(int argc, char *argv[]) {
     fclose(fi);
 
     FILE *fo = fopen(out, "wb");
+    const bool timing = getenv("XFREF_TIMING") != nullptr;
     solver.physicalTime = 0.0;
     solver.BoundaryCondition(setup.q);
     solver.UpdateStates(setup.q);
+    const auto clock0 = std::chrono::steady_clock::now();
+    int done = 0;
     for (int step = 1; step <= nsteps && solver.physicalTime < tend; step++) {
         Setup::adv_nd[0].resize(1);
         Setup::sbm_id = 0, Setup::adv_id = 0, Setup::adv_push = true;
@@ -88,6 +94,7 @@ int main(int argc, char *argv[]) {
                 fclose(fo);
                 return 4;
             }
+            if (timing) continue;
             double tt = solver.physicalTime;
             put(fo, &step, 4), put(fo, &flag, 4), put(fo, &dt, 8), put(fo, &tt, 8);
             put(fo, fl->d_U, sizeof(real_t) * E * ncell);
@@ -98,6 +105,12 @@ int main(int argc, char *argv[]) {
             for (real_t *a : prim) put(fo, a, sizeof(real_t) * ncell);
             put(fo, d.y, sizeof(real_t) * NUM_SPECIES * ncell);
         }
+        done = step;
+    }
+    if (timing) {
+        const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - clock0).count();
+        printf("xfref_time %.6f %d\n", sec, done);
+        put(fo, fl->d_U, sizeof(real_t) * Emax * ncell);
     }
     fclose(fo);
     return 0;

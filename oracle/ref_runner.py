@@ -30,6 +30,17 @@ FLAVOURS = {
 }
 
 
+def reference_root():
+    """Location of the reference sources: $XF_REFERENCE, else the default of the build recipe
+    (oracle/ref/build_ref.sh --root). None when no reference checkout is there."""
+    root = os.environ.get("XF_REFERENCE")
+    if not root:
+        r = subprocess.run(["bash", os.path.join(HERE, "ref", "build_ref.sh"), "--root"], capture_output=True,
+                           text=True)
+        root = r.stdout.strip() if r.returncode == 0 else ""
+    return root if root and os.path.isdir(os.path.join(root, "src")) else None
+
+
 def available(flavour: str) -> bool:
     return os.access(os.path.join(REF_DIR, flavour, "xfluids_ref"), os.X_OK)
 
@@ -63,6 +74,35 @@ def read_transport(path):
         o += n
     out["ns"], out["order"] = ns, order
     return out
+
+
+def time_reference(flavour, block, U, T=None, steps=1, domain=None):
+    """Seconds the reference build spends in `steps` time steps (its own clock around the step
+    loop, no per-stage records) and its final U (AoS)."""
+    E, NS = FLAVOURS[flavour]
+    if not available(flavour):
+        raise FileNotFoundError(f"reference flavour {flavour} is not built (oracle/ref/build_ref.sh)")
+    if domain is None:
+        domain = (block.dx * block.X_inner, block.dy * block.Y_inner, block.dz * block.Z_inner)
+    N = block.ncell
+    U = np.ascontiguousarray(U, dtype=np.float64).reshape(-1)
+    with open(os.path.join(REF_DIR, flavour, "case.json"), "w") as f:
+        json.dump(_case_json(block, block.CFLnumber, domain), f)
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.bin"), os.path.join(d, "out.bin")
+        with open(fin, "wb") as f:
+            f.write(struct.pack("<iqi", E, N, 1 if T is not None else 0))
+            f.write(U.tobytes())
+            if T is not None:
+                f.write(np.ascontiguousarray(T, dtype=np.float64).tobytes())
+        env = dict(os.environ, XFREF_IN=fin, XFREF_OUT=fout, XFREF_STEPS=str(steps), XFREF_TIMING="1")
+        r = subprocess.run([os.path.join(".", flavour, "xfluids_ref")], cwd=REF_DIR, env=env, capture_output=True,
+                           text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference run failed ({r.returncode}): {r.stderr[-2000:]}")
+        line = [x for x in r.stdout.splitlines() if x.startswith("xfref_time")][-1].split()
+        Uf = np.fromfile(fout, dtype=np.float64)
+    return float(line[1]), int(line[2]), Uf
 
 
 def run_reference(flavour, block, U, T=None, steps=1, t_end=1e300, domain=None, transport_out=None):

@@ -3,7 +3,7 @@
 Each case is run stage by stage through the reference's class XFLUIDS / Fluid, compiled from the
 unmodified reference sources by oracle/ref/build_ref.sh and driven by oracle/ref/ref_driver.cpp.
 The fixture holds the inputs (U, T, block, scheme) and, after every RK stage of 2 steps, dt and the
-inner-cell U and LU; the primitives after the last stage. Needs /root/reference (this container).
+inner-cell U and LU; the primitives after the last stage. Needs the reference sources ($XF_REFERENCE, else the default of oracle/ref/build_ref.sh).
 
 usage: python tests/golden/make_golden.py
 """

@@ -17,7 +17,9 @@ SPECIES = ["H2", "O2", "N2", "H2O", "AR"]
 
 
 def main(runtime_dir=None):
-    runtime_dir = runtime_dir or os.path.join(os.environ.get("XF_REFERENCE", "/root/reference"), "runtime.dat")
+    if not runtime_dir:
+        from oracle.ref_runner import reference_root
+        runtime_dir = os.path.join(reference_root() or "", "runtime.dat")
     out = os.path.join(HERE, "transport_tables.json")
     transport.dump_transport_tables(runtime_dir, SPECIES, out)
     print("wrote", out)

@@ -134,3 +134,12 @@ def test_noalloc_rejects_bad_arguments_before_touching_a_device(cuda_lib):
     big, s2, th2, _, _ = cases.isentropic_vortex(512)
     assert call(big, s2, th2) == -2
     assert "XFG_NOALLOC_MAX_SCRATCH_BYTES" in cuda_lib.xfg_last_error().decode()
+    # a z-only block of 70000 cells fits the scratch (37 arrays x 70 k cells) but not the face
+    # launch's grid limit: rejected by the checks xfg_create makes, before any launch
+    from xfluids_gb300.mesh import make_block, make_scheme, empty_thermal
+    from xfluids_gb300.abi import PERIODIC
+    zb = make_block((0, 0, 70000), (1.0, 1.0, 1.0), [PERIODIC] * 6, bwidth=3)
+    assert call(zb, make_scheme(), empty_thermal()) == -1
+    assert "elongated" in cuda_lib.xfg_last_error().decode()
+    s.artificial_type = 7
+    assert call(b, s, th) == -1 and "artificial_type" in cuda_lib.xfg_last_error().decode()

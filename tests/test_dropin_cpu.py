@@ -9,7 +9,9 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("XF_REFERENCE", "/root/reference")
+from oracle.ref_runner import reference_root
+
+REF = reference_root() or ""
 OUT = os.path.join(ROOT, "oracle", "_ref")
 LIB = os.path.join(ROOT, "xfluids_gb300", "_build", "libxfluids_gb300.so")
 

@@ -106,7 +106,9 @@ def test_flop_count_per_face():
 def test_thermo_reader_matches_fixture():
     import os
     from xfluids_gb300 import thermo
-    rt = "/root/reference/runtime.dat"
+    from oracle.ref_runner import reference_root
+    root = reference_root()
+    rt = os.path.join(root, "runtime.dat") if root else ""
     if not os.path.isdir(rt):
         pytest.skip("reference runtime.dat not present")
     for sp, k in [(cases.MIXING_SPECIES, 0), (["H2", "O2", "AR", "N2"], 1)]:

@@ -1,7 +1,8 @@
 """The transport fits of xfluids_gb300.transport (a restatement of Setup::GetFitCoefficient,
 src/read_ini/src/viscfit.cpp:148-196) against the fitted data the reference produced for the
 viscous golden fixtures: bit for bit, every coefficient, including the H2 fits whose 3000 K node
-reads past the reference's T_star table."""
+reads past the reference's T_star table (reference_layout=True); and the default in-table
+interpolation of the last table interval."""
 import os
 
 import numpy as np
@@ -19,7 +20,8 @@ def test_fit_matches_reference_fixture_bitwise(name):
     th = H.thermal(cases.MIXING_SPECIES, 0)
     ref = H.transport_of(z)
     inv = (ref.yil_limiter,)  # max(1/dx, 1/dy, 1/dz) x clamp(1e10, 0, 1) = max(1/d)
-    tr = transport.fit_transport(cases.MIXING_SPECIES, th, 0, tables_json=TABLES, inv_spacing=inv)
+    tr = transport.fit_transport(cases.MIXING_SPECIES, th, 0, tables_json=TABLES, inv_spacing=inv,
+                                 reference_layout=True)
     ns = 5
     for field, n in (("visc", ns * 4), ("therm", ns * 4), ("dkj", ns * ns * 4), ("species_chara", ns * 9)):
         got = np.array(list(getattr(tr, field))[:n])
@@ -29,13 +31,39 @@ def test_fit_matches_reference_fixture_bitwise(name):
 
 
 def test_fit_from_runtime_dat_equals_fit_from_tables():
-    rt = os.path.join(os.environ.get("XF_REFERENCE", "/root/reference"), "runtime.dat")
+    from oracle.ref_runner import reference_root
+    root = reference_root()
+    rt = os.path.join(root, "runtime.dat") if root else ""
     if not os.path.isdir(rt):
         pytest.skip("reference runtime.dat not present")
     th = H.thermal(cases.MIXING_SPECIES, 1)
-    a = transport.fit_transport(cases.MIXING_SPECIES, th, 1, runtime_dir=rt, inv_spacing=(100.0,))
-    b = transport.fit_transport(cases.MIXING_SPECIES, th, 1, tables_json=TABLES, inv_spacing=(100.0,))
-    assert bytes(a) == bytes(b)
+    for layout in (False, True):
+        a = transport.fit_transport(cases.MIXING_SPECIES, th, 1, runtime_dir=rt, inv_spacing=(100.0,),
+                                    reference_layout=layout)
+        b = transport.fit_transport(cases.MIXING_SPECIES, th, 1, tables_json=TABLES, inv_spacing=(100.0,),
+                                    reference_layout=layout)
+        assert bytes(a) == bytes(b)
+
+
+def test_in_table_interpolation_is_the_default():
+    """By default the last interval of the collision tables interpolates through the last three
+    nodes: the fits that never reach it (O2, N2, H2O, Ar viscosities) equal the reference's bit for
+    bit, and H2's, whose 3000 K node lies there, stay within 2 % of the reference's fitted
+    viscosity over the fitting nodes."""
+    import math
+    th = H.thermal(cases.MIXING_SPECIES, 0)
+    kw = dict(tables_json=TABLES, inv_spacing=(100.0,))
+    ref = transport.fit_transport(cases.MIXING_SPECIES, th, 0, reference_layout=True, **kw)
+    new = transport.fit_transport(cases.MIXING_SPECIES, th, 0, **kw)
+    a = np.array(list(ref.visc)[:20]).reshape(5, 4)
+    b = np.array(list(new.visc)[:20]).reshape(5, 4)
+    assert np.array_equal(a[1:], b[1:])
+    assert not np.array_equal(a[0], b[0])
+    for T in transport.TNODE:
+        L = math.log(T)
+        mu_a = math.exp(sum(a[0][k] * L ** k for k in range(4)))
+        mu_b = math.exp(sum(b[0][k] * L ** k for k in range(4)))
+        assert abs(mu_b / mu_a - 1.0) < 0.02, (T, mu_a, mu_b)
 
 
 def test_least_squares_recovers_an_exact_cubic():

@@ -1,7 +1,8 @@
 """xfg_compute_lu_noalloc: the right-hand side of a state for callers that cannot allocate device
 memory (they pass device pointers in and out; the library's intermediates live in a fixed device
 array). Checked against the allocating path (xfg_create + xfg_boundary + xfg_update_states +
-xfg_compute_lu) on two calls in a row. Collected last on purpose (file name)."""
+xfg_compute_lu) on two calls in a row, and against the oracle's right-hand side of the same state.
+Collected last on purpose (file name)."""
 import ctypes as C
 import ctypes.util
 import glob
@@ -49,6 +50,16 @@ class DevBuf:
         self.rt.cudaFree(self.p)
 
 
+def _oracle_lu(b, s, th, U, T):
+    """The oracle's right-hand side of U and the dt of the same state."""
+    from oracle.xfo import Oracle
+    o = Oracle(b, s, th, U, T)
+    o.boundary(0)
+    o.update_states(0)
+    o.compute_lu(0)
+    return o.get("LU"), o.get_dt()
+
+
 def _reference_lu(b, s, th, U, T):
     from xfluids_gb300.fluid import Fluid
     f = Fluid(b, s, th)
@@ -69,6 +80,7 @@ def test_noalloc_matches_allocating_path_twice(case, cuda_lib):
         b, s, th, U, T = H.mixing_small((16, 12, 8))
     E = s.Emax
     ref = _reference_lu(b, s, th, U, T)
+    oracle, dt = _oracle_lu(b, s, th, U, T)
     rt = _cudart()
     rt.cudaSetDevice(0)
     dU = DevBuf(rt, U.size * 8)
@@ -86,6 +98,15 @@ def test_noalloc_matches_allocating_path_twice(case, cuda_lib):
             got = dLU.get(U.size)
             r = H.normwise(H.inner_aos(b, got, E), H.inner_aos(b, ref, E), E)
             assert np.all(r <= H.PARITY_TOL), f"call {call}: {r}"
+            # against the oracle: per component for the single gas; for the mixture (whose FP64
+            # face sweeps are contracted) through the stage increment max|dt dLU| / max|U|, as the
+            # stage parity tests compare it
+            g, o = H.inner_aos(b, got, E), H.inner_aos(b, oracle, E)
+            if s.cop:
+                ro = np.abs(dt * (g - o)).max(axis=0) / np.abs(H.inner_aos(b, U, E)).max(axis=0).clip(1e-300)
+            else:
+                ro = H.normwise(g, o, E)
+            assert np.all(ro <= H.PARITY_TOL), f"call {call} against the oracle: {ro}"
             ghosts = got.reshape(b.Zmax, b.Ymax, b.Xmax, E).copy()
             ghosts[b.inner_slices()] = 0.0
             assert not ghosts.any()
@@ -96,7 +117,7 @@ def test_noalloc_matches_allocating_path_twice(case, cuda_lib):
 
 
 def test_noalloc_rejects_blocks_beyond_scratch(cuda_lib):
-    b, s, th, U, T = cases.isentropic_vortex(1024)   # needs ~340 MB of scratch > 64 MiB
+    b, s, th, U, T = cases.isentropic_vortex(1024)   # 50 arrays x 1.06 M cells: about 424 MB > 64 MiB
     rc = cuda_lib.xfg_compute_lu_noalloc(C.byref(b), C.byref(s), C.byref(th), C.c_void_p(16), None,
                                          C.c_void_p(16), None)
     assert rc < 0

@@ -146,7 +146,9 @@ struct xfg_handle {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *t) {
+// Argument and block checks shared by xfg_create and xfg_compute_lu_noalloc (declared in xfg_ops.h).
+namespace xfg {
+int validate_block_scheme(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *t) {
     if (!b || !s || !t) return fail(-1, "null argument");
     if (s->scheme_order < 5 || s->scheme_order > 7)
         return fail(-1, "scheme_order must be 5 (WENO5), 6 (WENO-CU6) or 7 (WENO7) (got %d)", s->scheme_order);
@@ -182,6 +184,7 @@ static int validate(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *
         return fail(-1, "block too elongated for the face launches (Z_inner or, in 3D, Y_inner above 65534)");
     return 0;
 }
+}  // namespace xfg
 
 extern "C" {
 
@@ -205,7 +208,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
                xfg_handle **out) {
     if (!out) return fail(-1, "null out");
     *out = nullptr;
-    int v = validate(block, scheme, thermal);
+    int v = validate_block_scheme(block, scheme, thermal);
     if (v) return v;
     // Mixtures with the positivity limiter keep the no-contraction face sweeps in the FP64 form:
     // the limiter's theta = (rho_low - eps) / (rho_low - rho_high) amplifies the rounding of the

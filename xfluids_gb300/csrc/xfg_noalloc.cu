@@ -1,13 +1,14 @@
 // xfg_noalloc.cu - the convective right-hand side of one state without any device allocation.
 //
-// Some callers cannot call cudaMalloc: code running inside a CUDA-graph capture or inside a
-// memory-pool-managed host application that forbids the driver allocator, plugins loaded into a
-// host that owns every allocation, and real-time loops where an allocation (and the implicit
-// synchronisation it may cause) is not allowed. xfg_compute_lu_noalloc serves them: the caller
-// passes device pointers to the input state and to the output right-hand side, and every
-// intermediate array (primitives, physical fluxes, face fluxes, the SoA copy of the state) lives in
-// one file-scope __device__ array of fixed size, g_noalloc_scratch, which every GPU that loads the
-// library holds until the process exits.
+// Some callers cannot call cudaMalloc: plugins loaded into a host application that owns every
+// device allocation (its own pool allocator, a fixed memory budget), and real-time or
+// latency-bound loops in which an allocation, and the synchronisation the driver allocator may
+// imply, is not allowed. xfg_compute_lu_noalloc serves them: the caller passes device pointers to
+// the input state and to the output right-hand side, and every intermediate array (primitives,
+// physical fluxes, face fluxes, the SoA copy of the state) lives in one file-scope __device__
+// array of fixed size, g_noalloc_scratch, which every GPU that loads the library holds until the
+// process exits. The first call on a device looks up the array's device address with that device
+// current; make that first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -73,30 +74,20 @@ size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 extern "C" int xfg_compute_lu_noalloc(const xfg_block *block, const xfg_scheme *scheme, const xfg_thermal *thermal,
                                       const double *U_aos, const double *T, double *LU_aos, void *stream) {
     if (!block || !scheme || !thermal || !U_aos || !LU_aos) return fail(-1, "null argument");
-    if (scheme->scheme_order < 5 || scheme->scheme_order > 7) return fail(-1, "scheme_order must be 5, 6 or 7");
+    // the checks of xfg_create first (scheme switches, sizes, the face launches' grid limits), so
+    // that nothing is launched for a block the kernels cannot cover
+    if (xfg::validate_block_scheme(block, scheme, thermal)) return -1;
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_FP64_STRICT)
         return fail(-1, "xfg_compute_lu_noalloc serves the FP64 forms (precision 0 or 2)");
     if (scheme->viscous) return fail(-1, "xfg_compute_lu_noalloc has no viscous fluxes (they need transport data)");
     if (scheme->positivity)
         return fail(-1, "xfg_compute_lu_noalloc has no positivity limiter (it needs the step's GetDt maxima)");
     if (scheme->cop && !T) return fail(-1, "a mixture needs the temperature T (Newton warm start)");
-    if (scheme->cop && (scheme->num_species < 2 || scheme->num_species > XFG_MAX_SPECIES || thermal->num_species != scheme->num_species))
-        return fail(-1, "num_species out of range or inconsistent with thermal");
     const xfg::Ops *ops = xfg::find_ops(scheme->cop ? 1 : 0, scheme->cop ? scheme->num_species : 1,
                                         scheme->scheme_order, scheme->precision);
     if (!ops) return fail(-1, "no kernels built for this scheme");
     const int dims[3] = {block->DimX, block->DimY, block->DimZ};
     const int ndim = dims[0] + dims[1] + dims[2];
-    const int need = scheme->scheme_order == 7 ? 4 : 3;
-    const int bw[3] = {block->Bwidth_X, block->Bwidth_Y, block->Bwidth_Z};
-    const int inner[3] = {block->X_inner, block->Y_inner, block->Z_inner};
-    const int mx[3] = {block->Xmax, block->Ymax, block->Zmax};
-    if (!ndim) return fail(-1, "no active direction");
-    for (int d = 0; d < 3; d++) {
-        if (dims[d] && (bw[d] < need || inner[d] < bw[d] || mx[d] != inner[d] + 2 * bw[d]))
-            return fail(-1, "inconsistent block sizes");
-        if (!dims[d] && (mx[d] != 1 || inner[d] != 1 || bw[d] != 0)) return fail(-1, "absent direction must be 1/1/0");
-    }
     const int E = scheme->cop ? scheme->num_species + 4 : 5, NS = scheme->cop ? scheme->num_species : 1;
     const long long N = (long long)block->Xmax * block->Ymax * block->Zmax;
     const long long P = (long long)up((size_t)N, 64);

@@ -42,6 +42,11 @@ struct Ops {
 // Message returned by xfg_last_error() on this host thread.
 void set_last_error(const char *msg);
 
+// Checks of a block, scheme and thermal set that every entry point taking them shares: scheme
+// switches in range, Bwidth against the scheme's stencil, consistent sizes, the face launches'
+// grid limits. Returns 0 or -1 with the message set.
+int validate_block_scheme(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *t);
+
 // Registry filled by the instantiation units.
 const Ops *find_ops(int cop, int ns, int order, int precision);
 void register_ops(const Ops *ops);

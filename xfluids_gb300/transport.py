@@ -15,9 +15,15 @@ of the reference's host build. For a reduced temperature between the table's las
 (75 < T* < 100) the reference's Omega_interpolated reads one element past T_star (viscfit.cpp:
 378-386, ti3 = 37) and one row past each Omega table: the element past T_star is the first member
 of the next data member of Setup (Reaction::React_ThirdCoef, a pointer), whose bits read as a
-double are zero or subnormal, and the rows past the tables are the members that follow them. The
-restatement reads the same (_Fitter.mem); this reproduces the reference's fits of H2 and of its
-pairs with N2 and O2, whose nodes at 3000 K fall there.
+double are zero or subnormal, and the rows past the tables are the members that follow them (the
+same happens for a reduced dipole moment in the last interval of delta_star).
+
+fit_transport takes the interpolation nodes inside the tables by default: a quadratic through the
+last three nodes of T_star (and of delta_star) for a point in the last interval, the mathematically
+intended interpolation. reference_layout=True reproduces the reference's reads past the tables
+through the reference's member layout (_Fitter.mem) and with them the reference's fits of H2 and
+of its pairs with N2 and O2, whose nodes at 3000 K fall there, bit for bit: a parity switch for the
+comparisons with the reference build, not a modelling choice.
 """
 from __future__ import annotations
 
@@ -103,7 +109,8 @@ class _Fitter:
     (setupini.h:48-49), so that an index one past delta_star or past a table row reads what the
     reference reads there."""
 
-    def __init__(self, chara, thermal, thermo_kind, coll):
+    def __init__(self, chara, thermal, thermo_kind, coll, reference_layout=False):
+        self.reference_layout = reference_layout
         self.chara = chara
         self.Hia = list(thermal.Hia)
         self.Ri = list(thermal.Ri)
@@ -130,7 +137,9 @@ class _Fitter:
             ii = 1
             while Tstar > T(ii):
                 ii += 1
-            ti = (ii - 1, ii, ii + 1)  # ii = 36 reads past T_star (see the module doc)
+            # ii = 36: the reference reads past T_star (see the module doc); otherwise the last
+            # three nodes
+            ti = (ii - 1, ii, ii + 1) if (ii < 36 or self.reference_layout) else (34, 35, 36)
         elif Tstar <= T(0):
             ti = (0, 1, 2)
         else:
@@ -140,7 +149,7 @@ class _Fitter:
             jj = 1
             while deltastar > dl(jj):
                 jj += 1
-            tj = (jj - 1, jj, jj + 1)
+            tj = (jj - 1, jj, jj + 1) if (jj < 7 or self.reference_layout) else (5, 6, 7)
         elif deltastar <= dl(0):
             tj = (0, 1, 2)
         else:
@@ -270,13 +279,14 @@ def _solve_overdetermined(AA, b):
 
 
 def fit_transport(species, thermal, thermo_kind, runtime_dir=None, tables_json=None, inv_spacing=None,
-                  yil_limiter=1.0e10, dim_limiter=2.0e-3, tnode=None):
+                  yil_limiter=1.0e10, dim_limiter=2.0e-3, tnode=None, reference_layout=False):
     """xfg_transport of a mixture (Setup::GetFitCoefficient, viscfit.cpp:148-196) from the
     Lennard-Jones data and collision tables of runtime.dat (runtime_dir) or of a JSON written by
     dump_transport_tables (tables_json). thermal: the scheme's xfg_thermal (molar masses and the
     heat-capacity tables of thermo_kind, 0 JANAF / 1 NASA-9). inv_spacing: (1/dx, 1/dy, 1/dz) of the
     block for Block::Yil_limiter = max(1/d) * clamp(yil_limiter, 0, 1); dim_limiter: the JSON
-    "Dim_limiter" (iniset.cpp:358-359)."""
+    "Dim_limiter" (iniset.cpp:358-359). reference_layout: reproduce the reference's reads past the
+    collision tables (module doc); off, the last interval interpolates within the tables."""
     from .thermo import transport_from_arrays
     if tables_json is not None:
         with open(tables_json) as f:
@@ -289,7 +299,7 @@ def fit_transport(species, thermal, thermo_kind, runtime_dir=None, tables_json=N
         coll = read_collision_integrals(runtime_dir)
     ns = len(species)
     chara = [list(lj[i]) + [thermal.Wi[i], 0.0, float(i)] for i in range(ns)]
-    fz = _Fitter(chara, thermal, thermo_kind, coll)
+    fz = _Fitter(chara, thermal, thermo_kind, coll, reference_layout=reference_layout)
     tn = TNODE if tnode is None else list(tnode)
     visc, therm = [], []
     dkj = [[None] * ns for _ in range(ns)]
