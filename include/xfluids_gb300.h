@@ -203,7 +203,10 @@ int xfg_pinned_free(void *ptr);
 
 /* One fused step like xfg_step with CUDA events between the launches: ms_out[7] receives the
  * device time of each phase summed over the three stages: [0] dt, [1] boundary, [2] primitive
- * recovery, [3..5] face fluxes x/y/z, [6] divergence + RK update. Advances the state. */
+ * recovery, [3..5] face fluxes x/y/z, [6] divergence + RK update. Advances the state. A handle that
+ * runs the fused mixed stage (2D single gas, XFG_MIXED, WENO5, LLF or Roe, no positivity limiter:
+ * primitive recovery, both face sweeps, divergence and RK update in one kernel per stage) reports
+ * that kernel in [3] and [2], [4..6] are 0; [1] then includes the ghost cells' dt maxima. */
 int xfg_time_phases(xfg_handle *h, double target_t, float *ms_out);
 
 /* Current simulated time of the handle (set by xfg_step / xfg_advance, reset by xfg_set_time). */

@@ -140,6 +140,7 @@ struct xfg_handle {
     double t = 0.0;
     bool states_ready = false;
     bool transport_ready = false;     // viscous schemes: xfg_set_transport called
+    bool fused = false;               // stages run as the fused mixed kernel (xfg_fused.cuh)
     cudaGraphExec_t graph = nullptr;  // one fused step, replayed by xfg_advance
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
@@ -221,6 +222,10 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
         return fail(-1, "no kernels built for cop=%d num_species=%d order=%d precision=%d", scheme->cop,
                     scheme->num_species, scheme->scheme_order, scheme->precision);
     CK(cudaSetDevice(device));
+    if (fused_applies(*block, *scheme, ops)) {  // the fused kernels' shared memory, once per device
+        const cudaError_t fe = (cudaError_t)ops->fused_prepare();
+        if (fe != cudaSuccess) return fail(-2, "fused stage set-up failed: %s", cudaGetErrorString(fe));
+    }
     xfg_handle *h = new xfg_handle();
     h->device = device;
     h->bl = *block;
@@ -232,10 +237,12 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     h->P = (long long)align_up((size_t)h->N, 64);
     const int E = h->E, NS = h->NS;
     const bool mixed = scheme->precision == XFG_MIXED;  // FP32 copies instead of FP64 fluxes
+    h->fused = fused_applies(*block, *scheme, ops);
     const int dims[3] = {block->DimX, block->DimY, block->DimZ};
     const size_t arr8 = (size_t)h->P * 8, arr4 = align_up((size_t)h->P * 4, 256);
     // layout of the pool
     size_t nd = 3 * E + 12 + (scheme->cop ? NS : 0);           // U, U1, LU, primitives, y
+    if (h->fused) nd += E;                                      // U2, the fused stages' third buffer
     if (scheme->cop) nd += 3 + (NS - 1);                        // per-cell sound-speed terms
     if (scheme->viscous && !mixed) nd += 9 + 2;                 // velocity derivatives, mu, kappa
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;  // single-gas fast path extras
@@ -267,6 +274,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     DevFields &f = h->ctx.f;
     std::memset(&f, 0, sizeof f);
     f.U = take8(E), f.U1 = take8(E), f.LU = take8(E);
+    if (h->fused) f.U2 = take8(E);
     f.rho = take8(1), f.u = take8(1), f.v = take8(1), f.w = take8(1), f.p = take8(1), f.H = take8(1);
     f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
     if (scheme->cop) f.y = take8(NS), f.xc = take8(3 + (NS - 1));
@@ -358,6 +366,10 @@ int xfg_set_state(xfg_handle *h, const double *U_aos, const double *T) {
     const long long tot = h->N * h->E;
     k_aos_to_soa<<<grid_for(tot, 256), 256, 0, h->st>>>(h->stage, h->ctx.f.U, h->E, h->N, h->P);
     CK(cudaMemcpyAsync(h->ctx.f.U1, h->ctx.f.U, (size_t)h->P * h->E * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    // the fused stages' first output buffer starts as U1 does: ghost cells of a side whose fill does
+    // nothing (Inflow; slip and viscous walls in y and z) keep the initial state, as U1's do
+    if (h->fused)
+        CK(cudaMemcpyAsync(h->ctx.f.U2, h->ctx.f.U, (size_t)h->P * h->E * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if (T) CK(cudaMemcpyAsync(h->ctx.f.T, T, (size_t)h->N * sizeof(double), cudaMemcpyDefault, h->st));
     CK(cudaMemsetAsync(h->ctx.f.err, 0, 64 * sizeof(int), h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -506,6 +518,8 @@ int xfg_set_array(xfg_handle *h, int which, const double *in) {
         CK(cudaMemcpyAsync(h->stage, in, (size_t)tot * sizeof(double), cudaMemcpyDefault, h->st));
         k_aos_to_soa<<<grid_for(tot, 256), 256, 0, h->st>>>(h->stage, which == XFG_U ? f.U : f.U1, h->E, h->N, h->P);
         CK(cudaGetLastError());
+        if (which == XFG_U1 && h->fused)  // the stage-2 input buffer takes U1's ghost cells
+            CK(cudaMemcpyAsync(f.U2, f.U1, (size_t)h->P * h->E * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     } else {
         return fail(-1, "array %d cannot be set (XFG_U, XFG_U1 or XFG_T)", which);
     }
@@ -560,9 +574,14 @@ int xfg_compute_lu(xfg_handle *h, int flag, float *timers23) {
     if (h->sc.viscous && !h->transport_ready) return fail(-1, "viscous scheme: call xfg_set_transport first");
     CK(cudaSetDevice(h->device));
     CK(cudaEventRecord(h->ev[0], h->st));
-    launch_lu(h, stage_U(h, flag), 0);
-    CK(cudaEventRecord(h->ev[1], h->st));
-    h->ops->div_rk(h->ctx, 0, 0.0, nullptr, 0, 1, 0);
+    if (h->fused) {  // the fused stage recovers its own states and stores LU
+        h->ops->fused(h->ctx, 0, stage_U(h, flag), nullptr, nullptr, nullptr, 0, 1, 0, 0);
+        CK(cudaEventRecord(h->ev[1], h->st));
+    } else {
+        launch_lu(h, stage_U(h, flag), 0);
+        CK(cudaEventRecord(h->ev[1], h->st));
+        h->ops->div_rk(h->ctx, 0, 0.0, nullptr, 0, 1, 0);
+    }
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->ev[2], h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -630,6 +649,18 @@ int xfg_estimate_nan(xfg_handle *h, int flag, int *error, int *error_pos) {
 static void launch_step(xfg_handle *h) {
     DevFields &f = h->ctx.f;
     k_dt_step<<<1, 1, 0, h->st>>>(h->ctx.g, f, h->bl.CFLnumber);
+    if (h->fused) {
+        // U -> U2 -> U1 -> U: a stage never writes the array its tiles read as halo; U1 ends as
+        // the second stage's result, as in the reference
+        h->ops->bc(h->ctx, f.U, f.dtbuf);
+        h->ops->fused(h->ctx, 1, f.U, nullptr, f.U2, f.dtbuf, 1, 0, 0, 1);
+        h->ops->bc(h->ctx, f.U2, f.dtbuf);
+        h->ops->fused(h->ctx, 2, f.U2, f.U, f.U1, f.dtbuf, 1, 0, 0, 1);
+        h->ops->bc(h->ctx, f.U1, f.dtbuf);
+        h->ops->fused_ghost_lam(h->ctx, f.U1, 1);
+        h->ops->fused(h->ctx, 3, f.U1, f.U, f.U, f.dtbuf, 1, 0, 1, 1);
+        return;
+    }
     for (int flag = 1; flag <= 3; flag++) {
         double *UI = flag == 1 ? f.U : f.U1;
         h->ops->bc(h->ctx, UI, f.dtbuf);
@@ -714,6 +745,7 @@ int xfg_launches_per_step(xfg_handle *h, int *n) {
     const int dims = h->bl.DimX + h->bl.DimY + h->bl.DimZ;
     const int glf = h->sc.artificial_type == XFG_GLF ? 1 : 0;
     *n = 1 + 3 * (dims + 1 + glf + dims + 1);  // dt, then per stage: bc per dim, states, [glf], faces per dim, div+rk
+    if (h->fused) *n = 1 + 3 * (dims + 1) + 1;  // dt, per stage: bc per dim, the fused stage; ghost maxima
     return 0;
 }
 
@@ -734,8 +766,19 @@ int xfg_time_phases(xfg_handle *h, double target_t, float *ms_out) {
     CK(cudaEventRecord(ev[ne++], h->st));
     k_dt_step<<<1, 1, 0, h->st>>>(h->ctx.g, f, h->bl.CFLnumber);
     phase_of[ne] = 0;
+    CK(cudaEventRecord(ev[ne++], h->st));
+    // fused stages: [1] boundary (+ ghost-cell dt maxima), [3] the fused stage kernel
+    double *const fin[3] = {f.U, f.U2, f.U1}, *const fout[3] = {f.U2, f.U1, f.U};
+    for (int flag = 1; flag <= 3 && h->fused; flag++) {
+        h->ops->bc(h->ctx, fin[flag - 1], f.dtbuf);
+        if (flag == 3) h->ops->fused_ghost_lam(h->ctx, f.U1, 1);
+        phase_of[ne] = 1;
         CK(cudaEventRecord(ev[ne++], h->st));
-    for (int flag = 1; flag <= 3; flag++) {
+        h->ops->fused(h->ctx, flag, fin[flag - 1], f.U, fout[flag - 1], f.dtbuf, 1, 0, flag == 3, 1);
+        phase_of[ne] = 3;
+        CK(cudaEventRecord(ev[ne++], h->st));
+    }
+    for (int flag = 1; flag <= 3 && !h->fused; flag++) {
         double *UI = flag == 1 ? f.U : f.U1;
         h->ops->bc(h->ctx, UI, f.dtbuf);
         phase_of[ne] = 1;

@@ -76,6 +76,7 @@ inline void geo_split_spacing(Geo &g) {
 // Device arrays of one block. All SoA with the block pitch.
 struct DevFields {
     double *U, *U1, *LU;
+    double *U2;                // third stage buffer of the fused mixed stage (stage 1 output)
     double *rho, *u, *v, *w, *p, *H, *c, *T, *gamma, *e, *Cp, *R;
     double *y;                 // NS components (COP)
     double *F[3];              // physical fluxes per direction (E components)

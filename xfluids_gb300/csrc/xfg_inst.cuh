@@ -7,6 +7,7 @@
 //   xfg_inst_cop<N>_mixed.cu  N-species mixture, mixed form
 #pragma once
 
+#include "xfg_fused.cuh"
 #include "xfg_kernels.cuh"
 #include "xfg_mixed.cuh"
 #include "xfg_ops.h"
@@ -134,13 +135,57 @@ struct Inst {
         }
     }
 
+    // the fused mixed stage (2D single gas, WENO5; fused_applies decides)
+    static FusedK fused_consts(const LaunchCtx &c) {
+        const double gm1 = c.th.ncop_gamma - 1.0;
+        FusedK k;
+        k.gamma = (float)c.th.ncop_gamma;
+        k.gm1h = (float)gm1;
+        k.gm1l = (float)(gm1 - (double)k.gm1h);
+        k.igm1 = (float)(1.0 / gm1);
+        return k;
+    }
+    static void fused(const LaunchCtx &c, int flag, const double *UI, const double *Uprev, double *Uout,
+                      const double *dt_dev, int do_rk, int store_lu, int want_lam, int guard) {
+        if constexpr (MIXED && !COP) {
+            const Geo &g = c.g;
+            const dim3 grid((g.Xi + fz::TX - 1) / fz::TX, (g.Yi + fz::TY - 1) / fz::TY, 1);
+            const size_t smem = sizeof(FusedTile);
+            if (c.artificial == XFG_LLF)
+                k_fused_stage<true><<<grid, fz::THREADS, smem, c.st>>>(g, c.f, fused_consts(c), UI, Uprev, Uout, flag,
+                                                                        0.0, dt_dev, do_rk, store_lu, want_lam, guard);
+            else
+                k_fused_stage<false><<<grid, fz::THREADS, smem, c.st>>>(g, c.f, fused_consts(c), UI, Uprev, Uout, flag,
+                                                                         0.0, dt_dev, do_rk, store_lu, want_lam, guard);
+        }
+    }
+    static int fused_prepare() {
+        if constexpr (MIXED && !COP) {
+            const int smem = (int)sizeof(FusedTile);
+            cudaError_t e = cudaFuncSetAttribute(k_fused_stage<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_fused_stage<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            return (int)e;
+        }
+        return 0;
+    }
+    static void fused_ghost_lam(const LaunchCtx &c, const double *UI, int guard) {
+        if constexpr (MIXED && !COP) {
+            const Geo &g = c.g;
+            const long long n = 2LL * g.By * g.Xmax + 2LL * g.Bx * g.Yi;
+            k_fused_ghost_lam<<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, (float)c.th.ncop_gamma, UI, guard);
+        }
+    }
+
     // tables for scheme orders 5 (WENO5-JS), 6 (WENO-CU6) and 7 (WENO7), registered under
     // precision id `prec`
     static const Ops *table(int order, int prec) {
         static Ops t[3][3];
         Ops &o = t[order - 5][prec];
+        const bool has_fused = MIXED && !COP && order == 5;
         o = Ops{COP ? 1 : 0, NS, order, prec, bc, states, order == 7 ? faces<7> : (order == 6 ? faces<6> : faces<5>),
-                div_rk, glf, rk, estimate_nan, pp, visc};
+                div_rk, glf, rk, estimate_nan, pp, visc, has_fused ? fused : nullptr,
+                has_fused ? fused_ghost_lam : nullptr, has_fused ? fused_prepare : nullptr};
         return &o;
     }
 };

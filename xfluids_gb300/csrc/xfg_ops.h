@@ -37,7 +37,24 @@ struct Ops {
     void (*estimate_nan)(const LaunchCtx &, const double *UI, int *pos);
     void (*pp)(const LaunchCtx &, int d, const double *UI, const double *lam0, int guard);
     void (*visc)(const LaunchCtx &, int guard);   // viscous and heat-conduction fluxes (mixtures)
+    // Fused RK stage of a 2D single-gas block in the mixed form (xfg_fused.cuh): states, face
+    // fluxes, divergence and the stage combination in one launch; null in the other tables.
+    void (*fused)(const LaunchCtx &, int flag, const double *UI, const double *Uprev, double *Uout,
+                  const double *dt_dev, int do_rk, int store_lu, int want_lam, int guard);
+    // GetDt maxima (and FP32 primitives) of the ghost cells, beside the stage-3 fused launch.
+    void (*fused_ghost_lam)(const LaunchCtx &, const double *UI, int guard);
+    // Shared-memory attribute of the fused kernels (called once at handle creation, outside any
+    // stream capture); returns a CUDA error code.
+    int (*fused_prepare)();
 };
+
+// Whether a handle of this block and scheme runs the fused mixed stage: two active directions
+// x and y, single gas, WENO5, LLF or Roe, no positivity limiter.
+inline bool fused_applies(const xfg_block &b, const xfg_scheme &s, const Ops *ops) {
+    return ops && ops->fused && b.DimX && b.DimY && !b.DimZ && !s.cop && s.precision == XFG_MIXED &&
+           s.scheme_order == 5 && (s.artificial_type == XFG_LLF || s.artificial_type == XFG_ROE) && !s.positivity &&
+           !s.viscous;
+}
 
 // Message returned by xfg_last_error() on this host thread.
 void set_last_error(const char *msg);
