@@ -47,7 +47,7 @@ static_assert(TX == 32, "one warp per tile row");
 static_assert(THREADS == 8 * 32 && TY + 1 == 8, "x face rows + 1 warp, y face rows = warps");
 }  // namespace fz
 
-// Shared memory of one tile (70.6 KB): SoA per quantity, region index (r + 3) * RW + (c + 3) for
+// Shared memory of one tile (80.3 KB): SoA per quantity, region index (r + 3) * RW + (c + 3) for
 // tile row r in [-3, TY + 3) and column c in [-3, TX + 3).
 struct FusedTile {
     float uh[5][fz::RC], ul[5][fz::RC];       // U = uh + ul
@@ -56,8 +56,8 @@ struct FusedTile {
     float hh[fz::RC], pr[fz::RC], cs[fz::RC]; // total enthalpy, pressure, sound speed
     float fxh[5][fz::FXN], fxl[5][fz::FXN];   // x flux = fxh + fxl, index r * RW + (c + 3)
     float fyh[5][fz::FYN], fyl[5][fz::FYN];   // y flux, index (r + 3) * TX + c
-    float dvx[5][fz::NXF];                    // x face flux minus the left cell's fxh, r * (TX + 1) + c
-    float dvy[5][fz::NYF];                    // y face flux minus the lower cell's fyh, r * TX + c
+    float2 phx[5][fz::NXF];                   // x face flux as an exact float pair, r * (TX + 1) + c
+    float2 phy[5][fz::NYF];                   // y face flux as an exact float pair, r * TX + c
 };
 
 // Constants of the single-gas equation of state.
@@ -71,9 +71,21 @@ struct FusedK {
 struct fp2 {
     float h, l;
 };
+// FP64 -> float pair by the bit patterns, integer operations and two FP32 operations (no FP64
+// pipe work): h keeps the sign, the exponent and the top 24 significand bits of x (truncated), l the
+// next 23 bits, so h + l equals x to 2^-47 relative. |x| below 2^-126 (zeros included) gives a
+// signed zero, |x| of 2^128 and above (inf, NaN included) a NaN, which the state checks report.
 __device__ __forceinline__ fp2 split_d(double x) {
-    const float h = __double2float_rn(x);
-    return {h, __double2float_rn(x - (double)h)};  // x - h is exact in FP64
+    const unsigned hw = (unsigned)__double2hiint(x), lw = (unsigned)__double2loint(x);
+    const unsigned ex = (hw >> 20) & 0x7ffu, sg = hw & 0x80000000u;
+    const bool normal = ex - 897u < 254u;  // biased FP32 exponent ex - 896 in [1, 254]
+    const unsigned hb = sg | ((ex - 896u) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
+    // the low 29 bits: their top 23 as an exact float (magic-number conversion), scaled by
+    // 2^(ex - 1023 - 52 + 6); below 2^-80 the scale leaves the FP32 range and l is dropped
+    const float m = __uint_as_float(0x4b000000u | ((lw & 0x1fffffffu) >> 6)) - 8388608.0f;
+    const float sc = __uint_as_float(ex >= 943u ? (ex - 942u) << 23 : 0u);
+    const unsigned lb = __float_as_uint(m * sc) | sg;
+    return {__uint_as_float(normal ? hb : (ex > 1150u ? 0x7fc00000u : sg)), __uint_as_float(normal ? lb : sg)};
 }
 // Product: the high parts' product and its exact rounding error (FMA), plus the cross terms.
 __device__ __forceinline__ fp2 mul22(fp2 a, fp2 b) {
@@ -94,38 +106,61 @@ __device__ __forceinline__ float frcp_a(float x) {
     return r;
 }
 
-// WENO5-JS of one side on doubled inputs v = 2 (f +- a u), about the centre value v3: returns the
+// Packed FP32 pairs (FFMA2 / FADD2 / FMUL2: two lanes of arithmetic per instruction).
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// a - b = s + e exactly (TwoSum of a and -b) on packed pairs; fma(x, -1, y) is y - x correctly
+// rounded.
+__device__ __forceinline__ float2 two_diff2(float2 a, float2 b, float2 &e) {
+    const float2 m1 = bc2(-1.f);
+    const float2 sd = fma2(b, m1, a);   // a - b
+    const float2 bv = fma2(a, m1, sd);  // s - a
+    const float2 av = fma2(bv, m1, sd); // s - bv
+    e = fma2(add2(b, bv), m1, fma2(av, m1, a));
+    return sd;
+}
+
+// WENO5-JS of two sides (.x and .y: the plus and the minus side of a face, independent stencils
+// with the same operations) on doubled inputs v = 2 (f +- a u), about the centre value v3: returns the
 // weighted sum num of the candidate offsets and the weight sum den, so that the side's WENO value
 // is v3 / 2 + num / den (weno5old_BODY, WENO5s_schemes.hpp:12-69: indicators 13 a^2 + 3 b^2 + 1e-6,
 // here over 13 with the epsilon scaled by 4 for the doubled input; candidates q_k = v3 + r_k with
 // r_1 = a_1/12 + b_1/4, r_2 = a_2/12 - b_2/4, r_3 = a_3/12 - b_3/4, halved for the doubled input).
 // The weights d_k / s_k^2 are formed against the smallest indicator, d_k (s_min / s_k)^2, so that
 // they lie in [0, d_k] and their sum in [0.1, 1] whatever the scale of the data.
-__device__ __forceinline__ void fz_side(float v1, float v2, float v3, float v4, float v5, float &num, float &den) {
-    constexpr float kW = 3.0f / 13.0f, kEps = 4.0e-6f / 13.0f, kA = 1.0f / 24.0f, kB = 1.0f / 8.0f;
-    const float a1 = fmaf(-2.f, v2, v1) + v3;
-    const float b1 = fmaf(3.f, v3, fmaf(-4.f, v2, v1));
-    const float s1 = fmaf(a1, a1, fmaf(kW * b1, b1, kEps));
-    const float a2 = fmaf(-2.f, v3, v2) + v4;
-    const float b2 = v2 - v4;
-    const float s2 = fmaf(a2, a2, fmaf(kW * b2, b2, kEps));
-    const float a3 = fmaf(-2.f, v4, v3) + v5;
-    const float b3 = fmaf(3.f, v3, fmaf(-4.f, v4, v5));
-    const float s3 = fmaf(a3, a3, fmaf(kW * b3, b3, kEps));
-    const float r1 = fmaf(kA, a1, kB * b1), r2 = fmaf(kA, a2, -kB * b2), r3 = fmaf(kA, a3, -kB * b3);
-    const float sm = fminf(s1, fminf(s2, s3));
-    const float i1 = sm * frcp_a(s1), i2 = sm * frcp_a(s2), i3 = sm * frcp_a(s3);
-    const float w1 = 0.1f * i1 * i1, w2 = 0.6f * i2 * i2, w3 = 0.3f * i3 * i3;
-    den = w1 + w2 + w3;
-    num = fmaf(w3, r3, fmaf(w2, r2, w1 * r1));
+__device__ __forceinline__ void fz_side2(float2 v1, float2 v2, float2 v3, float2 v4, float2 v5, float2 &num,
+                                         float2 &den) {
+    const float2 m2 = bc2(-2.f), p3 = bc2(3.f), m4 = bc2(-4.f), m1 = bc2(-1.f);
+    const float2 kW = bc2(3.0f / 13.0f), kEps = bc2(4.0e-6f / 13.0f), kA = bc2(1.0f / 24.0f);
+    const float2 kB = bc2(1.0f / 8.0f), kNB = bc2(-1.0f / 8.0f);
+    const float2 a1 = add2(fma2(m2, v2, v1), v3);
+    const float2 b1 = fma2(p3, v3, fma2(m4, v2, v1));
+    const float2 s1 = fma2(a1, a1, fma2(mul2(kW, b1), b1, kEps));
+    const float2 a2 = add2(fma2(m2, v3, v2), v4);
+    const float2 b2 = fma2(m1, v4, v2);
+    const float2 s2 = fma2(a2, a2, fma2(mul2(kW, b2), b2, kEps));
+    const float2 a3 = add2(fma2(m2, v4, v3), v5);
+    const float2 b3 = fma2(p3, v3, fma2(m4, v4, v5));
+    const float2 s3 = fma2(a3, a3, fma2(mul2(kW, b3), b3, kEps));
+    const float2 r1 = fma2(kA, a1, mul2(kB, b1)), r2 = fma2(kA, a2, mul2(kNB, b2)), r3 = fma2(kA, a3, mul2(kNB, b3));
+    const float2 sm = make_float2(fminf(s1.x, fminf(s2.x, s3.x)), fminf(s1.y, fminf(s2.y, s3.y)));
+    const float2 i1 = mul2(sm, make_float2(frcp_a(s1.x), frcp_a(s1.y)));
+    const float2 i2 = mul2(sm, make_float2(frcp_a(s2.x), frcp_a(s2.y)));
+    const float2 i3 = mul2(sm, make_float2(frcp_a(s3.x), frcp_a(s3.y)));
+    const float2 w1 = mul2(mul2(bc2(0.1f), i1), i1), w2 = mul2(mul2(bc2(0.6f), i2), i2), w3 = mul2(mul2(bc2(0.3f), i3), i3);
+    den = add2(add2(w1, w2), w3);
+    num = fma2(w3, r3, fma2(w2, r2, mul2(w1, r1)));
 }
-// Face value of one characteristic field from the doubled split values of offsets -2..3 (index
-// 0..5): the plus side reads offsets -2..2, the minus side offsets 3..-1 (weno5old_GPU :71-95).
-__device__ __forceinline__ float fz_weno5(const float *P, const float *M) {
-    float np, dp, nm, dm;
-    fz_side(P[0], P[1], P[2], P[3], P[4], np, dp);
-    fz_side(M[5], M[4], M[3], M[2], M[1], nm, dm);
-    return fmaf(0.5f, P[2] + M[3], fmaf(np, dm, nm * dp) * frcp_a(dp * dm));
+// Face value of one characteristic field: V[k] = (plus side at offset k - 2, minus side at offset
+// 3 - k) for k = 0..4, the doubled split values; the plus side reads offsets -2..2, the minus side
+// offsets 3..-1 (weno5old_GPU :71-95).
+__device__ __forceinline__ float fz_weno5_2(const float2 *V) {
+    float2 num, den;
+    fz_side2(V[0], V[1], V[2], V[3], V[4], num, den);
+    return fmaf(0.5f, V[2].x + V[2].y, fmaf(num.x, den.y, num.y * den.x) * frcp_a(den.x * den.y));
 }
 
 // Deviation flux of one face of direction D (0 = x, 1 = y) of the tile: the face flux minus the
@@ -177,55 +212,78 @@ __device__ __forceinline__ void fused_face(const FusedTile &s, int rcL, int fL, 
     // shear fields: along v and w (x faces), along u and w (y faces), with the signs of
     // RoeAverageLeft: x (v, 0, -1, 0, 0), (-w, 0, 0, 1, 0); y (-u, 1, 0, 0, 0), (w, 0, 0, -1, 0)
     constexpr int ka = D == 0 ? 2 : 1, kb = 3;
-    constexpr float sa = D == 1 ? 1.f : -1.f, sb = D == 0 ? 1.f : -1.f;
     const float va = vel[ka - 1], vb = vel[kb - 1];
-    float uhL[5], fhL[5];
+    // Stencil points in pairs (m, 5 - m), m = 0..2 (offsets m - 2 and 3 - m), every operation on
+    // both points at once. A split pair (a u + f, -a u + f) of the pair gives (P_m, M_{5-m}), the
+    // WENO input pair k = m; (-a u + f, a u + f) gives (M_m, P_{5-m}), swapped into the pair
+    // k = 5 - m (offset 0 is not read by the minus side, offset 3 not by the plus side).
+    // Shear rows are taken without their sign s (x_k - v_k x0 for s (x_k - v_k x0)): WENO is odd,
+    // so the field's flux is s times the unsigned one, and s^2 = 1 in the right eigenvectors.
+    float2 V0[5], V1[5], V4[5], VA[5], VB[5];
+    {
+        float2 uhL[5], fhL[5];
 #pragma unroll
-    for (int n = 0; n < 5; n++) uhL[n] = s.uh[n][rcL], fhL[n] = Fh[n * FN + fL];
-    float P0[6], M0[6], P1[6], M1[6], P4[6], M4[6], PA[6], MA[6], PB[6], MB[6];
+        for (int n = 0; n < 5; n++) uhL[n] = bc2(-s.uh[n][rcL]), fhL[n] = bc2(-Fh[n * FN + fL]);
+        const float2 NU = bc2(-_u), NV = bc2(-_v), NW = bc2(-_w), NUN = bc2(-un), HB2 = bc2(hb2), HB1 = bc2(hb1);
+        const float2 HC1 = bc2(hc1), NENT = bc2(-ent0), NVA = bc2(-va), NVB = bc2(-vb), M1 = bc2(-1.f);
+        const float2 A0 = make_float2(a0, -a0), A1 = make_float2(a1, -a1), A4 = make_float2(a4, -a4);
 #pragma unroll
-    for (int m = 0; m < 6; m++) {
-        const int rc = rcL + (m - 2) * SU, fi = fL + (m - 2) * SF;
-        float x[5], y[5];
+        for (int m = 0; m < 3; m++) {
+            const int rca = rcL + (m - 2) * SU, rcb = rcL + (3 - m) * SU;
+            const int fia = fL + (m - 2) * SF, fib = fL + (3 - m) * SF;
+            float2 x[5], y[5];
 #pragma unroll
-        for (int n = 0; n < 5; n++) {
-            x[n] = (s.uh[n][rc] - uhL[n]) + s.ul[n][rc];
-            y[n] = (Fh[n * FN + fi] - fhL[n]) + Fl[n * FN + fi];
+            for (int n = 0; n < 5; n++) {
+                x[n] = add2(add2(make_float2(s.uh[n][rca], s.uh[n][rcb]), uhL[n]), make_float2(s.ul[n][rca], s.ul[n][rcb]));
+                y[n] = add2(add2(make_float2(Fh[n * FN + fia], Fh[n * FN + fib]), fhL[n]),
+                            make_float2(Fl[n * FN + fia], Fl[n * FN + fib]));
+            }
+            // projections of U (0) and F (1): with mt = x4 - (u x1 + v x2 + w x3) = -T.x,
+            // A = b2/2 x0 + b1/2 mt, B' = (x_{D+1} - un x0) / (2c): acoustic rows A - B', A + B';
+            // the entropy row negated (mt - ent0 x0, its flux enters R with the sign folded back)
+            float2 r0[2], r1[2], r4[2], ra[2], rb[2];
+#pragma unroll
+            for (int a = 0; a < 2; a++) {
+                const float2 *X = a == 0 ? x : y;
+                const float2 mt = fma2(NU, X[1], fma2(NV, X[2], fma2(NW, X[3], X[4])));
+                const float2 av = fma2(HB1, mt, mul2(HB2, X[0]));
+                const float2 bv = mul2(HC1, fma2(NUN, X[0], X[D + 1]));
+                r0[a] = fma2(M1, bv, av);
+                r4[a] = add2(av, bv);
+                r1[a] = fma2(NENT, X[0], mt);
+                ra[a] = fma2(NVA, X[0], X[ka]);
+                rb[a] = fma2(NVB, X[0], X[kb]);
+            }
+            V0[m] = fma2(A0, r0[0], r0[1]);
+            V1[m] = fma2(A1, r1[0], r1[1]);
+            V4[m] = fma2(A4, r4[0], r4[1]);
+            VA[m] = fma2(A1, ra[0], ra[1]);
+            VB[m] = fma2(A1, rb[0], rb[1]);
+            if (m > 0) {
+                const float2 q0 = fma2(mul2(M1, A0), r0[0], r0[1]), q1 = fma2(mul2(M1, A1), r1[0], r1[1]);
+                const float2 q4 = fma2(mul2(M1, A4), r4[0], r4[1]), qa = fma2(mul2(M1, A1), ra[0], ra[1]);
+                const float2 qb = fma2(mul2(M1, A1), rb[0], rb[1]);
+                V0[5 - m] = make_float2(q0.y, q0.x), V1[5 - m] = make_float2(q1.y, q1.x);
+                V4[5 - m] = make_float2(q4.y, q4.x), VA[5 - m] = make_float2(qa.y, qa.x);
+                VB[5 - m] = make_float2(qb.y, qb.x);
+            }
         }
-        float pa[2][3];
-#pragma unroll
-        for (int a = 0; a < 2; a++) {
-            const float *X = a == 0 ? x : y;
-            const float t = fmaf(_u, X[1], fmaf(_v, X[2], fmaf(_w, X[3], -X[4])));
-            const float av = fmaf(hb2, X[0], -hb1 * t);
-            const float bv = hc1 * fmaf(un, X[0], -X[D + 1]);
-            pa[a][0] = av + bv;
-            pa[a][1] = fmaf(ent0, X[0], t);
-            pa[a][2] = av - bv;
-        }
-        P0[m] = fmaf(a0, pa[0][0], pa[1][0]), M0[m] = fmaf(-a0, pa[0][0], pa[1][0]);
-        P1[m] = fmaf(a1, pa[0][1], pa[1][1]), M1[m] = fmaf(-a1, pa[0][1], pa[1][1]);
-        P4[m] = fmaf(a4, pa[0][2], pa[1][2]), M4[m] = fmaf(-a4, pa[0][2], pa[1][2]);
-        const float ua = fmaf(-sa * va, x[0], sa * x[ka]), fa = fmaf(-sa * va, y[0], sa * y[ka]);
-        const float ub = fmaf(-sb * vb, x[0], sb * x[kb]), fb = fmaf(-sb * vb, y[0], sb * y[kb]);
-        PA[m] = fmaf(a1, ua, fa), MA[m] = fmaf(-a1, ua, fa);
-        PB[m] = fmaf(a1, ub, fb), MB[m] = fmaf(-a1, ub, fb);
     }
-    const float fl0 = fz_weno5(P0, M0), fl1 = fz_weno5(P1, M1), fl4 = fz_weno5(P4, M4);
-    const float fla = fz_weno5(PA, MA), flb = fz_weno5(PB, MB);
+    const float fl0 = fz_weno5_2(V0), nfl1 = fz_weno5_2(V1), fl4 = fz_weno5_2(V4);  // nfl1 = -fl1
+    const float fla = fz_weno5_2(VA), flb = fz_weno5_2(VB);  // unsigned shear fluxes
     // right eigenvectors (RoeAverageRight_x/y) in the factored form: S = fl0 + fl4,
     // Sb = S + b1 fl1, Dc = c (fl4 - fl0)
     const float S = fl0 + fl4;
-    const float Sb = fmaf(b1, fl1, S);
+    const float Sb = fmaf(-b1, nfl1, S);
     const float Dc = _c * (fl4 - fl0);
     out[0] = Sb;
 #pragma unroll
     for (int c = 1; c <= 3; c++) {
         if (c == D + 1) out[c] = fmaf(vel[c - 1], Sb, Dc);
-        else if (c == ka) out[c] = fmaf(vel[c - 1], Sb, sa * fla);
-        else out[c] = fmaf(vel[c - 1], Sb, sb * flb);
+        else if (c == ka) out[c] = vel[c - 1] * Sb + fla;
+        else out[c] = vel[c - 1] * Sb + flb;
     }
-    out[4] = fmaf(_H, Sb, fmaf(un, Dc, fmaf(sa * va, fla, fmaf(sb * vb, flb, -fl1))));
+    out[4] = fmaf(_H, Sb, fmaf(un, Dc, fmaf(va, fla, fmaf(vb, flb, nfl1))));
 }
 
 // One RK stage of a 2D single-gas block, mixed form (see the file comment). UI: the stage's input
@@ -352,17 +410,27 @@ __global__ void __launch_bounds__(fz::THREADS, 2)
             r = task < fz::TY ? task : lane, c = task < fz::TY ? lane : fz::TX;
             if (r < fz::TY && x0 + c <= g.Xi && y0 + r < g.Yi) {
                 float out[5];
-                fused_face<0, LLF>(s, (r + fz::HW) * fz::RW + (c + fz::HW) - 1, r * fz::RW + (c + fz::HW) - 1, k, out);
+                const int fL = r * fz::RW + (c + fz::HW) - 1;
+                fused_face<0, LLF>(s, (r + fz::HW) * fz::RW + (c + fz::HW) - 1, fL, k, out);
 #pragma unroll
-                for (int n = 0; n < 5; n++) s.dvx[n][r * (fz::TX + 1) + c] = out[n];
+                for (int n = 0; n < 5; n++) {  // the face flux fxh_L + deviation, exactly as a pair
+                    float e;
+                    const float h = two_sum(s.fxh[n][fL], out[n], e);
+                    s.phx[n][r * (fz::TX + 1) + c] = make_float2(h, e);
+                }
             }
         } else {
             r = task - fz::TY, c = lane;  // face row r: between rows r - 1 and r
             if (x0 + c < g.Xi && y0 + r <= g.Yi) {
                 float out[5];
-                fused_face<1, LLF>(s, (r - 1 + fz::HW) * fz::RW + (c + fz::HW), (r - 1 + fz::HW) * fz::TX + c, k, out);
+                const int fL = (r - 1 + fz::HW) * fz::TX + c;
+                fused_face<1, LLF>(s, (r - 1 + fz::HW) * fz::RW + (c + fz::HW), fL, k, out);
 #pragma unroll
-                for (int n = 0; n < 5; n++) s.dvy[n][r * fz::TX + c] = out[n];
+                for (int n = 0; n < 5; n++) {
+                    float e;
+                    const float h = two_sum(s.fyh[n][fL], out[n], e);
+                    s.phy[n][r * fz::TX + c] = make_float2(h, e);
+                }
             }
         }
     }
@@ -375,17 +443,25 @@ __global__ void __launch_bounds__(fz::THREADS, 2)
             const int i = g.Bx + x0 + c, j = g.By + y0 + r;
             const long long id = (long long)j * g.Xmax + i;
             const double dt = dt_dev ? dt_dev[0] : dt_arg;
-            const int fxc = r * fz::RW + (c + fz::HW), fyc = (r + fz::HW) * fz::TX + c;
             const int dx_ = r * (fz::TX + 1) + c, dy_ = r * fz::TX + c;
+            const float2 IH = make_float2(g.idh[0], g.idh[1]), IL = make_float2(g.idl[0], g.idl[1]);
             int code = 0;
 #pragma unroll
             for (int n = 0; n < 5; n++) {
-                // (Phi_{i-1/2} - Phi_{i+1/2}) / dx with Phi = the left cell's high flux + deviation
-                float sa = 0.f, ca = 0.f;
-                div_acc(s.fxh[n][fxc - 1], s.fxh[n][fxc], g.idh[0], g.idl[0], sa, ca);
-                div_acc(s.dvx[n][dx_], s.dvx[n][dx_ + 1], g.idh[0], g.idl[0], sa, ca);
-                div_acc(s.fyh[n][fyc - fz::TX], s.fyh[n][fyc], g.idh[1], g.idl[1], sa, ca);
-                div_acc(s.dvy[n][dy_], s.dvy[n][dy_ + fz::TX], g.idh[1], g.idl[1], sa, ca);
+                // (Phi_{i-1/2} - Phi_{i+1/2}) / dx + (Phi_{j-1/2} - Phi_{j+1/2}) / dy, x and y packed:
+                // the high difference exact (TwoSum), the low parts and its error beside it, the
+                // products with 1/dx, 1/dy as float pairs; a face flux enters its two cells with
+                // equal and opposite weight, so the sum over cells telescopes
+                const float2 fL = s.phx[n][dx_], fR = s.phx[n][dx_ + 1];
+                const float2 fB = s.phy[n][dy_], fT = s.phy[n][dy_ + fz::TX];
+                float2 e;
+                const float2 d = two_diff2(make_float2(fL.x, fB.x), make_float2(fR.x, fT.x), e);
+                const float2 t = add2(fma2(make_float2(fR.y, fT.y), bc2(-1.f), make_float2(fL.y, fB.y)), e);
+                const float2 pr = mul2(d, IH);
+                const float2 pl = fma2(d, IL, fma2(t, IH, fma2(d, IH, mul2(pr, bc2(-1.f)))));
+                float e2;
+                const float sa = two_sum(pr.x, pr.y, e2);
+                const float ca = e2 + (pl.x + pl.y);
                 const double LU0 = f2d_bits(sa) + f2d_bits(ca);
                 const long long q = n * P + id;
                 if (store_lu) f.LU[q] = LU0;
