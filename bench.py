@@ -253,6 +253,40 @@ def bench_ensemble(args, local, members, scheme, precision):
             "tuned_ms_per_step": [round(t[1], 3) for t in rep["trials"]]}, states
 
 
+def bench_ensemble_solve(local, members, scheme, precision, chunk=256):
+    """Whole solve of the batched ensemble to its end time t = 0.25: every member advanced until it
+    is done; members that finished (or stopped on a numerical error) leave the launch tables after
+    each chunk of graph-replayed steps. Device time (CUDA events) and wall time of the solve,
+    cell-updates performed, the members stopped by an error."""
+    from xfluids_gb300.ensemble import Ensemble
+    scheme.precision = precision
+    pool = sum(Ensemble.member_bytes(b, precision) for b, _ in members) + 4096 * len(members)
+    e = Ensemble(scheme, capacity=len(members), pool_bytes=pool, device=local)
+    failed, work, dev_ms, chunks = [], 0, 0.0, 0
+    try:
+        live = {e.add(b, U, 0.25): q for q, (b, U) in enumerate(members)}
+        assert None not in live
+        t0 = time.perf_counter()
+        while live:
+            _, ms = e.advance(chunk)
+            dev_ms += ms
+            chunks += 1
+            for slot in list(live):
+                info = e.status(slot)
+                if info["done"]:
+                    q = live.pop(slot)
+                    work += members[q][0].X_inner * members[q][0].Y_inner * info["steps"]
+                    if info["error"]:
+                        failed.append(q)
+                    e.remove(slot)
+        wall = time.perf_counter() - t0
+    finally:
+        e.close()
+    return {"t_end": 0.25, "device_s": dev_ms * 1e-3, "wall_s": wall, "cell_updates": work,
+            "cell_updates_per_s": work / (dev_ms * 1e-3), "failed_members": sorted(failed), "chunks": chunks,
+            "steps_per_chunk": chunk}
+
+
 def bench_serving(local, count, precision, fp64_check_work=3e8):
     """Continuous-batching server on the first `count` requests of the seeded Poisson trace
     (mean 200 req/s, 1D and 2D Riemann solves, N per side round(2^U[8,11]), t_end U[0.1,0.3]);
@@ -337,8 +371,8 @@ def bench_mixing_layer(args, local, steps):
     # momentum components against the mean magnitude of the momentum vector (the transverse
     # components carry only the 1% noise, so their own mean is not their scale)
     mom = np.sqrt((states[0][:, 1:4] ** 2).sum(axis=1)).mean()
-    per = {names[n]: {"l1": float(d[:, n].mean()), "mean_abs": float(scale[n]), "max_abs": float(np.abs(states[0][:, n]).max())}
-           for n in range(9)}
+    from xfluids_gb300.workloads import per_component
+    per = per_component(states[MIXED], states[0], names)
     vec_scale = np.array([scale[0], mom, mom, mom, scale[4]] + [scale[0]] * 4)
     l1_state = float((d[:, live].mean(axis=0) / vec_scale[live]).max())
     d, states[0], scale = d[:, live], states[0][:, live], scale[live]
@@ -499,7 +533,10 @@ def run_gpu_arm(args, world, rank, local):
     Umi = Um.reshape(b.Zmax, b.Ymax, b.Xmax, E)[b.inner_slices()]
     l1 = float(np.abs(Umi - Ui).mean())
     linf = float(np.abs(Umi - Ui).max())
+    from xfluids_gb300.workloads import per_component
+    mixed_components = per_component(Umi.reshape(-1, E), Ui.reshape(-1, E))
     phases_m = fm.time_phases()
+    # the fused mixed stage kernel (one launch per stage) is reported in the faces_x phase
     mixed_face_ms = phases_m["faces_x"] / 3.0
     fm.close()
     f.close()
@@ -524,6 +561,8 @@ def run_gpu_arm(args, world, rank, local):
                "l1_mixed_vs_fp64": float(sum(x.sum() for x in diff) / (ncell_all * 5)),
                "linf_mixed_vs_fp64": float(max(x.max() for x in diff))}
         del s64, smx, diff
+        if args.ensemble_solve:
+            ens["whole_solve_mixed"] = bench_ensemble_solve(local, members, scheme_e, MIXED)
     serving = bench_serving(local, args.serve_requests, MIXED) if args.serve_requests > 0 else None
     mixing = bench_mixing_layer(args, local, args.mixing_steps) if args.mixing_steps > 0 else None
     accuracy_runs = accuracy_gpu(local) if args.accuracy else None
@@ -556,7 +595,14 @@ def run_gpu_arm(args, world, rank, local):
         "phases_ms_per_step": ph,
         "mixed": {"value": value_mixed, "unit": "cell-updates/s", "speedup_vs_fp64": value_mixed / value,
                   "steps": km, "l1_vs_fp64": l1, "linf_vs_fp64": linf, "t": tm,
-                  "faces_x_launch_ms": mixed_face_ms, "phases_ms_per_step": phases_m,
+                  "per_component_vs_fp64": mixed_components,
+                  "fused_stage_launch_ms": mixed_face_ms, "phases_ms_per_step": phases_m,
+                  "roofline": {"bound": "fp32 (instruction issue)", "kernel": "k_fused_stage (2D mixed RK stage)",
+                               "achieved": FLOPS_PER_CELL_UPDATE / 3.0 * n * n / (mixed_face_ms * 1e-3) / 1e12,
+                               "peak": peaks["fp32_flops"] / 1e12, "unit": "TFLOP/s",
+                               "frac": FLOPS_PER_CELL_UPDATE / 3.0 * n * n / (mixed_face_ms * 1e-3) / peaks["fp32_flops"],
+                               "note": "algorithmic flops of one RK stage (the oracle's count, a third of a "
+                                       "cell-update's) over the launch time; peak: measured scalar FP32 FMA chain"},
                   "fp32_peak_tflops": peaks["fp32_flops"] / 1e12},
         "ensemble": ens or None,
         "serving": serving,
@@ -580,7 +626,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=4096)
     ap.add_argument("--ensemble", type=int, default=1, help="run the 256-member batched ensemble (0 = skip)")
-    ap.add_argument("--serve-requests", type=int, default=8, help="requests of the serving trace (0 = skip)")
+    ap.add_argument("--ensemble-solve", type=int, default=1, help="whole mixed solve of the ensemble to t = 0.25 (0 = skip)")
+    ap.add_argument("--serve-requests", type=int, default=100, help="requests of the serving trace (0 = skip)")
     ap.add_argument("--mixing-steps", type=int, default=2, help="timed steps of the 3D mixing layer (0 = skip)")
     ap.add_argument("--accuracy", type=int, default=1, help="FP64 drift vs the oracle and error vs the exact vortex")
     args = ap.parse_args()

@@ -815,6 +815,23 @@ void face_flux(const Config &cf, const ThermoTable &tt, const Fields<R> &f, cons
     (void)out;
 }
 
+// max over cells id in [0, n) of term(id), starting from init: the reference's SYCL max
+// reductions, over the threads (fmax is order-independent, so the result does not depend on them).
+template <class R, class T>
+R max_over_cells(long n, R init, T term) {
+    using std::fmax;
+    R mx = init;
+#pragma omp parallel
+    {
+        R loc = init;
+#pragma omp for schedule(static) nowait
+        for (long id = 0; id < n; id++) loc = fmax(loc, term(id));
+#pragma omp critical(xfo_max_over_cells)
+        mx = fmax(mx, loc);
+    }
+    return mx;
+}
+
 // GetLocalEigen, Eigen_value.hpp:5-36, for direction d on all cells.
 template <class R>
 void local_eigen(const Config &cf, Fields<R> &f, int d) {
@@ -854,11 +871,9 @@ void lu_eigen(const Config &cf, Fields<R> &f) {
         // ConVenction_block.hpp:115-215: the SYCL max reduction folds in the previous value of
         // eigen_block (zeroed once at allocation, src/Fluids.cpp:421-429), so the GLF maxima are
         // running maxima over every GetLU call of the run
-        for (int n = 0; n < E; n++) {
-            R mx = f.eigen_block[d][n];
-            for (long id = 0; id < ncell; id++) mx = fmax(mx, fabs(f.eig[d][E * id + n]));
-            f.eigen_block[d][n] = mx;
-        }
+        const std::vector<R> &eg = f.eig[d];
+        for (int n = 0; n < E; n++)
+            f.eigen_block[d][n] = max_over_cells(ncell, f.eigen_block[d][n], [&](long id) { return fabs(eg[E * id + n]); });
     }
 }
 
@@ -1310,12 +1325,11 @@ R get_dt(const Config &cf, Fields<R> &f) {
     for (int d = 0; d < 3; d++) {
         f.uvw_c_max[d] = R(0.0);
         if (!dims[d]) continue;
-        R mx = R(0.0);
-        for (long id = 0; id < n; id++) {
+        const std::vector<R> &vd = *vel[d];
+        f.uvw_c_max[d] = max_over_cells(n, R(0.0), [&](long id) {
             R c_local = sqrt(R(1.4) * f.p[id] / f.rho[id]);
-            mx = fmax(mx, fabs((*vel[d])[id]) + c_local);
-        }
-        f.uvw_c_max[d] = mx;
+            return fabs(vd[id]) + c_local;
+        });
     }
     R dtref = f.uvw_c_max[0] * b._dx + f.uvw_c_max[1] * b._dy + f.uvw_c_max[2] * b._dz;
     return R(b.CFLnumber) / dtref;

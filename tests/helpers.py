@@ -11,6 +11,7 @@ from xfluids_gb300.mesh import make_block, make_scheme, empty_thermal
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 THERMO_JSON = os.path.join(GOLDEN, "thermo_tables.json")
+TRANSPORT_JSON = os.path.join(GOLDEN, "transport_tables.json")
 
 # per-stage parity bound of the FP64 path against the oracle (normwise relative, per component)
 PARITY_TOL = 1e-12

@@ -114,6 +114,32 @@ def random_case(seed, cop=None, order=None, art=None, pos=None, thermo_kind=None
     return b, s, th, np.ascontiguousarray(U.reshape(-1, 9)), np.ascontiguousarray(T.reshape(-1))
 
 
+GHOST_SPECIES = ["H2", "O2", "AR", "N2"]
+
+
+def ghost_species_case(seed):
+    """Random block and boundary kinds of random_case(seed) with a random 4-species NASA-9 state
+    (H2, O2, AR, N2), the last species a ghost species (not transported: its mass fraction is
+    1 minus the others)."""
+    b, _, _, _, _ = random_case(seed, cop=False, order=5, art=LLF, pos=False)
+    rng = np.random.default_rng(9000 + seed)
+    th = H.thermal(GHOST_SPECIES, 1)
+    s = make_scheme(cop=True, num_species=4, scheme_order=5, artificial_type=LLF, thermo=1, ghost_species=True)
+    X, Y, Z = cases.cell_centres(b)
+    T = fill_ghosts_like_bc(b, _field(rng, b, X, Y, Z, 900.0, 0.2, float(rng.uniform(-0.4, 0.4))))
+    p = _field(rng, b, X, Y, Z, 1.0e5, 0.1, float(rng.uniform(-0.2, 0.2)))
+    Ys = np.stack([_field(rng, b, X, Y, Z, float(rng.uniform(0.05, 0.3)), 0.2, float(rng.uniform(-0.3, 0.3)))
+                   for _ in range(3)], axis=-1)
+    Ys = np.concatenate([Ys, 1.0 - Ys.sum(-1, keepdims=True)], axis=-1)
+    R = thermo.RU * sum(Ys[..., q] / th.Wi[q] for q in range(4))
+    rho = p / (R * T)
+    h = sum(Ys[..., q] * cases.species_cp_h(th, q, T, nasa=True)[1] for q in range(4))
+    u, v, w = [60.0 * (_field(rng, b, X, Y, Z, 1.0, 0.3, 0.0) - 1.0) * d for d in (b.DimX, b.DimY, b.DimZ)]
+    E = rho * (h - R * T + 0.5 * (u * u + v * v + w * w))
+    U = np.concatenate([np.stack([rho, rho * u, rho * v, rho * w, E], axis=-1), rho[..., None] * Ys[..., :3]], axis=-1)
+    return b, s, th, np.ascontiguousarray(U.reshape(-1, 8)), np.ascontiguousarray(T.reshape(-1))
+
+
 @pytest.mark.parametrize("precision", [FP64, FP64_STRICT], ids=["fp64", "strict"])
 @pytest.mark.parametrize("seed", range(16))
 def test_random_case_matches_oracle(seed, precision, cuda_lib):
@@ -203,3 +229,28 @@ def test_smallest_and_ragged_blocks_match_oracle(name, precision, cuda_lib):
     res, dom, bc, order, cop = TINY[name]
     worst = run_stagewise(_tiny_case(res, dom, bc, order, cop), steps=2, precision=precision)
     print(f"{name}: worst {worst:.2e}")
+
+
+@pytest.mark.parametrize("precision", [FP64, FP64_STRICT], ids=["fp64", "strict"])
+@pytest.mark.parametrize("seed", range(8))
+def test_random_viscous_case_matches_oracle(seed, precision, cuda_lib):
+    """Viscous stress, heat conduction and species diffusion on the random blocks and boundary
+    kinds of the reference-pinned viscous cases (walls, inflow, symmetry included; the 5-species
+    JANAF mixture, WENO5 LLF), with transport data fitted for the block's spacing."""
+    from xfluids_gb300 import transport
+    b, s, th, U, T = random_case(200 + seed, cop=True, order=5, art=LLF, pos=False, thermo_kind=0)
+    s.viscous = 7
+    tr = transport.fit_transport(cases.MIXING_SPECIES, th, 0, tables_json=H.TRANSPORT_JSON,
+                                 inv_spacing=(b._dx, b._dy, b._dz))
+    worst = run_stagewise((b, s, th, U, T), steps=2, precision=precision, transport=tr)
+    print(f"viscous seed {seed}: dims {b.DimX}{b.DimY}{b.DimZ} bc {list(b.Boundarys)}: worst {worst:.2e}")
+
+
+@pytest.mark.parametrize("precision", [FP64, FP64_STRICT], ids=["fp64", "strict"])
+@pytest.mark.parametrize("seed", range(8))
+def test_random_ghost_species_case_matches_oracle(seed, precision, cuda_lib):
+    """GhostSpecies (renormalised mass fractions written back into U) with NASA-9 polynomials on
+    the random blocks and boundary kinds of the reference-pinned GhostSpecies cases."""
+    b, s, th, U, T = ghost_species_case(300 + seed)
+    worst = run_stagewise((b, s, th, U, T), steps=2, precision=precision)
+    print(f"ghost seed {seed}: dims {b.DimX}{b.DimY}{b.DimZ} bc {list(b.Boundarys)}: worst {worst:.2e}")

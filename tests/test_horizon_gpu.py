@@ -3,11 +3,14 @@
 - Sod shock tube, 1024 cells to t = 0.2: the strict form and the FP64 form run free next to the
   oracle for every step of the solve; the density is compared with the exact Riemann solution.
 - 2D isentropic vortex, 10 periods (t = 100, the exact solution is the initial state): the FP64
-  form against the oracle on a 32^2 grid (about 3700 steps), and the mixed form against FP64.
+  form against the oracle on a 32^2 grid (about 3700 steps), and the mixed form against FP64 at
+  64^2, 128^2, 512^2 (and 1024^2 on request): L1 per conserved component within 1e-6 of its mean.
 
 Every measured figure is printed before it is checked. The bounds are drift bounds over the whole
 solve, not the per-stage parity bound.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -85,8 +88,19 @@ def test_vortex_ten_periods_fp64_against_oracle(cuda_lib):
     assert res["fp64"][3] <= 1e-9, res["fp64"]
 
 
-@pytest.mark.parametrize("n", [64, 128])
+MIXED_L1_BOUND = 1e-6   # mixed against FP64, L1 per conserved component over its own mean
+
+
+@pytest.mark.parametrize("n", [
+    64, 128, 512,
+    pytest.param(1024, marks=pytest.mark.skipif(
+        not os.environ.get("XFG_HORIZON_1024"),
+        reason="the FP64 reference solve of 1024^2 over 10 periods takes about 18 min; set XFG_HORIZON_1024=1")),
+])
 def test_vortex_ten_periods_mixed_against_fp64(n, cuda_lib):
+    """The vortex over its 10 periods (t = 100) in FP64 and in the mixed form: every conserved
+    component of the mixed state within 1e-6 of the FP64 state in L1 relative to its own mean, and
+    the totals kept to the FP64 stage arithmetic's level."""
     from xfluids_gb300.workloads import vortex_horizon
     out = vortex_horizon(n, 10, precisions=(FP64, MIXED), chunk=2048)
     print(out)
@@ -96,5 +110,7 @@ def test_vortex_ten_periods_mixed_against_fp64(n, cuda_lib):
         # arithmetic); the FP32 face fluxes must add nothing to that
         assert abs(out[name]["mass_drift_rel"]) <= 2e-16 * out[name]["steps"], out[name]
     assert out["fp64"]["steps"] == out["mixed"]["steps"] or abs(out["fp64"]["steps"] - out["mixed"]["steps"]) <= 1
-    # FP32 reconstruction against FP64 after the whole solve
-    assert max(out["mixed_vs_fp64"]["l1_rel"]) <= 1e-5, out["mixed_vs_fp64"]
+    pc = out["mixed_vs_fp64"]["per_component"]
+    for nm in ("rho", "rho_u", "rho_v", "E"):
+        assert pc[nm]["l1_rel"] <= MIXED_L1_BOUND, (nm, pc)
+    assert pc["rho_w"]["linf"] == 0.0   # a 2D flow without w keeps rho w = 0 exactly

@@ -27,7 +27,7 @@ import pytest
 import helpers as H
 from oracle import ref_runner
 from oracle.xfo import Oracle
-from test_fuzz_gpu import _field, fill_ghosts_like_bc, random_case
+from test_fuzz_gpu import GHOST_SPECIES, ghost_species_case, random_case
 from xfluids_gb300 import cases, thermo
 from xfluids_gb300.abi import GLF, INFLOW, LLF, NSLIPWALL, OUTFLOW, ROE, SLIPWALL, VISCWALL
 from xfluids_gb300.mesh import make_scheme
@@ -69,7 +69,6 @@ SEEDS = range(6 * len(NAMES))
 
 VISCOUS = "cop5_w5_llf_janaf_visc"
 GHOST = "cop4g_w5_llf_nasa"
-GHOST_SPECIES = ["H2", "O2", "AR", "N2"]
 
 pytestmark = pytest.mark.skipif(not all(ref_runner.available(f) for f in NAMES + [VISCOUS, GHOST]),
                                 reason="reference flavours not built (oracle/ref/build_ref.sh)")
@@ -132,29 +131,6 @@ def test_oracle_equals_reference_on_random_viscous_case(seed, tmp_path):
     t = ref_runner.read_transport(tpath)
     tr = thermo.transport_from_arrays(5, t["visc"], t["therm"], t["dkj"], t["chara"], *t["limits"])
     _compare_stages(b, s, th, U, T, recs, transport=tr)
-
-
-def ghost_species_case(seed):
-    """Random block and boundary kinds of random_case(seed) with a random 4-species NASA-9 state
-    (H2, O2, AR, N2), the last species a ghost species (not transported: its mass fraction is
-    1 minus the others)."""
-    b, _, _, _, _ = random_case(seed, cop=False, order=5, art=LLF, pos=False)
-    rng = np.random.default_rng(9000 + seed)
-    th = H.thermal(GHOST_SPECIES, 1)
-    s = make_scheme(cop=True, num_species=4, scheme_order=5, artificial_type=LLF, thermo=1, ghost_species=True)
-    X, Y, Z = cases.cell_centres(b)
-    T = fill_ghosts_like_bc(b, _field(rng, b, X, Y, Z, 900.0, 0.2, float(rng.uniform(-0.4, 0.4))))
-    p = _field(rng, b, X, Y, Z, 1.0e5, 0.1, float(rng.uniform(-0.2, 0.2)))
-    Ys = np.stack([_field(rng, b, X, Y, Z, float(rng.uniform(0.05, 0.3)), 0.2, float(rng.uniform(-0.3, 0.3)))
-                   for _ in range(3)], axis=-1)
-    Ys = np.concatenate([Ys, 1.0 - Ys.sum(-1, keepdims=True)], axis=-1)
-    R = thermo.RU * sum(Ys[..., q] / th.Wi[q] for q in range(4))
-    rho = p / (R * T)
-    h = sum(Ys[..., q] * cases.species_cp_h(th, q, T, nasa=True)[1] for q in range(4))
-    u, v, w = [60.0 * (_field(rng, b, X, Y, Z, 1.0, 0.3, 0.0) - 1.0) * d for d in (b.DimX, b.DimY, b.DimZ)]
-    E = rho * (h - R * T + 0.5 * (u * u + v * v + w * w))
-    U = np.concatenate([np.stack([rho, rho * u, rho * v, rho * w, E], axis=-1), rho[..., None] * Ys[..., :3]], axis=-1)
-    return b, s, th, np.ascontiguousarray(U.reshape(-1, 8)), np.ascontiguousarray(T.reshape(-1))
 
 
 @pytest.mark.parametrize("seed", range(12))

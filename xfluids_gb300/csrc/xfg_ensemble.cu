@@ -21,6 +21,7 @@
 
 #include "../../include/xfluids_gb300.h"
 #define XFG_KNS ens
+#include "xfg_fused.cuh"
 #include "xfg_kernels.cuh"
 #include "xfg_mixed.cuh"
 #include "xfg_ops.h"
@@ -38,12 +39,14 @@ struct Member {
     int bc[6];
     int active;
     int ltx;  // face tile of this member: 2^ltx faces along x by kThreads >> ltx across
+    int fused;  // 2D member of a mixed WENO5 LLF / Roe ensemble: its stages run as fused tiles
     unsigned long long *glf;  // GLF running maxima (9 words in the member's small-word area)
 };
 
 // phases with a block table; PH_FALL holds three entries per member (x, y, z face sweeps of the
-// fused face launch), the others one
-enum { PH_BC0, PH_BC1, PH_BC2, PH_STATES, PH_F0, PH_F1, PH_F2, PH_DIV, PH_FALL, PH_N };
+// fused face launch), the others one. PH_FUSED: the 32 x 7 tiles of the fused mixed stage
+// (xfg_fused.cuh) of the fused members, PH_GLAM: their ghost cells' dt maxima.
+enum { PH_BC0, PH_BC1, PH_BC2, PH_STATES, PH_F0, PH_F1, PH_F2, PH_DIV, PH_FALL, PH_FUSED, PH_GLAM, PH_N };
 
 // size classes with their own face tile: 1D, 2D below 384 cells per side, 2D from 384, 3D
 enum { CL_1D, CL_2D_SMALL, CL_2D_LARGE, CL_3D, CL_N };
@@ -66,7 +69,30 @@ __global__ void __launch_bounds__(kThreads) kb_bc(const Member *__restrict__ M, 
     const Member &m = M[mi];
     if (member_done(m)) return;
     const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
-    bc_body<D, 5>(m.g, flag == 1 || flag == 0 ? m.f.U : m.f.U1, m.bc[2 * D], m.bc[2 * D + 1], t);
+    // a fused member's second stage reads U2, the first stage's output
+    double *UI = flag == 1 || flag == 0 ? m.f.U : (flag == 2 && m.fused ? m.f.U2 : m.f.U1);
+    bc_body<D, 5>(m.g, UI, m.bc[2 * D], m.bc[2 * D + 1], t);
+}
+
+// One stage of the fused members: CTA = one 32 x 7 tile of one member (fused_stage_tile), stage
+// buffers U -> U2 -> U1 -> U as in the single-grid fused step.
+template <bool LLF>
+__global__ void __launch_bounds__(fz::THREADS, 2)
+    kb_fused(const Member *__restrict__ M, const int *__restrict__ off, int n, FusedK k, int flag) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    const int lb = blockIdx.x - off[mi], tx = (m.g.Xi + fz::TX - 1) / fz::TX;
+    const double *UI = flag == 1 ? m.f.U : (flag == 2 ? m.f.U2 : m.f.U1);
+    double *Uout = flag == 1 ? m.f.U2 : (flag == 2 ? m.f.U1 : m.f.U);
+    fused_stage_tile<LLF>(m.g, m.f, k, UI, m.f.U, Uout, flag, m.f.dtbuf[0], 1, 0, flag == 3, lb % tx, lb / tx);
+}
+__global__ void __launch_bounds__(kThreads) kb_fused_ghost(const Member *__restrict__ M, const int *__restrict__ off,
+                                                           int n, float gamma) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const Member &m = M[mi];
+    if (member_done(m)) return;
+    fused_ghost_lam_body(m.g, m.f, gamma, m.f.U1, (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x);
 }
 
 template <bool MIXED>
@@ -322,16 +348,21 @@ struct xfg_ensemble {
     int fused_faces = 0;                  // one launch for all face sweeps
     int graph_steps = 1;                  // fused steps per captured graph
     int ltx[CL_N] = {7, 5, 5, 5};         // face tile per size class
+    bool fused_ok = false;                // mixed WENO5 LLF / Roe without limiter: 2D members fused
+    FusedK fk{};
 };
 
 namespace {
 
 size_t row_len(const xfg_ensemble *e) { return 3 * (size_t)e->capacity + 1; }
 
+bool two_d(const xfg_block &b) { return b.DimX && b.DimY && !b.DimZ; }
+
 size_t member_bytes(const xfg_block &b, bool mixed) {
     const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
     const int dims = b.DimX + b.DimY + b.DimZ;
     size_t nd = 3 * 5 + 12;                              // U, U1, LU, primitives
+    if (mixed && two_d(b)) nd += 5;                      // U2 of the fused stages
     if (!mixed) nd += 2 * 5 * dims + 2 + 3 * dims;       // F, Fw, sqrt(rho), 1/sqrt(rho), |lambda|
     size_t bytes = nd * P * 8;
     if (mixed) bytes += (size_t)(5 + 7 + 2 * 5 * dims) * up(P * 4, 256);
@@ -347,6 +378,7 @@ void carve(Member &m, char *base, const xfg_block &b, bool mixed) {
     DevFields &f = m.f;
     std::memset(&f, 0, sizeof f);
     f.U = t8(5), f.U1 = t8(5), f.LU = t8(5);
+    if (mixed && two_d(b)) f.U2 = t8(5);
     f.rho = t8(1), f.u = t8(1), f.v = t8(1), f.w = t8(1), f.p = t8(1), f.H = t8(1);
     f.c = t8(1), f.T = t8(1), f.gamma = t8(1), f.e = t8(1), f.Cp = t8(1), f.R = t8(1);
     if (!mixed) {
@@ -386,9 +418,14 @@ int face_blocks(const Geo &g, int d, int ltx) {
     return (int)(b.x * b.y * b.z);
 }
 
-int blocks_of(const Geo &g, int ph, int ltx) {
+int blocks_of(const Member &m, int ph, int ltx) {
+    const Geo &g = m.g;
     const long long N = g.ncell(), inner = (long long)g.Xi * g.Yi * g.Zi;
     auto gb = [](long long n) { return (int)((n + kThreads - 1) / kThreads); };
+    if (ph == PH_FUSED)
+        return m.fused ? ((g.Xi + fz::TX - 1) / fz::TX) * ((g.Yi + fz::TY - 1) / fz::TY) : 0;
+    if (ph == PH_GLAM) return m.fused ? gb(fused_ghost_cells(g)) : 0;
+    if (m.fused && ph >= PH_STATES && ph <= PH_DIV) return 0;  // done by the fused tiles
     switch (ph) {
     case PH_BC0: return g.dimx ? gb((long long)g.Bx * g.Ymax * g.Zmax) : 0;
     case PH_BC1: return g.dimy ? gb((long long)g.By * g.Xmax * g.Zmax) : 0;
@@ -421,10 +458,11 @@ int rebuild(xfg_ensemble *e) {
         int *t = &tab[(size_t)ph * row_len(e)];
         if (ph == PH_FALL) {
             for (int q = 0; q < n; q++)
-                for (int d = 0; d < 3; d++) t[3 * q + d] = (int)acc, acc += face_blocks(ordered[q].g, d, ordered[q].ltx);
+                for (int d = 0; d < 3; d++)
+                    t[3 * q + d] = (int)acc, acc += ordered[q].fused ? 0 : face_blocks(ordered[q].g, d, ordered[q].ltx);
             t[3 * n] = (int)acc;
         } else {
-            for (int q = 0; q < n; q++) t[q] = (int)acc, acc += blocks_of(ordered[q].g, ph, ordered[q].ltx);
+            for (int q = 0; q < n; q++) t[q] = (int)acc, acc += blocks_of(ordered[q], ph, ordered[q].ltx);
             t[n] = (int)acc;
         }
         if (acc > 0x7fffffffLL) return efail(-1, "ensemble too large for one launch per phase%s");
@@ -451,6 +489,15 @@ void launch_step(xfg_ensemble *e) {
         if (e->nblk[PH_BC0]) kb_bc<0><<<e->nblk[PH_BC0], kThreads, 0, st>>>(e->dm, tab(e, PH_BC0), n, flag);
         if (e->nblk[PH_BC1]) kb_bc<1><<<e->nblk[PH_BC1], kThreads, 0, st>>>(e->dm, tab(e, PH_BC1), n, flag);
         if (e->nblk[PH_BC2]) kb_bc<2><<<e->nblk[PH_BC2], kThreads, 0, st>>>(e->dm, tab(e, PH_BC2), n, flag);
+        if (e->nblk[PH_FUSED]) {  // fused members: one launch for the whole stage
+            if (flag == 3 && e->nblk[PH_GLAM])
+                kb_fused_ghost<<<e->nblk[PH_GLAM], kThreads, 0, st>>>(e->dm, tab(e, PH_GLAM), n, e->fk.gamma);
+            if (e->sc.artificial_type == XFG_LLF)
+                kb_fused<true><<<e->nblk[PH_FUSED], fz::THREADS, sizeof(FusedTile), st>>>(e->dm, tab(e, PH_FUSED), n, e->fk, flag);
+            else
+                kb_fused<false><<<e->nblk[PH_FUSED], fz::THREADS, sizeof(FusedTile), st>>>(e->dm, tab(e, PH_FUSED), n, e->fk, flag);
+        }
+        if (!e->nblk[PH_STATES]) continue;  // no member left on the separate stage kernels
         if (mixed) kb_states<true><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
         else kb_states<false><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
         const int art = e->sc.artificial_type;
@@ -543,6 +590,22 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
     }
     e->pool_bytes = pool_bytes;
     e->alloc.init(pool_bytes);
+    e->fused_ok = scheme->precision == XFG_MIXED && scheme->scheme_order == 5 && !scheme->positivity &&
+                  (scheme->artificial_type == XFG_LLF || scheme->artificial_type == XFG_ROE);
+    if (e->fused_ok) {
+        const double gm1 = scheme->ncop_gamma - 1.0;
+        e->fk.gamma = (float)scheme->ncop_gamma;
+        e->fk.gm1h = (float)gm1;
+        e->fk.gm1l = (float)(gm1 - (double)e->fk.gm1h);
+        e->fk.igm1 = (float)(1.0 / gm1);
+        err = cudaFuncSetAttribute(kb_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedTile));
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(kb_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedTile));
+        if (err != cudaSuccess) {
+            xfg_ensemble_destroy(e);
+            return efail(-2, "fused stage set-up failed: %s", cudaGetErrorString(err));
+        }
+    }
     *out = e;
     return 0;
 }
@@ -584,6 +647,7 @@ int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_ao
     m.f.dtbuf = e->ddt + 8 * s;
     m.f.err = e->derr + 8 * s;
     m.active = 1;
+    m.fused = e->fused_ok && two_d(*block) ? 1 : 0;
     e->m_off[s] = off, e->m_len[s] = need, e->blocks[s] = *block;
     const long long N = m.g.ncell(), P = m.g.pitch;
     ECK(cudaMemsetAsync(e->pool + off, 0, need, e->st));
@@ -591,6 +655,8 @@ int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_ao
     ECK(cudaMemcpyAsync(stage, U_aos, sizeof(double) * 5 * N, cudaMemcpyDefault, e->st));
     kb_aos_to_soa<<<(unsigned)((5 * N + 255) / 256), 256, 0, e->st>>>(stage, m.f.U, 5, N, P);
     ECK(cudaMemcpyAsync(m.f.U1, m.f.U, sizeof(double) * 5 * P, cudaMemcpyDeviceToDevice, e->st));
+    if (m.fused)  // the first stage's output buffer starts as U1 does (ghost cells of no-op sides)
+        ECK(cudaMemcpyAsync(m.f.U2, m.f.U, sizeof(double) * 5 * P, cudaMemcpyDeviceToDevice, e->st));
     double dtb[8] = {0.0, 0.0, target_t, 0.0, 0.0, 0.0, 0.0, 0.0};
     ECK(cudaMemcpyAsync(m.f.dtbuf, dtb, sizeof dtb, cudaMemcpyHostToDevice, e->st));
     ECK(cudaMemsetAsync(m.f.err, 0, 8 * sizeof(int), e->st));

@@ -292,16 +292,17 @@ __device__ __forceinline__ void fused_face(const FusedTile &s, int rcL, int fL, 
 // Uout = UI + dt LU; 2: Uout = 3/4 Uprev + 1/4 UI + 1/4 dt LU; 3: Uout = (Uprev + 2 UI + 2 dt LU)/3.
 // store_lu keeps LU; want_lam adds the GetDt maxima of the inner cells (GlobalDt_block.hpp:31-66)
 // and writes their FP32 primitives (the last UpdateFluidStates a caller can read).
+// The tile (bx, by) of the block, run by one CTA of fz::THREADS threads with a FusedTile of
+// dynamic shared memory; dt the stage's time step (used when do_rk).
 template <bool LLF>
-__global__ void __launch_bounds__(fz::THREADS, 2)
-    k_fused_stage(Geo g, DevFields f, FusedK k, const double *__restrict__ UI, const double *__restrict__ Uprev,
-                  double *__restrict__ Uout, int flag, double dt_arg, const double *__restrict__ dt_dev, int do_rk,
-                  int store_lu, int want_lam, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void fused_stage_tile(const Geo &g, const DevFields &f, const FusedK &k,
+                                                 const double *__restrict__ UI, const double *__restrict__ Uprev,
+                                                 double *__restrict__ Uout, int flag, double dt, int do_rk, int store_lu,
+                                                 int want_lam, int bx, int by) {
     extern __shared__ float4 fz_smem[];
     FusedTile &s = *reinterpret_cast<FusedTile *>(fz_smem);
     __shared__ float red[2][fz::THREADS / 32];
-    const int x0 = blockIdx.x * fz::TX, y0 = blockIdx.y * fz::TY;
+    const int x0 = bx * fz::TX, y0 = by * fz::TY;
     const long long P = g.pitch;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -442,7 +443,6 @@ __global__ void __launch_bounds__(fz::THREADS, 2)
         if (x0 + c < g.Xi && y0 + r < g.Yi) {
             const int i = g.Bx + x0 + c, j = g.By + y0 + r;
             const long long id = (long long)j * g.Xmax + i;
-            const double dt = dt_dev ? dt_dev[0] : dt_arg;
             const int dx_ = r * (fz::TX + 1) + c, dy_ = r * fz::TX + c;
             const float2 IH = make_float2(g.idh[0], g.idh[1]), IL = make_float2(g.idl[0], g.idl[1]);
             int code = 0;
@@ -483,12 +483,23 @@ __global__ void __launch_bounds__(fz::THREADS, 2)
     }
 }
 
-// GetDt maxima and FP32 primitives of the ghost cells of a 2D block (the stage-3 fused kernel
-// covers the inner cells): one thread per ghost cell, the FP32 recovery of k_states_mixed.
-static __global__ void __launch_bounds__(kThreads) k_fused_ghost_lam(Geo g, DevFields f, float gamma,
-                                                                     const double *__restrict__ UI, int guard) {
+template <bool LLF>
+__global__ void __launch_bounds__(fz::THREADS, 2)
+    k_fused_stage(Geo g, DevFields f, FusedK k, const double *__restrict__ UI, const double *__restrict__ Uprev,
+                  double *__restrict__ Uout, int flag, double dt_arg, const double *__restrict__ dt_dev, int do_rk,
+                  int store_lu, int want_lam, int guard) {
     if (guard && step_done(f)) return;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    fused_stage_tile<LLF>(g, f, k, UI, Uprev, Uout, flag, dt_dev ? dt_dev[0] : dt_arg, do_rk, store_lu, want_lam,
+                          blockIdx.x, blockIdx.y);
+}
+
+// Ghost cells of a 2D block: 2 By rows of Xmax cells and 2 Bx columns of the Yi inner rows.
+__host__ __device__ inline long long fused_ghost_cells(const Geo &g) { return 2LL * g.By * g.Xmax + 2LL * g.Bx * g.Yi; }
+
+// GetDt maxima and FP32 primitives of ghost cell t of a 2D block (the stage-3 fused kernel covers
+// the inner cells), the FP32 recovery of k_states_mixed; every thread of the block calls it.
+__device__ __forceinline__ void fused_ghost_lam_body(const Geo &g, const DevFields &f, float gamma,
+                                                     const double *__restrict__ UI, long long t) {
     const long long rows = (long long)g.By * g.Xmax, sides = 2LL * g.Bx * g.Yi;
     float lamx = 0.f, lamy = 0.f;
     if (t < 2 * rows + sides) {
@@ -516,6 +527,11 @@ static __global__ void __launch_bounds__(kThreads) k_fused_ghost_lam(Geo g, DevF
         if (!(lamy >= 0.f)) lamy = __int_as_float(0x7f800000);
     }
     lam_block_reduce_f(g, f, lamx, lamy, 0.f);
+}
+static __global__ void __launch_bounds__(kThreads) k_fused_ghost_lam(Geo g, DevFields f, float gamma,
+                                                                     const double *__restrict__ UI, int guard) {
+    if (guard && step_done(f)) return;
+    fused_ghost_lam_body(g, f, gamma, UI, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 }  // namespace XFG_KNS

@@ -172,7 +172,7 @@ struct Inst {
     static void fused_ghost_lam(const LaunchCtx &c, const double *UI, int guard) {
         if constexpr (MIXED && !COP) {
             const Geo &g = c.g;
-            const long long n = 2LL * g.By * g.Xmax + 2LL * g.Bx * g.Yi;
+            const long long n = fused_ghost_cells(g);
             k_fused_ghost_lam<<<grid_for(n, kThreads), kThreads, 0, c.st>>>(g, c.f, (float)c.th.ncop_gamma, UI, guard);
         }
     }

@@ -6,8 +6,14 @@
 // keep their layouts and are allocated through the reference's queue as before, so output,
 // checkpoint and restart code keep working; the CUDA handle holds the state in its own SoA layout:
 //   - InitialU runs the sample's initial condition into d_U, then loads d_U (and T) into the handle;
-//   - UpdateFluidStates mirrors the primitives back into d_fstate (Output reads them);
-//   - UpdateFluidURK3 with flag 3 (end of a step) mirrors U back into d_U (CopyToUbak reads it).
+//   - the primitives are mirrored into d_fstate only where XFLUIDS can read them: Output reads them
+//     at the top of an iteration (those of the step's third UpdateStates, or of main.cpp's initial
+//     one) and after a reported error (those of the failing stage). UpdateFluidStates therefore
+//     mirrors on the initial call, on the third stage of a step and when it reports an error, and
+//     EstimateFluidNAN mirrors before it reports one; the first two stages' primitives stay in the
+//     handle (XFLUIDS::RungeKuttaSP3rd reads none of them, src/XFLUIDS.cpp:441-525);
+//   - UpdateFluidURK3 with flag 3 (end of a step) mirrors U back into d_U (CopyToUbak reads it at
+//     the top of every iteration, src/XFLUIDS.cpp:174).
 // Chemistry (ODESolver), viscosity and the SBI diagnostics are outside the ported path.
 #include <cstdio>
 #include <cstring>
@@ -19,6 +25,9 @@
 
 namespace {
 std::unordered_map<const Fluid *, xfg_handle *> g_handles;
+// RK stage the next UpdateFluidStates belongs to (1..3), from the last UpdateFluidURK3 flag;
+// 0 before the first step (main.cpp's initial UpdateStates)
+std::unordered_map<const Fluid *, int> g_next_stage;
 
 xfg_handle *H(const Fluid *f) { return g_handles.at(f); }
 
@@ -108,6 +117,7 @@ Fluid::Fluid(Setup &setup) : Fs(setup), q(setup.q), rank(0), nranks(1), SBIOutIt
 Fluid::~Fluid() {
     auto it = g_handles.find(this);
     if (it != g_handles.end()) xfg_destroy(it->second), g_handles.erase(it);
+    g_next_stage.erase(this);
     for (real_t *p : {d_U, d_U1, d_LU, Ubak, d_FluxF, d_FluxG, d_FluxH, d_wallFluxF, d_wallFluxG, d_wallFluxH})
         if (p) sycl::free(p, q);
 }
@@ -161,24 +171,30 @@ void Fluid::InitialU(sycl::queue &q) {
                           d_FluxG, d_FluxH, d_wallFluxF, d_wallFluxG, d_wallFluxH);
     q.wait();
     check(xfg_set_state(H(this), d_U, d_fstate.T), "xfg_set_state");
+    g_next_stage[this] = 0;
 }
 
 void Fluid::BoundaryCondition(sycl::queue &q, BConditions BCs[6], int flag) {
     check(xfg_boundary(H(this), flag), "xfg_boundary");
 }
 
+// The primitives of the handle's last UpdateFluidStates into the reference-visible d_fstate arrays
+// that XFLUIDS::Output / CopyDataFromDevice read (src/XFLUIDS.cpp:726-760).
+static void mirror_primitives(xfg_handle *h, FlowData &d) {
+    const int ids[] = {XFG_RHO, XFG_P, XFG_U_VEL, XFG_V_VEL, XFG_W_VEL, XFG_C, XFG_H, XFG_T, XFG_GAMMA, XFG_E};
+    real_t *dst[] = {d.rho, d.p, d.u, d.v, d.w, d.c, d.H, d.T, d.gamma, d.e};
+    for (int n = 0; n < 10; n++) check(xfg_get_array(h, ids[n], dst[n]), "xfg_get_array");
+#ifdef COP
+    check(xfg_get_array(h, XFG_Y, d.y), "xfg_get_array");
+#endif
+}
+
 std::pair<bool, std::vector<float>> Fluid::UpdateFluidStates(sycl::queue &q, int flag) {
     int err = 0;
     std::vector<float> timers(4, 0.f);
     check(xfg_update_states(H(this), flag, &err, timers.data()), "xfg_update_states");
-    // primitives back into the reference-visible arrays read by XFLUIDS::Output
-    const int ids[] = {XFG_RHO, XFG_P, XFG_U_VEL, XFG_V_VEL, XFG_W_VEL, XFG_C, XFG_H, XFG_T, XFG_GAMMA, XFG_E};
-    real_t *dst[] = {d_fstate.rho, d_fstate.p, d_fstate.u, d_fstate.v, d_fstate.w, d_fstate.c, d_fstate.H,
-                     d_fstate.T, d_fstate.gamma, d_fstate.e};
-    for (int n = 0; n < 10; n++) check(xfg_get_array(H(this), ids[n], dst[n]), "xfg_get_array");
-#ifdef COP
-    check(xfg_get_array(H(this), XFG_Y, d_fstate.y), "xfg_get_array");
-#endif
+    const int stage = g_next_stage[this];
+    if (err || stage == 0 || stage == 3) mirror_primitives(H(this), d_fstate);
     return std::make_pair(err != 0, timers);
 }
 
@@ -190,6 +206,7 @@ std::vector<float> Fluid::ComputeFluidLU(sycl::queue &q, int flag) {
 
 void Fluid::UpdateFluidURK3(sycl::queue &q, int flag, real_t const dt) {
     check(xfg_update_rk3(H(this), flag, dt), "xfg_update_rk3");
+    g_next_stage[this] = flag % 3 + 1;
     if (flag == 3) check(xfg_get_array(H(this), XFG_U, d_U), "xfg_get_array");  // CopyToUbak / Output read d_U
 }
 
@@ -204,6 +221,7 @@ bool Fluid::EstimateFluidNAN(sycl::queue &q, int flag) {
     int rc = xfg_estimate_nan(H(this), flag, &err, pos);
     check(rc < 0 ? rc : 0, "xfg_estimate_nan");
     if (!err) return false;
+    mirror_primitives(H(this), d_fstate);  // the error output reads this stage's primitives
     std::cout << "\nErrors of LU[";
     for (int n = 0; n < Emax - 1; n++) std::cout << pos[n] << ", ";
     std::cout << pos[Emax - 1] << "] located at (i, j, k)= (" << pos[Emax + 1] << ", " << pos[Emax + 2] << ", "

@@ -79,6 +79,26 @@ def _rel_l1(a, r):
     return [float(x) for x in d / scale]
 
 
+COMPONENTS = ["rho", "rho_u", "rho_v", "rho_w", "E"]
+
+
+def per_component(a, r, names=COMPONENTS):
+    """Difference of two inner-cell states per conserved component: L1 (mean |a - r|) and Linf
+    (max |a - r|), each also relative to the component's own scale (mean |r| for L1, max |r| for
+    Linf); components that are zero in r report their absolute values only. 'worst' names the
+    component with the largest relative L1."""
+    d = np.abs(np.asarray(a) - np.asarray(r))
+    out = {}
+    for q, nm in enumerate(names):
+        mean, mx = float(np.abs(r[:, q]).mean()), float(np.abs(r[:, q]).max())
+        l1, li = float(d[:, q].mean()), float(d[:, q].max())
+        out[nm] = {"l1": l1, "linf": li, "l1_rel": l1 / mean if mean > 0 else None,
+                   "linf_rel": li / mx if mx > 0 else None}
+    rel = {k: v["l1_rel"] for k, v in out.items() if v["l1_rel"] is not None}
+    out["worst"] = max(rel, key=rel.get) if rel else None
+    return out
+
+
 def vortex_horizon(n, periods=10, precisions=(0, MIXED), device=0, chunk=4096):
     """The 2D vortex n^2 advanced to t = 10 * periods (whole periods: the exact solution is the
     initial state) in each precision; per precision the steps, the device time, the L1 and Linf
@@ -119,7 +139,8 @@ def vortex_horizon(n, periods=10, precisions=(0, MIXED), device=0, chunk=4096):
         out["mixed_vs_fp64"] = {
             "l1_rel": _rel_l1(a, r),
             "linf_normwise": float(max(np.abs(a[:, q] - r[:, q]).max() / np.abs(r[:, q]).max()
-                                       for q in range(5) if np.abs(r[:, q]).max() > 0))}
+                                       for q in range(5) if np.abs(r[:, q]).max() > 0)),
+            "per_component": per_component(a, r)}
     return out
 
 
