@@ -239,7 +239,7 @@ int xfg_checkpoint_write(xfg_handle *h, const char *path, int step, double time,
 int xfg_checkpoint_read(xfg_handle *h, const char *path, int *step, double *time, float *duration);
 
 /* ------------------------------------------------------------------------------------------
- * Ensemble of independent single-gas grids (batched ensemble, request serving).
+ * Ensemble of independent grids (batched ensemble, request serving).
  * No single counterpart in the reference, which advances one block per process: the members are
  * XFLUIDS runs of the same scheme (each member's step is XFLUIDS::Evolution's loop body with its
  * own dt and target time, src/XFLUIDS.cpp:172-214), advanced together by batched kernels.
@@ -247,20 +247,30 @@ int xfg_checkpoint_read(xfg_handle *h, const char *path, int *step, double *time
 typedef struct xfg_ensemble xfg_ensemble;
 
 /* Create an ensemble with `capacity` member slots and a device pool of pool_bytes from which the
- * members are sub-allocated (admission by HBM budget). scheme: single gas (cop = 0), inviscid,
- * ROE, LLF or GLF (running maxima per member), WENO5 / WENO-CU6 / WENO7, positivity limiter on or
- * off, precision XFG_FP64 or XFG_MIXED. */
+ * members are sub-allocated (admission by HBM budget). scheme: single gas (cop = 0) or a mixture of
+ * 5 species (cop = 1, num_species = 5, thermal holding its tables; GhostSpecies and NASA-9 / JANAF
+ * as the single-grid path), inviscid, ROE, LLF or GLF (running maxima per member), WENO5 /
+ * WENO-CU6 / WENO7, positivity limiter on or off, precision XFG_FP64 or XFG_MIXED. The batched
+ * kernels of each gas model and form are compiled with the contraction flags of the single-grid
+ * kernels, so a member advances as the same block alone in a handle would. */
 int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *scheme, const xfg_thermal *thermal,
                         int device, xfg_ensemble **out);
 int xfg_ensemble_destroy(xfg_ensemble *e);
 
-/* Device bytes one member of this block takes from the pool. */
+/* Device bytes one single-gas member of this block takes from the pool; _for: a member of this
+ * block under the given scheme (single gas or mixture). */
 size_t xfg_ensemble_member_bytes(const xfg_block *block, int precision);
+size_t xfg_ensemble_member_bytes_for(const xfg_block *block, const xfg_scheme *scheme);
 
 /* Admit a member: state U (AoS, host or device), target time; runs BoundaryCondition(U) and
  * UpdateStates(U) for it (main.cpp:45-47). Returns 0 and *slot, 1 when no slot is free, 2 when the
  * pool has no room (the caller retries after members leave). */
 int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_aos, double target_t, int *slot);
+/* xfg_ensemble_add with the member's temperature (Xmax*Ymax*Zmax doubles, host or device), the warm
+ * start of its temperature Newton iteration; required for a mixture, may be NULL for a single gas.
+ * A mixture member cannot come from xfg_ensemble_add_checkpoint (the file holds no temperature). */
+int xfg_ensemble_add_t(xfg_ensemble *e, const xfg_block *block, const double *U_aos, const double *T,
+                       double target_t, int *slot);
 
 /* Release a member's slot and pool memory. */
 int xfg_ensemble_remove(xfg_ensemble *e, int slot);

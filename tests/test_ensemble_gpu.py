@@ -250,3 +250,50 @@ def test_member_with_numerical_error_stops_and_others_go_on(cuda_lib):
         assert st != 0
     finally:
         f.close()
+
+
+def _mixture_members(order):
+    """5-species JANAF mixtures of uneven sizes: three temporal mixing layers (3D) and a 2D block
+    with walls and a periodic pair (the ragged mixture case of the random tests)."""
+    from helpers import mixing_small
+    from test_fuzz_gpu import _tiny_case
+    out = []
+    for shape in ((16, 12, 8), (24, 16, 8), (12, 20, 6)):
+        b, s, th, U, T = mixing_small(shape, order=order)
+        out.append((b, U, T))
+    b, s, th, U, T = _tiny_case((5, 9, 0), (0.01, 0.013, 1.0), [4, 1, 3, 3, 0, 0], order, cop=True)
+    out.append((b, U, T))
+    return s, th, out
+
+
+@pytest.mark.parametrize("order,prec", [(7, FP64), (7, MIXED), (5, FP64), (5, MIXED)],
+                         ids=["w7-fp64", "w7-mixed", "w5-fp64", "w5-mixed"])
+def test_mixture_members_equal_single_grid_runs(cuda_lib, order, prec):
+    """Mixture members (the temperature Newton iteration, the per-cell sound-speed terms, the
+    mixture Roe state) advanced in one ensemble equal the same blocks advanced alone."""
+    s, th, ms = _mixture_members(order)
+    s.precision = prec
+    E = s.Emax
+    nsteps = 4
+    pool = sum(Ensemble.member_bytes(b, prec, scheme=s) for b, _, _ in ms) + 4096 * len(ms)
+    e = Ensemble(s, capacity=len(ms), pool_bytes=pool, thermal=th)
+    try:
+        slots = [e.add(b, U, 1e300, T=T) for b, U, T in ms]
+        assert None not in slots
+        st, _ = e.advance(nsteps)
+        assert st == 0
+        for (b, U, T), slot in zip(ms, slots):
+            f = Fluid(b, s, th)
+            f.InitialU(U, T)
+            f.initialize()
+            st1, t_ref, n_ref = f.advance(nsteps)
+            ref = f.get("U").reshape(-1)
+            f.close()
+            info = e.status(slot)
+            assert st1 == 0 and info["error"] == 0 and info["steps"] == n_ref
+            assert info["t"] == pytest.approx(t_ref, rel=1e-13 if prec == FP64 else MIXED_T_TOL, abs=0)
+            err = normwise(e.get_state(slot), ref, E).max()
+            print(f"member {slot} {b.X_inner}x{b.Y_inner}x{b.Z_inner}: normwise {err:.3e}")
+            assert err <= (PARITY_TOL if prec == FP64 else MIXED_TOL), (slot, err)
+    finally:
+        e.close()

@@ -156,6 +156,7 @@ def lib():
         "xfg_ensemble_create": [I, C.c_size_t, C.POINTER(Scheme), C.POINTER(Thermal), I, C.POINTER(P)],
         "xfg_ensemble_destroy": [P],
         "xfg_ensemble_add": [P, C.POINTER(Block), P, D, pi],
+        "xfg_ensemble_add_t": [P, C.POINTER(Block), P, P, D, pi],
         "xfg_ensemble_remove": [P, I],
         "xfg_ensemble_advance": [P, I, I, C.POINTER(C.c_float)],
         "xfg_ensemble_status": [P, I, pd, pi, pi],
@@ -175,6 +176,8 @@ def lib():
         fn.restype = C.c_int
     L.xfg_ensemble_member_bytes.argtypes = [C.POINTER(Block), I]
     L.xfg_ensemble_member_bytes.restype = C.c_size_t
+    L.xfg_ensemble_member_bytes_for.argtypes = [C.POINTER(Block), C.POINTER(Scheme)]
+    L.xfg_ensemble_member_bytes_for.restype = C.c_size_t
     L.xfg_ensemble_free_bytes.argtypes = [P]
     L.xfg_ensemble_free_bytes.restype = C.c_size_t
     _lib = L

@@ -20,6 +20,7 @@ UNITS = [("xfg_api.cu", []), ("xfg_noalloc.cu", []), ("xfg_inst_ncop.cu", []), (
 UNITS += [(f"xfg_inst_cop{n}.cu", NOFMA) for n in (2, 3, 4, 5, 6)]
 UNITS += [(f"xfg_inst_cop{n}_mixed.cu", []) for n in (2, 3, 4, 5, 6)]
 UNITS += [(f"xfg_inst_cop{n}_faces.cu", []) for n in (2, 3, 4, 5, 6)]
+UNITS += [("xfg_ensemble_cop5.cu", NOFMA), ("xfg_ensemble_cop5_fma.cu", [])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

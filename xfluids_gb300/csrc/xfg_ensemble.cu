@@ -21,58 +21,57 @@
 
 #include "../../include/xfluids_gb300.h"
 #define XFG_KNS ens
-#include "xfg_fused.cuh"
-#include "xfg_kernels.cuh"
-#include "xfg_mixed.cuh"
-#include "xfg_ops.h"
+#include "xfg_ensemble.cuh"
 
 using namespace xfg;
 using namespace xfg::ens;
 
+namespace xfg {
+// ensemble launcher registry (xfg_ensemble.cuh)
+static std::vector<EnsOps> &ens_registry() {
+    static std::vector<EnsOps> r;
+    return r;
+}
+void register_ens_ops(const EnsOps *ops) {
+    for (EnsOps &o : ens_registry())
+        if (o.cop == ops->cop && o.ns == ops->ns && o.precision == ops->precision) {
+            auto faces = o.faces;
+            auto faces_all = o.faces_all;
+            const bool overridden = o.bc == nullptr;  // a face override registered first
+            o = *ops;
+            if (overridden) o.faces = faces, o.faces_all = faces_all;
+            return;
+        }
+    ens_registry().push_back(*ops);
+}
+void register_ens_faces(int cop, int ns, int precision, decltype(EnsOps::faces) faces,
+                        decltype(EnsOps::faces_all) faces_all) {
+    for (EnsOps &o : ens_registry())
+        if (o.cop == cop && o.ns == ns && o.precision == precision) {
+            o.faces = faces, o.faces_all = faces_all;
+            return;
+        }
+    EnsOps o{};
+    o.cop = cop, o.ns = ns, o.precision = precision, o.faces = faces, o.faces_all = faces_all;
+    ens_registry().push_back(o);
+}
+const EnsOps *find_ens_ops(int cop, int ns, int precision) {
+    for (const EnsOps &o : ens_registry())
+        if (o.cop == cop && o.ns == ns && o.precision == precision && o.bc) return &o;
+    return nullptr;
+}
+}  // namespace xfg
+
+// the single-gas tables (mixtures: xfg_ensemble_cop<N>*.cu)
+static EnsRegistrar<false, 1, false> reg_fp64(XFG_FP64);
+static EnsRegistrar<false, 1, true> reg_mixed(XFG_MIXED);
+
 namespace {
 
-// Device descriptor of one member.
-struct Member {
-    Geo g;
-    DevFields f;
-    double cfl;
-    int bc[6];
-    int active;
-    int ltx;  // face tile of this member: 2^ltx faces along x by kThreads >> ltx across
-    int fused;  // 2D member of a mixed WENO5 LLF / Roe ensemble: its stages run as fused tiles
-    unsigned long long *glf;  // GLF running maxima (9 words in the member's small-word area)
-};
-
-// phases with a block table; PH_FALL holds three entries per member (x, y, z face sweeps of the
-// fused face launch), the others one. PH_FUSED: the 32 x 7 tiles of the fused mixed stage
-// (xfg_fused.cuh) of the fused members, PH_GLAM: their ghost cells' dt maxima.
-enum { PH_BC0, PH_BC1, PH_BC2, PH_STATES, PH_F0, PH_F1, PH_F2, PH_DIV, PH_FALL, PH_FUSED, PH_GLAM, PH_N };
+using Member = EnsMember;
 
 // size classes with their own face tile: 1D, 2D below 384 cells per side, 2D from 384, 3D
 enum { CL_1D, CL_2D_SMALL, CL_2D_LARGE, CL_3D, CL_N };
-
-__device__ __forceinline__ int member_of_block(const int *__restrict__ off, int n, int b) {
-    int lo = 0, hi = n;  // off[0] = 0 <= b < off[n]
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (__ldg(off + mid) <= b) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
-__device__ __forceinline__ bool member_done(const Member &m) { return m.f.dtbuf[4] != 0.0; }
-
-template <int D>
-__global__ void __launch_bounds__(kThreads) kb_bc(const Member *__restrict__ M, const int *__restrict__ off, int n, int flag) {
-    const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
-    // a fused member's second stage reads U2, the first stage's output
-    double *UI = flag == 1 || flag == 0 ? m.f.U : (flag == 2 && m.fused ? m.f.U2 : m.f.U1);
-    bc_body<D, 5>(m.g, UI, m.bc[2 * D], m.bc[2 * D + 1], t);
-}
 
 // One stage of the fused members: CTA = one 32 x 7 tile of one member (fused_stage_tile), stage
 // buffers U -> U2 -> U1 -> U as in the single-grid fused step.
@@ -93,154 +92,6 @@ __global__ void __launch_bounds__(kThreads) kb_fused_ghost(const Member *__restr
     const Member &m = M[mi];
     if (member_done(m)) return;
     fused_ghost_lam_body(m.g, m.f, gamma, m.f.U1, (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x);
-}
-
-template <bool MIXED>
-__global__ void __launch_bounds__(kThreads) kb_states(const Member *__restrict__ M, const int *__restrict__ off, int n,
-                                                      DevThermo th, int flag, int want_lam) {
-    const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    const long long id = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
-    double *UI = flag == 1 || flag == 0 ? m.f.U : m.f.U1;
-    if (MIXED) {
-        float lx = 0.f, ly = 0.f, lz = 0.f;
-        states_mixed_body<false, 1>(m.g, m.f, th, UI, 0, want_lam, id, lx, ly, lz);
-        if (want_lam) lam_block_reduce_f(m.g, m.f, lx, ly, lz);
-    } else {
-        double lx = 0.0, ly = 0.0, lz = 0.0;
-        states_body<false, 1>(m.g, m.f, th, UI, 0, want_lam, id, lx, ly, lz);
-        if (want_lam) lam_block_reduce(m.g, m.f, lx, ly, lz);
-    }
-}
-
-template <int D, int ORDER, bool MIXED>
-__device__ __forceinline__ void member_face(const Member &m, int lb, const DevThermo &th, int flag, int artificial) {
-    const dim3 gd = face_grid_tile<D>(m.g, m.ltx);
-    const int bx = lb % gd.x, by = (lb / gd.x) % gd.y, bz = lb / (gd.x * gd.y);
-    int i, j, k;
-    if (!face_of_tile<D>(m.g, bx, by, bz, m.ltx, i, j, k)) return;
-    const double *glf = artificial == XFG_GLF ? (const double *)m.glf + 3 * D : nullptr;
-    if (MIXED)
-        faces_mixed_body<D, false, 1, ORDER>(m.g, m.f, th, artificial, glf, i, j, k);
-    else
-        faces_body<D, false, 1, ORDER>(m.g, m.f, th, flag == 1 || flag == 0 ? m.f.U : m.f.U1, artificial, glf, i, j, k);
-}
-
-// one face sweep (direction D) of every member
-template <int D, int ORDER, bool MIXED>
-__global__ void __launch_bounds__(kThreads) kb_faces(const Member *__restrict__ M, const int *__restrict__ off, int n,
-                                                     DevThermo th, int flag, int artificial) {
-    const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    member_face<D, ORDER, MIXED>(m, blockIdx.x - off[mi], th, flag, artificial);
-}
-
-// all face sweeps of every member in one launch (entries 3 q + D of the table)
-template <int ORDER, bool MIXED>
-__global__ void __launch_bounds__(kThreads) kb_faces_all(const Member *__restrict__ M, const int *__restrict__ off,
-                                                         int n3, DevThermo th, int flag, int artificial) {
-    const int e = member_of_block(off, n3, blockIdx.x);
-    const Member &m = M[e / 3];
-    if (member_done(m)) return;
-    const int lb = blockIdx.x - off[e];
-    switch (e % 3) {
-    case 0: member_face<0, ORDER, MIXED>(m, lb, th, flag, artificial); break;
-    case 1: member_face<1, ORDER, MIXED>(m, lb, th, flag, artificial); break;
-    default: member_face<2, ORDER, MIXED>(m, lb, th, flag, artificial); break;
-    }
-}
-
-// The mixed WENO5 face sweeps with registers fitted to XFG_FACES_MIXED_MINB resident blocks per
-// SM, as k_faces_mixed_w5 of the single-grid path (the other forms stay unbounded).
-template <int D>
-__global__ void __launch_bounds__(kThreads, XFG_FACES_MIXED_MINB)
-    kb_faces_m5(const Member *__restrict__ M, const int *__restrict__ off, int n, DevThermo th, int flag, int artificial) {
-    const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    member_face<D, 5, true>(m, blockIdx.x - off[mi], th, flag, artificial);
-}
-__global__ void __launch_bounds__(kThreads, XFG_FACES_MIXED_MINB)
-    kb_faces_all_m5(const Member *__restrict__ M, const int *__restrict__ off, int n3, DevThermo th, int flag,
-                    int artificial) {
-    const int e = member_of_block(off, n3, blockIdx.x);
-    const Member &m = M[e / 3];
-    if (member_done(m)) return;
-    const int lb = blockIdx.x - off[e];
-    switch (e % 3) {
-    case 0: member_face<0, 5, true>(m, lb, th, flag, artificial); break;
-    case 1: member_face<1, 5, true>(m, lb, th, flag, artificial); break;
-    default: member_face<2, 5, true>(m, lb, th, flag, artificial); break;
-    }
-}
-
-template <bool MIXED>
-__global__ void __launch_bounds__(kThreads) kb_div_rk(const Member *__restrict__ M, const int *__restrict__ off, int n, int flag) {
-    const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
-    if (MIXED)
-        div_rk_mixed_body<5>(m.g, m.f, flag, m.f.dtbuf[0], 1, 0, t);
-    else
-        div_rk_body<5>(m.g, m.f, flag, m.f.dtbuf[0], 1, 0, t);
-}
-
-// positivity-preserving flux limiter (PositivityPreserving_kernels.hpp:5-76) on the face fluxes of
-// every active direction of every member, with the member's wave-speed maxima of this step
-// (written by kb_dt into dtbuf[5..7]); one thread per inner cell, as the divergence phase
-template <bool MIXED>
-__global__ void __launch_bounds__(kThreads) kb_pp(const Member *__restrict__ M, const int *__restrict__ off, int n, int flag) {
-    const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
-    const double *UI = flag == 1 || flag == 0 ? m.f.U : m.f.U1;
-    const int dims[3] = {m.g.dimx, m.g.dimy, m.g.dimz};
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        if (!dims[d]) continue;
-        const double l0 = m.f.dtbuf[5 + d];
-        if (MIXED) {
-            if (d == 0) pp_body<0, 5, 0, float>(m.g, UI, m.f.Ff[0], m.f.Fwf[0], l0, m.cfl / l0, t);
-            else if (d == 1) pp_body<1, 5, 0, float>(m.g, UI, m.f.Ff[1], m.f.Fwf[1], l0, m.cfl / l0, t);
-            else pp_body<2, 5, 0, float>(m.g, UI, m.f.Ff[2], m.f.Fwf[2], l0, m.cfl / l0, t);
-        } else {
-            if (d == 0) pp_body<0, 5, 0, double>(m.g, UI, m.f.F[0], m.f.Fw[0], l0, m.cfl / l0, t);
-            else if (d == 1) pp_body<1, 5, 0, double>(m.g, UI, m.f.F[1], m.f.Fw[1], l0, m.cfl / l0, t);
-            else pp_body<2, 5, 0, double>(m.g, UI, m.f.F[2], m.f.Fw[2], l0, m.cfl / l0, t);
-        }
-    }
-}
-
-// GLF maxima (ConVenction_block.hpp:115-215) of every member, folded into its running maxima as
-// k_glf / k_glf_mixed do for a single grid: |u_d - c|, |u_d|, |u_d + c| over all cells
-template <bool MIXED>
-__global__ void __launch_bounds__(kThreads) kb_glf(const Member *__restrict__ M, const int *__restrict__ off, int n) {
-    const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    const long long id = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
-    const long long N = m.g.ncell(), P = m.g.pitch;
-    double mx[9];
-    for (int q = 0; q < 9; q++) mx[q] = 0.0;
-    if (id < N) {
-        const double c = MIXED ? (double)m.f.primf[6 * P + id] : m.f.c[id];
-        for (int d = 0; d < 3; d++) {
-            const double v = MIXED ? (double)m.f.primf[(1 + d) * P + id] : (d == 0 ? m.f.u[id] : (d == 1 ? m.f.v[id] : m.f.w[id]));
-            mx[3 * d + 0] = fabs(v - c);
-            mx[3 * d + 1] = fabs(v);
-            mx[3 * d + 2] = fabs(v + c);
-        }
-    }
-    // a block belongs to one member, so a warp's maxima are one member's
-    for (int q = 0; q < 9; q++) {
-        double x = mx[q];
-        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
-        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&m.glf[q], x);
-    }
 }
 
 __global__ void kb_dt(const Member *__restrict__ M, int n) {
@@ -350,6 +201,8 @@ struct xfg_ensemble {
     int ltx[CL_N] = {7, 5, 5, 5};         // face tile per size class
     bool fused_ok = false;                // mixed WENO5 LLF / Roe without limiter: 2D members fused
     FusedK fk{};
+    const EnsOps *ops = nullptr;          // batched launchers of the ensemble's gas model and form
+    int E = 5, NS = 1;
 };
 
 namespace {
@@ -358,39 +211,45 @@ size_t row_len(const xfg_ensemble *e) { return 3 * (size_t)e->capacity + 1; }
 
 bool two_d(const xfg_block &b) { return b.DimX && b.DimY && !b.DimZ; }
 
-size_t member_bytes(const xfg_block &b, bool mixed) {
+// Device bytes of one member: the single-grid arrays of its gas model (ns species, 1 for a single
+// gas) and form, as xfg_create lays them out, without the viscous and transpose arrays.
+size_t member_bytes(const xfg_block &b, int cop, int ns, bool mixed) {
     const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
-    const int dims = b.DimX + b.DimY + b.DimZ;
-    size_t nd = 3 * 5 + 12;                              // U, U1, LU, primitives
-    if (mixed && two_d(b)) nd += 5;                      // U2 of the fused stages
-    if (!mixed) nd += 2 * 5 * dims + 2 + 3 * dims;       // F, Fw, sqrt(rho), 1/sqrt(rho), |lambda|
+    const int dims = b.DimX + b.DimY + b.DimZ, E = cop ? ns + 4 : 5;
+    size_t nd = 3 * E + 12;                                    // U, U1, LU, primitives
+    if (cop) nd += ns + 3 + (ns - 1);                          // y, per-cell sound-speed terms
+    if (mixed && !cop && two_d(b)) nd += 5;                    // U2 of the fused stages
+    if (!mixed) nd += 2 * E * dims + (cop ? 0 : 2 + 3 * dims); // F, Fw; single gas: sqrt(rho), 1/sqrt(rho), |lambda|
     size_t bytes = nd * P * 8;
-    if (mixed) bytes += (size_t)(5 + 7 + 2 * 5 * dims) * up(P * 4, 256);
-    return bytes + 1024;                                 // lam + small words
+    if (mixed) bytes += (size_t)(E + 7 + 2 * E * dims) * up(P * 4, 256);
+    return bytes + 1024;                                       // lam + small words
 }
 
-void carve(Member &m, char *base, const xfg_block &b, bool mixed) {
+void carve(Member &m, char *base, const xfg_block &b, int cop, int ns, bool mixed) {
     const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
-    const int dims[3] = {b.DimX, b.DimY, b.DimZ};
+    const int dims[3] = {b.DimX, b.DimY, b.DimZ}, E = cop ? ns + 4 : 5;
     char *p = base;
     auto t8 = [&](int c) { double *r = (double *)p; p += (size_t)c * P * 8; return r; };
     auto t4 = [&](int c) { float *r = (float *)p; p += (size_t)c * up(P * 4, 256); return r; };
     DevFields &f = m.f;
     std::memset(&f, 0, sizeof f);
-    f.U = t8(5), f.U1 = t8(5), f.LU = t8(5);
-    if (mixed && two_d(b)) f.U2 = t8(5);
+    f.U = t8(E), f.U1 = t8(E), f.LU = t8(E);
+    if (mixed && !cop && two_d(b)) f.U2 = t8(5);
     f.rho = t8(1), f.u = t8(1), f.v = t8(1), f.w = t8(1), f.p = t8(1), f.H = t8(1);
     f.c = t8(1), f.T = t8(1), f.gamma = t8(1), f.e = t8(1), f.Cp = t8(1), f.R = t8(1);
+    if (cop) f.y = t8(ns), f.xc = t8(3 + (ns - 1));
     if (!mixed) {
         for (int d = 0; d < 3; d++)
-            if (dims[d]) f.F[d] = t8(5), f.Fw[d] = t8(5);
-        f.sr = t8(1), f.isr = t8(1);
-        for (int d = 0; d < 3; d++)
-            if (dims[d]) f.eab[d] = t8(3);
+            if (dims[d]) f.F[d] = t8(E), f.Fw[d] = t8(E);
+        if (!cop) {
+            f.sr = t8(1), f.isr = t8(1);
+            for (int d = 0; d < 3; d++)
+                if (dims[d]) f.eab[d] = t8(3);
+        }
     } else {
-        f.Uf = t4(5), f.primf = t4(7);
+        f.Uf = t4(E), f.primf = t4(7);
         for (int d = 0; d < 3; d++)
-            if (dims[d]) f.Ff[d] = t4(5), f.Fwf[d] = t4(5);
+            if (dims[d]) f.Ff[d] = t4(E), f.Fwf[d] = t4(E);
     }
     f.lam = (unsigned long long *)p;
     m.glf = (unsigned long long *)(p + 64);
@@ -400,6 +259,7 @@ void carve(Member &m, char *base, const xfg_block &b, bool mixed) {
     g._dx = b._dx, g._dy = b._dy, g._dz = b._dz, g.pitch = (long long)P;
     geo_split_spacing(g);
     g.dx = b.dx, g.dy = b.dy, g.dz = b.dz;
+    for (int q = 0; q < 6; q++) g.bc[q] = b.Boundarys[q];
     m.cfl = b.CFLnumber;
     for (int q = 0; q < 6; q++) m.bc[q] = b.Boundarys[q];
 }
@@ -481,70 +341,33 @@ const int *tab(const xfg_ensemble *e, int ph) { return e->doff + (size_t)ph * ro
 void launch_step(xfg_ensemble *e) {
     const int n = (int)e->order.size();
     if (!n) return;
-    const bool mixed = e->sc.precision == XFG_MIXED;
-    const int order = e->sc.scheme_order;
+    const EnsOps *ops = e->ops;
+    const int order = e->sc.scheme_order, art = e->sc.artificial_type;
     cudaStream_t st = e->st;
     kb_dt<<<(n + 127) / 128, 128, 0, st>>>(e->dm, n);
     for (int flag = 1; flag <= 3; flag++) {
-        if (e->nblk[PH_BC0]) kb_bc<0><<<e->nblk[PH_BC0], kThreads, 0, st>>>(e->dm, tab(e, PH_BC0), n, flag);
-        if (e->nblk[PH_BC1]) kb_bc<1><<<e->nblk[PH_BC1], kThreads, 0, st>>>(e->dm, tab(e, PH_BC1), n, flag);
-        if (e->nblk[PH_BC2]) kb_bc<2><<<e->nblk[PH_BC2], kThreads, 0, st>>>(e->dm, tab(e, PH_BC2), n, flag);
+        for (int d = 0; d < 3; d++)
+            if (e->nblk[PH_BC0 + d]) ops->bc(e->dm, tab(e, PH_BC0 + d), e->nblk[PH_BC0 + d], n, d, flag, st);
         if (e->nblk[PH_FUSED]) {  // fused members: one launch for the whole stage
             if (flag == 3 && e->nblk[PH_GLAM])
                 kb_fused_ghost<<<e->nblk[PH_GLAM], kThreads, 0, st>>>(e->dm, tab(e, PH_GLAM), n, e->fk.gamma);
-            if (e->sc.artificial_type == XFG_LLF)
+            if (art == XFG_LLF)
                 kb_fused<true><<<e->nblk[PH_FUSED], fz::THREADS, sizeof(FusedTile), st>>>(e->dm, tab(e, PH_FUSED), n, e->fk, flag);
             else
                 kb_fused<false><<<e->nblk[PH_FUSED], fz::THREADS, sizeof(FusedTile), st>>>(e->dm, tab(e, PH_FUSED), n, e->fk, flag);
         }
         if (!e->nblk[PH_STATES]) continue;  // no member left on the separate stage kernels
-        if (mixed) kb_states<true><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
-        else kb_states<false><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n, e->th, flag, flag == 3);
-        const int art = e->sc.artificial_type;
-        if (art == XFG_GLF) {
-            if (mixed) kb_glf<true><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n);
-            else kb_glf<false><<<e->nblk[PH_STATES], kThreads, 0, st>>>(e->dm, tab(e, PH_STATES), n);
-        }
+        ops->states(e->dm, tab(e, PH_STATES), e->nblk[PH_STATES], n, e->th, e->sc.ghost_species, flag, flag == 3, st);
+        if (art == XFG_GLF) ops->glf(e->dm, tab(e, PH_STATES), e->nblk[PH_STATES], n, st);
         if (e->fused_faces) {
-            const int nb = e->nblk[PH_FALL];
-            const int *t = tab(e, PH_FALL);
-            if (nb) {
-                if (mixed) {
-                    if (order == 5) kb_faces_all_m5<<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
-                    else if (order == 6) kb_faces_all<6, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
-                    else kb_faces_all<7, true><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
-                } else {
-                    if (order == 5) kb_faces_all<5, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
-                    else if (order == 6) kb_faces_all<6, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
-                    else kb_faces_all<7, false><<<nb, kThreads, 0, st>>>(e->dm, t, 3 * n, e->th, flag, art);
-                }
-            }
+            if (e->nblk[PH_FALL]) ops->faces_all(e->dm, tab(e, PH_FALL), e->nblk[PH_FALL], 3 * n, e->th, order, flag, art, st);
         } else {
-#define XFG_FACES(D, PH)                                                                                           \
-            if (e->nblk[PH]) {                                                                                     \
-                const int *t = tab(e, PH);                                                                         \
-                const unsigned nb = e->nblk[PH];                                                                   \
-                if (mixed) {                                                                                       \
-                    if (order == 5) kb_faces_m5<D><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);         \
-                    else if (order == 6) kb_faces<D, 6, true><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art); \
-                    else kb_faces<D, 7, true><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);             \
-                } else {                                                                                           \
-                    if (order == 5) kb_faces<D, 5, false><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);  \
-                    else if (order == 6) kb_faces<D, 6, false><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art); \
-                    else kb_faces<D, 7, false><<<nb, kThreads, 0, st>>>(e->dm, t, n, e->th, flag, art);            \
-                }                                                                                                  \
-            }
-            XFG_FACES(0, PH_F0)
-            XFG_FACES(1, PH_F1)
-            XFG_FACES(2, PH_F2)
-#undef XFG_FACES
+            for (int d = 0; d < 3; d++)
+                if (e->nblk[PH_F0 + d])
+                    ops->faces(e->dm, tab(e, PH_F0 + d), e->nblk[PH_F0 + d], n, e->th, d, order, flag, art, st);
         }
-        if (e->sc.positivity) {
-            if (mixed) kb_pp<true><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
-            else kb_pp<false><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
-        }
-        if (mixed) kb_div_rk<true><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
-        else kb_div_rk<false><<<e->nblk[PH_DIV], kThreads, 0, st>>>(e->dm, tab(e, PH_DIV), n, flag);
+        if (e->sc.positivity) ops->pp(e->dm, tab(e, PH_DIV), e->nblk[PH_DIV], n, flag, st);
+        ops->div_rk(e->dm, tab(e, PH_DIV), e->nblk[PH_DIV], n, flag, st);
     }
 }
 
@@ -556,18 +379,33 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
                         int device, xfg_ensemble **out) {
     if (!out || !scheme || capacity <= 0) return efail(-1, "bad argument%s");
     *out = nullptr;
-    if (scheme->cop) return efail(-1, "the ensemble engine serves single-gas members (cop = 0)%s");
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_MIXED)
         return efail(-1, "ensemble precision must be XFG_FP64 or XFG_MIXED%s");
     if (scheme->positivity != 0 && scheme->positivity != 1) return efail(-1, "positivity must be 0 or 1%s");
-    if (scheme->viscous) return efail(-1, "the ensemble engine serves inviscid single-gas members%s");
+    if (scheme->viscous) return efail(-1, "the ensemble engine serves inviscid members%s");
     if (scheme->scheme_order < 5 || scheme->scheme_order > 7) return efail(-1, "scheme_order must be 5, 6 or 7%s");
+    const int ns = scheme->cop ? scheme->num_species : 1;
+    if (scheme->cop && (!thermal || thermal->num_species != ns))
+        return efail(-1, "a mixture ensemble needs the thermal tables of its num_species%s");
+    // mixtures with the positivity limiter keep the uncontracted face sweeps in the FP64 form, as
+    // the single-grid path does (its theta amplifies the rounding of the high-order flux)
+    const int table_prec = scheme->cop && scheme->positivity && scheme->precision == XFG_FP64 ? XFG_FP64_STRICT
+                                                                                           : scheme->precision;
+    const EnsOps *ops = find_ens_ops(scheme->cop ? 1 : 0, ns, table_prec);
+    if (!ops || !ops->faces)
+        return efail(-1, "no batched kernels for this gas model (single gas, or a mixture of 5 species)%s");
     ECK(cudaSetDevice(device));
     xfg_ensemble *e = new xfg_ensemble();
     e->device = device, e->sc = *scheme, e->capacity = capacity;
+    e->ops = ops, e->NS = ns, e->E = scheme->cop ? ns + 4 : 5;
     std::memset(&e->th, 0, sizeof e->th);
     e->th.ncop_gamma = scheme->ncop_gamma;
-    e->th.nasa = 1;
+    e->th.nasa = scheme->cop ? (scheme->thermo ? 1 : 0) : 1;
+    if (scheme->cop) {  // the thermo tables as xfg_create passes them to the kernels
+        for (int n = 0; n < XFG_MAX_SPECIES; n++) e->th.Ri[n] = thermal->Ri[n], e->th._Wi[n] = thermal->_Wi[n];
+        for (int q = 0; q < XFG_MAX_SPECIES * 21; q++) e->th.Hia[q] = thermal->Hia[q];
+        for (int q = 0; q < XFG_MAX_SPECIES * 6; q++) e->th.Hib[q] = thermal->Hib[q];
+    }
     e->hm.assign(capacity, Member{});
     for (auto &m : e->hm) std::memset(&m, 0, sizeof m);
     e->m_off.assign(capacity, 0), e->m_len.assign(capacity, 0), e->blocks.assign(capacity, xfg_block{});
@@ -590,7 +428,7 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
     }
     e->pool_bytes = pool_bytes;
     e->alloc.init(pool_bytes);
-    e->fused_ok = scheme->precision == XFG_MIXED && scheme->scheme_order == 5 && !scheme->positivity &&
+    e->fused_ok = !scheme->cop && scheme->precision == XFG_MIXED && scheme->scheme_order == 5 && !scheme->positivity &&
                   (scheme->artificial_type == XFG_LLF || scheme->artificial_type == XFG_ROE);
     if (e->fused_ok) {
         const double gm1 = scheme->ncop_gamma - 1.0;
@@ -626,35 +464,49 @@ int xfg_ensemble_destroy(xfg_ensemble *e) {
 }
 
 size_t xfg_ensemble_member_bytes(const xfg_block *block, int precision) {
-    return block ? member_bytes(*block, precision == XFG_MIXED) : 0;
+    return block ? member_bytes(*block, 0, 1, precision == XFG_MIXED) : 0;
+}
+
+size_t xfg_ensemble_member_bytes_for(const xfg_block *block, const xfg_scheme *scheme) {
+    if (!block || !scheme) return 0;
+    return member_bytes(*block, scheme->cop ? 1 : 0, scheme->cop ? scheme->num_species : 1,
+                        scheme->precision == XFG_MIXED);
 }
 
 int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_aos, double target_t, int *slot) {
+    return xfg_ensemble_add_t(e, block, U_aos, nullptr, target_t, slot);
+}
+
+int xfg_ensemble_add_t(xfg_ensemble *e, const xfg_block *block, const double *U_aos, const double *T, double target_t,
+                       int *slot) {
     if (!e || !block || !U_aos || !slot) return efail(-1, "null argument%s");
+    if (e->sc.cop && !T) return efail(-1, "a mixture member needs its temperature (the Newton warm start)%s");
     *slot = -1;
     int s = -1;
     for (int q = 0; q < e->capacity; q++)
         if (!e->hm[q].active && e->m_len[q] == 0) { s = q; break; }
     if (s < 0) return 1;  // no free slot
     const bool mixed = e->sc.precision == XFG_MIXED;
-    const size_t need = member_bytes(*block, mixed);
+    const size_t need = member_bytes(*block, e->sc.cop, e->NS, mixed);
     size_t off = 0;
     if (!e->alloc.alloc(need, &off)) return 2;  // no memory: admission waits
     ECK(cudaSetDevice(e->device));
     Member &m = e->hm[s];
     std::memset(&m, 0, sizeof m);
-    carve(m, e->pool + off, *block, mixed);
+    carve(m, e->pool + off, *block, e->sc.cop, e->NS, mixed);
     m.f.dtbuf = e->ddt + 8 * s;
     m.f.err = e->derr + 8 * s;
     m.active = 1;
     m.fused = e->fused_ok && two_d(*block) ? 1 : 0;
     e->m_off[s] = off, e->m_len[s] = need, e->blocks[s] = *block;
     const long long N = m.g.ncell(), P = m.g.pitch;
+    const int E = e->E;
     ECK(cudaMemsetAsync(e->pool + off, 0, need, e->st));
-    double *stage = m.f.LU;  // AoS staging in LU (5 * P >= 5 * N)
-    ECK(cudaMemcpyAsync(stage, U_aos, sizeof(double) * 5 * N, cudaMemcpyDefault, e->st));
-    kb_aos_to_soa<<<(unsigned)((5 * N + 255) / 256), 256, 0, e->st>>>(stage, m.f.U, 5, N, P);
-    ECK(cudaMemcpyAsync(m.f.U1, m.f.U, sizeof(double) * 5 * P, cudaMemcpyDeviceToDevice, e->st));
+    double *stage = m.f.LU;  // AoS staging in LU (E * P >= E * N)
+    ECK(cudaMemcpyAsync(stage, U_aos, sizeof(double) * E * N, cudaMemcpyDefault, e->st));
+    kb_aos_to_soa<<<(unsigned)((E * N + 255) / 256), 256, 0, e->st>>>(stage, m.f.U, E, N, P);
+    ECK(cudaMemcpyAsync(m.f.U1, m.f.U, sizeof(double) * E * P, cudaMemcpyDeviceToDevice, e->st));
+    if (T) ECK(cudaMemcpyAsync(m.f.T, T, sizeof(double) * N, cudaMemcpyDefault, e->st));
     if (m.fused)  // the first stage's output buffer starts as U1 does (ghost cells of no-op sides)
         ECK(cudaMemcpyAsync(m.f.U2, m.f.U, sizeof(double) * 5 * P, cudaMemcpyDeviceToDevice, e->st));
     double dtb[8] = {0.0, 0.0, target_t, 0.0, 0.0, 0.0, 0.0, 0.0};
@@ -664,10 +516,11 @@ int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_ao
     LaunchCtx c;
     std::memset(&c, 0, sizeof c);
     c.g = m.g, c.f = m.f, c.th = e->th, c.st = e->st, c.artificial = e->sc.artificial_type;
+    c.ghost = e->sc.ghost_species;
     for (int q = 0; q < 6; q++) c.bc[q] = m.bc[q];
     c.precision = e->sc.precision;
-    const Ops *ops = find_ops(0, 1, e->sc.scheme_order, e->sc.precision);
-    if (!ops) return efail(-1, "no single-gas kernels for this scheme%s");
+    const Ops *ops = find_ops(e->sc.cop ? 1 : 0, e->NS, e->sc.scheme_order, e->sc.precision);
+    if (!ops) return efail(-1, "no single-grid kernels for this scheme%s");
     ops->bc(c, m.f.U, nullptr);
     ops->states(c, m.f.U, 1, 0);
     ECK(cudaGetLastError());
@@ -742,8 +595,9 @@ int xfg_ensemble_get_state(xfg_ensemble *e, int slot, double *U_aos) {
     ECK(cudaSetDevice(e->device));
     const Member &m = e->hm[slot];
     const long long N = m.g.ncell(), P = m.g.pitch;
-    kb_soa_to_aos<<<(unsigned)((5 * N + 255) / 256), 256, 0, e->st>>>(m.f.U, m.f.LU, 5, N, P);
-    ECK(cudaMemcpyAsync(U_aos, m.f.LU, sizeof(double) * 5 * N, cudaMemcpyDefault, e->st));
+    const int E = e->E;
+    kb_soa_to_aos<<<(unsigned)((E * N + 255) / 256), 256, 0, e->st>>>(m.f.U, m.f.LU, E, N, P);
+    ECK(cudaMemcpyAsync(U_aos, m.f.LU, sizeof(double) * E * N, cudaMemcpyDefault, e->st));
     ECK(cudaStreamSynchronize(e->st));
     return 0;
 }
@@ -763,7 +617,7 @@ int xfg_ensemble_get_option(xfg_ensemble *e, int option, int *value) {
 int xfg_ensemble_checkpoint_write(xfg_ensemble *e, int slot, const char *path, float duration, double *lam_out) {
     if (!e || !path || slot < 0 || slot >= e->capacity || e->m_len[slot] == 0) return efail(-1, "bad slot%s");
     const Member &m = e->hm[slot];
-    std::vector<double> U((size_t)m.g.ncell() * 5);
+    std::vector<double> U((size_t)m.g.ncell() * e->E);
     int rc = xfg_ensemble_get_state(e, slot, U.data());
     if (rc) return rc;
     double b[8];
@@ -790,6 +644,7 @@ int xfg_ensemble_add_checkpoint(xfg_ensemble *e, const xfg_block *block, const c
                                 const double *lam_in, int *slot) {
     if (!e || !block || !path || !slot) return efail(-1, "null argument%s");
     *slot = -1;
+    if (e->sc.cop) return efail(-1, "a mixture member cannot be restored from a checkpoint (it holds no temperature)%s");
     const size_t n = (size_t)block->Xmax * block->Ymax * block->Zmax * 5;
     std::FILE *fp = std::fopen(path, "rb");
     if (!fp) return efail(-1, "cannot open %s", path);

@@ -1,4 +1,5 @@
-"""Batched ensemble of independent single-gas grids over the C ABI (xfg_ensemble_*).
+"""Batched ensemble of independent grids (single gas, or 5-species mixtures) over the C ABI
+(xfg_ensemble_*).
 
 Each member is one XFLUIDS run of the same scheme with its own size, state, dt and target time;
 all members share one device pool and one sequence of batched kernels per step, replayed from a
@@ -42,15 +43,23 @@ class Ensemble:
             pass
 
     @staticmethod
-    def member_bytes(block: Block, precision: int) -> int:
+    def member_bytes(block: Block, precision, scheme: Scheme = None) -> int:
+        """Pool bytes of one member: a single gas of this precision, or a member under `scheme`."""
+        if scheme is not None:
+            return lib().xfg_ensemble_member_bytes_for(C.byref(block), C.byref(scheme))
         return lib().xfg_ensemble_member_bytes(C.byref(block), precision)
 
-    def add(self, block: Block, U: np.ndarray, target_t: float):
-        """Admit a member; returns its slot, or None when no slot or no pool memory is free."""
+    def add(self, block: Block, U: np.ndarray, target_t: float, T: np.ndarray = None):
+        """Admit a member (T: the temperature that warm-starts a mixture's Newton iteration);
+        returns its slot, or None when no slot or no pool memory is free."""
         U = np.ascontiguousarray(U, dtype=np.float64)
+        Tp = None
+        if T is not None:
+            T = np.ascontiguousarray(T, dtype=np.float64)
+            Tp = T.ctypes.data_as(C.c_void_p)
         slot = C.c_int(-1)
-        rc = check(lib().xfg_ensemble_add(self._e, C.byref(block), U.ctypes.data_as(C.c_void_p), float(target_t),
-                                          C.byref(slot)))
+        rc = check(lib().xfg_ensemble_add_t(self._e, C.byref(block), U.ctypes.data_as(C.c_void_p), Tp,
+                                            float(target_t), C.byref(slot)))
         if rc in (NO_SLOT, NO_MEMORY):
             return None
         self.blocks[slot.value] = block
@@ -73,7 +82,7 @@ class Ensemble:
 
     def get_state(self, slot: int) -> np.ndarray:
         b = self.blocks[slot]
-        out = np.empty(b.ncell * 5, dtype=np.float64)
+        out = np.empty(b.ncell * self.scheme.Emax, dtype=np.float64)
         check(lib().xfg_ensemble_get_state(self._e, slot, out.ctypes.data_as(C.c_void_p)))
         return out
 
