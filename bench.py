@@ -209,6 +209,15 @@ def run_reference_arm(args, world, rank):
     return 0
 
 
+_T0 = time.perf_counter()
+
+
+def progress(what):
+    """One progress line on stderr (the JSON result stays the only line on stdout)."""
+    sys.stderr.write(f"[bench {time.perf_counter() - _T0:8.1f} s] {what}\n")
+    sys.stderr.flush()
+
+
 def vortex_workload(n):
     """The config.workload string of both arms."""
     return f"2D isentropic Euler vortex {n}^2, periodic [0,10]^2, WENO5-JS LLF, SSP-RK3, CFL 0.5"
@@ -253,38 +262,45 @@ def bench_ensemble(args, local, members, scheme, precision):
             "tuned_ms_per_step": [round(t[1], 3) for t in rep["trials"]]}, states
 
 
-def bench_ensemble_solve(local, members, scheme, precision, chunk=256):
+def bench_ensemble_solve(local, members, scheme, precision, chunk=256, max_chunks=120):
     """Whole solve of the batched ensemble to its end time t = 0.25: every member advanced until it
     is done; members that finished (or stopped on a numerical error) leave the launch tables after
     each chunk of graph-replayed steps. Device time (CUDA events) and wall time of the solve,
-    cell-updates performed, the members stopped by an error."""
+    cell-updates performed, the members stopped by an error; bounded by max_chunks, with members
+    whose time stopped moving (dt = 0) reported as stalled and those left as unfinished."""
     from xfluids_gb300.ensemble import Ensemble
     scheme.precision = precision
     pool = sum(Ensemble.member_bytes(b, precision) for b, _ in members) + 4096 * len(members)
     e = Ensemble(scheme, capacity=len(members), pool_bytes=pool, device=local)
-    failed, work, dev_ms, chunks = [], 0, 0.0, 0
+    failed, stalled, work, dev_ms, chunks = [], [], 0, 0.0, 0
     try:
         live = {e.add(b, U, 0.25): q for q, (b, U) in enumerate(members)}
         assert None not in live
+        t_prev = {slot: 0.0 for slot in live}
         t0 = time.perf_counter()
-        while live:
+        while live and chunks < max_chunks:
             _, ms = e.advance(chunk)
             dev_ms += ms
             chunks += 1
             for slot in list(live):
                 info = e.status(slot)
-                if info["done"]:
+                # a member whose time did not move over a whole chunk (dt = 0) would never finish
+                stuck = not info["done"] and info["t"] <= t_prev[slot]
+                t_prev[slot] = info["t"]
+                if info["done"] or stuck:
                     q = live.pop(slot)
                     work += members[q][0].X_inner * members[q][0].Y_inner * info["steps"]
                     if info["error"]:
                         failed.append(q)
+                    if stuck:
+                        stalled.append(q)
                     e.remove(slot)
         wall = time.perf_counter() - t0
     finally:
         e.close()
     return {"t_end": 0.25, "device_s": dev_ms * 1e-3, "wall_s": wall, "cell_updates": work,
             "cell_updates_per_s": work / (dev_ms * 1e-3), "failed_members": sorted(failed), "chunks": chunks,
-            "steps_per_chunk": chunk}
+            "steps_per_chunk": chunk, "stalled_members": sorted(stalled), "unfinished_members": sorted(live.values())}
 
 
 def bench_serving(local, count, precision, fp64_check_work=3e8):
@@ -388,6 +404,61 @@ def bench_mixing_layer(args, local, steps):
     return res
 
 
+def mixing_members(count=16, seed=7):
+    """Members of the batched mixing-layer ensemble: `count` temporal mixing layers (the 5-species
+    case of bench_mixing_layer, WENO7 LLF) of seeded sizes 32 a x 16 b x 16 c, a, b, c uniform in
+    [4, 8] (about 2.4 M cells a member on average)."""
+    from xfluids_gb300 import thermo
+    th = thermo.load_thermal(cases_mod().MIXING_SPECIES, 0, tables_json=THERMO_JSON)
+    rng = np.random.default_rng(seed)
+    out, s = [], None
+    for q in range(count):
+        a, b_, c = (int(v) for v in rng.integers(4, 9, size=3))
+        b, s, th, U, T = cases_mod().mixing_layer((32 * a, 16 * b_, 16 * c), thermal=th, seed=1234 + q)
+        out.append((b, U, T))
+    return s, th, out
+
+
+def bench_mixing_ensemble(local, steps, count=16):
+    """Batched ensemble of 3D mixing layers (mixing_members), FP64 and mixed: all members admitted,
+    one warm-up step (graph capture), then `steps` batched steps timed with CUDA events; per
+    component L1 of the mixed states against the FP64 ones after the same steps."""
+    from xfluids_gb300.abi import MIXED
+    from xfluids_gb300.ensemble import Ensemble
+    from xfluids_gb300.workloads import per_component
+    s, th, ms = mixing_members(count)
+    res, states = {}, {}
+    for prec in (0, MIXED):
+        s.precision = prec
+        pool = sum(Ensemble.member_bytes(b, prec, scheme=s) for b, _, _ in ms) + 4096 * len(ms)
+        e = Ensemble(s, capacity=len(ms), pool_bytes=pool, device=local, thermal=th)
+        try:
+            slots = [e.add(b, U, 1e300, T=T) for b, U, T in ms]
+            assert None not in slots
+            e.advance(1)
+            before = [e.status(q)["steps"] for q in slots]
+            st, dev_ms = e.advance(steps)
+            info = [e.status(q) for q in slots]
+            states[prec] = [e.get_state(q) for q in slots]
+        finally:
+            e.close()
+        work = sum(b.X_inner * b.Y_inner * b.Z_inner * (i["steps"] - s0) for (b, _, _), i, s0 in zip(ms, info, before))
+        res["mixed" if prec else "fp64"] = {"value": work / (dev_ms * 1e-3), "ms_per_step": dev_ms / steps,
+                                            "cell_updates": work, "status": st,
+                                            "failed_members": [q for q, i in enumerate(info) if i["error"]]}
+    names = ["rho", "rho_u", "rho_v", "rho_w", "E", "rho_Y_H2", "rho_Y_O2", "rho_Y_N2", "rho_Y_H2O"]
+    inner = lambda b, x: x.reshape(b.Zmax, b.Ymax, b.Xmax, -1)[b.inner_slices()].reshape(-1, x.size // (b.Zmax * b.Ymax * b.Xmax))
+    got = np.concatenate([inner(b, x)[:, :9] for (b, _, _), x in zip(ms, states[MIXED])])
+    ref = np.concatenate([inner(b, x)[:, :9] for (b, _, _), x in zip(ms, states[0])])
+    res.update({"workload": f"{count} temporal mixing layers (5 species, WENO7-JS LLF, SSP-RK3, CFL 0.5) of sizes "
+                            "32a x 16b x 16c, a, b, c ~ U[4, 8] (seed 7), one batched launch per phase, CUDA-graph replay",
+                "cells": sum(b.X_inner * b.Y_inner * b.Z_inner for b, _, _ in ms), "steps": steps,
+                "sizes": [f"{b.X_inner}x{b.Y_inner}x{b.Z_inner}" for b, _, _ in ms],
+                "mixed_speedup_vs_fp64": res["mixed"]["value"] / res["fp64"]["value"],
+                "per_component_mixed_vs_fp64": per_component(got, ref, names)})
+    return res
+
+
 def accuracy_gpu(local, n=192, t_end=0.5):
     """FP64 and mixed runs of the 2D vortex n^2 to t_end on the GPU, free running (no
     resynchronisation); the inner-cell states are compared in the CPU leg (accuracy_vs_oracle)."""
@@ -477,6 +548,7 @@ def run_gpu_arm(args, world, rank, local):
         fl.time = 0.0
 
     # ---- plain FP64 path: device-timed value --------------------------------------------------
+    progress("plain FP64 vortex")
     f, b, U0 = setup(0)
     f.advance(args.warmup)          # warm-up (also captures the step graph)
     reset(f, U0)
@@ -499,6 +571,7 @@ def run_gpu_arm(args, world, rank, local):
     ms_total_fp64 = ms / k
 
     # ---- end to end through the public API with host buffers -----------------------------------
+    progress("e2e through the C ABI")
     E = 5
     host = PinnedArray(U0.size)
     host.array[:] = U0.reshape(-1)
@@ -521,6 +594,7 @@ def run_gpu_arm(args, world, rank, local):
     host.close()
 
     # ---- mixed precision form, from the same initial state to the same final time ---------------
+    progress("mixed vortex")
     fm, _, _ = setup(MIXED)
     fm.advance(args.warmup)
     reset(fm, U0)
@@ -544,6 +618,7 @@ def run_gpu_arm(args, world, rank, local):
     # ---- batched ensemble, FP64 and mixed, and the serving trace -----------------------------
     ens = {}
     if args.ensemble:
+        progress("batched ensemble")
         scheme_e, members = cases.riemann_ensemble(256, seed=0)
         e64, s64 = bench_ensemble(args, local, members, scheme_e, 0)
         emx, smx = bench_ensemble(args, local, members, scheme_e, MIXED)
@@ -562,9 +637,18 @@ def run_gpu_arm(args, world, rank, local):
                "linf_mixed_vs_fp64": float(max(x.max() for x in diff))}
         del s64, smx, diff
         if args.ensemble_solve:
+            progress("ensemble whole solve")
             ens["whole_solve_mixed"] = bench_ensemble_solve(local, members, scheme_e, MIXED)
+    progress("serving trace")
     serving = bench_serving(local, args.serve_requests, MIXED) if args.serve_requests > 0 else None
+    progress("mixing layer")
     mixing = bench_mixing_layer(args, local, args.mixing_steps) if args.mixing_steps > 0 else None
+    if mixing is not None and args.mixing_ensemble > 0:
+        progress("batched mixing-layer ensemble")
+        mixing["batched_ensemble"] = bench_mixing_ensemble(local, args.mixing_steps, args.mixing_ensemble)
+        for p in ("fp64", "mixed"):
+            mixing["batched_ensemble"][p]["vs_single_grid"] = mixing["batched_ensemble"][p]["value"] / mixing[p]["value"]
+    progress("accuracy runs")
     accuracy_runs = accuracy_gpu(local) if args.accuracy else None
     d.close()
     if rank != 0:
@@ -573,7 +657,9 @@ def run_gpu_arm(args, world, rank, local):
     fp64_peak = peaks["fp64_flops"] / 1e12
     traffic = None if NCU_FACE_BYTES_FP64 is None else NCU_FACE_BYTES_FP64 * faces_per_launch
     cpu_threads = os.cpu_count() or 1
+    progress("CPU leg")
     cpu_val, cpu_steps, cpu_el, accuracy = cpu_leg(cpu_threads, accuracy_runs)
+    progress("done")
     line = {
         "metric": "cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
         "steps": k, "warmup": args.warmup, "ms_per_step": ms_total_fp64, "higher_is_better": True,
@@ -629,6 +715,7 @@ def main():
     ap.add_argument("--ensemble-solve", type=int, default=1, help="whole mixed solve of the ensemble to t = 0.25 (0 = skip)")
     ap.add_argument("--serve-requests", type=int, default=100, help="requests of the serving trace (0 = skip)")
     ap.add_argument("--mixing-steps", type=int, default=2, help="timed steps of the 3D mixing layer (0 = skip)")
+    ap.add_argument("--mixing-ensemble", type=int, default=16, help="members of the batched mixing-layer ensemble (0 = skip)")
     ap.add_argument("--accuracy", type=int, default=1, help="FP64 drift vs the oracle and error vs the exact vortex")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

@@ -155,3 +155,31 @@ def test_fused_launches_and_phases(cuda_lib):
     rho = f.get("rho").reshape(b.Ymax, b.Xmax)
     assert np.all(rho > 0.3) and np.all(rho < 1.1)
     f.close()
+
+
+@pytest.mark.parametrize("name", ["vortex200x90", "riemann40_roe_inflow", "riemann48_outflow"])
+def test_tma_staged_kernel_equals_one_tile_per_cta(name, cuda_lib, monkeypatch):
+    """Blocks with an even Xmax run the persistent kernel whose state arrives by TMA copies
+    (k_fused_stage_tma); XFG_FUSED_TMA=0 at handle creation selects the one-tile-per-CTA kernel.
+    Both compute every tile with the same instructions from the same values: the states after
+    free-running steps (LU included, through a stage-API step) are bitwise equal."""
+    make = (lambda: _vortex(200, 90)) if name == "vortex200x90" else CASES[name]
+    out = []
+    for env in ("1", "0"):
+        monkeypatch.setenv("XFG_FUSED_TMA", env)
+        b, s, th, U, T = make()
+        if name.endswith("_roe"):
+            s.artificial_type = ROE
+        s.precision = MIXED
+        assert b.Xmax % 2 == 0
+        f = _fluid(b, s, th, U, T)
+        f.initialize()
+        st, t, n = f.advance(10)
+        assert st == 0 and n == 10
+        dt = f.GetFluidDt()
+        for flag in (1, 2, 3):
+            f.stage(flag, dt)
+        out.append((f.get("U").copy(), f.get("LU").copy(), t))
+        f.close()
+    assert out[0][2] == out[1][2]
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])

@@ -1,9 +1,12 @@
 // xfg_api.cu - C ABI of the library (include/xfluids_gb300.h): handle, device memory, the
 // stage-by-stage entry points that replace class Fluid's methods, the fused step and the
 // graph-replayed multi-step advance.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -143,9 +146,39 @@ struct xfg_handle {
     bool fused = false;               // stages run as the fused mixed kernel (xfg_fused.cuh)
     cudaGraphExec_t graph = nullptr;  // one fused step, replayed by xfg_advance
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    alignas(64) CUtensorMap tmap[3];  // fused stages: TMA maps of U, U1, U2 (xfg_fused.cuh)
 };
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// TMA maps of the fused stage's state buffers (k_fused_stage_tma): each a 3D tensor (Xmax, Ymax,
+// 5 components) of FP64 with row stride Xmax and component stride P cells, copied as boxes of
+// FUSED_BOX_X x FUSED_BOX_Y x 5. A map needs 16-byte strides, so Xmax even; an odd Xmax (or
+// XFG_FUSED_TMA=0 in the environment) keeps the one-tile-per-CTA kernel. cuTensorMapEncodeTiled is
+// taken through the runtime's driver entry point, so the library links no libcuda.
+static bool make_fused_tmaps(xfg_handle *h) {
+    const char *env = std::getenv("XFG_FUSED_TMA");
+    if ((env && env[0] == '0') || h->bl.Xmax % 2 || h->bl.DimZ) return false;
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess || q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }();
+    if (!encode) return false;
+    const cuuint64_t dim[3] = {(cuuint64_t)h->bl.Xmax, (cuuint64_t)h->bl.Ymax, 5};
+    const cuuint64_t stride[2] = {(cuuint64_t)h->bl.Xmax * 8, (cuuint64_t)h->P * 8};
+    const cuuint32_t box[3] = {(cuuint32_t)FUSED_BOX_X, (cuuint32_t)FUSED_BOX_Y, 5}, estride[3] = {1, 1, 1};
+    double *buf[3] = {h->ctx.f.U, h->ctx.f.U1, h->ctx.f.U2};
+    for (int q = 0; q < 3; q++)
+        if (encode(&h->tmap[q], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, buf[q], dim, stride, box, estride,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    return true;
+}
 
 // Argument and block checks shared by xfg_create and xfg_compute_lu_noalloc (declared in xfg_ops.h).
 namespace xfg {
@@ -247,6 +280,8 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     if (scheme->viscous && !mixed) nd += 9 + 2;                 // velocity derivatives, mu, kappa
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;  // single-gas fast path extras
     if (fast1) nd += 2 + 3 * (block->DimX + block->DimY + block->DimZ);
+    const bool mixcop = scheme->cop && mixed;                    // mixed mixtures: sqrt(rho), 1/sqrt(rho)
+    if (mixcop) nd += 2;
     for (int d = 0; d < 3; d++)
         if (dims[d] && !mixed) nd += 2 * E;                       // F, Fw
     size_t nf = 0;
@@ -279,6 +314,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
     if (scheme->cop) f.y = take8(NS), f.xc = take8(3 + (NS - 1));
     if (scheme->viscous && !mixed) f.vde = take8(9), f.mu = take8(1), f.kappa = take8(1);
+    if (mixcop) f.sr = take8(1), f.isr = take8(1);
     if (fast1) {
         f.sr = take8(1), f.isr = take8(1);
         for (int d = 0; d < 3; d++)
@@ -329,6 +365,13 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     h->ctx.cfl = block->CFLnumber;
     h->ctx.viscous = scheme->viscous;
     for (int q = 0; q < 6; q++) g.bc[q] = block->Boundarys[q];
+    if (h->fused && make_fused_tmaps(h)) {
+        int nsm = 0;
+        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && nsm > 0) {
+            for (int q = 0; q < 3; q++) h->ctx.tmap[q] = &h->tmap[q];
+            h->ctx.nsm = nsm;
+        }
+    }
     e = cudaMallocHost(&h->host_dtbuf, 8 * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&h->host_err, 64 * sizeof(int));
     for (int q = 0; q < 4 && e == cudaSuccess; q++) e = cudaEventCreate(&h->ev[q]);
@@ -678,6 +721,7 @@ static int finish(xfg_handle *h, double *t, double *dt, int *steps) {
     if (t) *t = h->t;
     if (dt) *dt = h->host_dtbuf[0];
     if (steps) *steps = (int)h->host_dtbuf[3];
+    if (h->host_err[ERR_TMA]) return fail(-2, "a TMA copy of the fused stage did not complete");
     if (h->host_err[ERR_STATE]) return 10000;
     if (h->host_err[ERR_PRIM]) return 1;
     return 0;

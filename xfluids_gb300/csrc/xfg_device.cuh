@@ -114,7 +114,8 @@ using FaceState = FaceStateT<double, NS>;
 // compiled with different floating-point contraction flags in two units stays two kernels.
 namespace XFG_KNS {
 
-// Reciprocal and inverse square root for the single-gas FP64 fast path: the hardware
+// Reciprocal and inverse square root for the single-gas FP64 fast path and the mixed form's
+// mixture states and Roe state: the hardware
 // approximation refined by two Newton-Raphson steps (r <- r (2 - x r); y <- y (1.5 - x y^2 / 2)),
 // within a few ulp of the correctly rounded value for normal finite x.
 __device__ __forceinline__ double rcp_nr(double x) {

@@ -24,7 +24,10 @@
 // exactly what it brings to the next; the RK stage sum is FP64.
 #pragma once
 
+#include <cuda.h>
+
 #include "xfg_mixed.cuh"
+#include "xfg_ops.h"
 
 namespace xfg {
 namespace XFG_KNS {
@@ -43,6 +46,9 @@ constexpr int N_INNER = TY * TX;           // phase-A items: the tile's cells (b
 constexpr int N_YHALO = 2 * HW * TX;       // the three rows below and above (y fluxes),
 constexpr int N_XHALO = TY * 2 * HW;       // the three columns left and right (x fluxes)
 constexpr int NITEMS = N_INNER + N_YHALO + N_XHALO;
+constexpr int RAWW = 40;                   // TMA box of the state: 40 columns (an even start),
+constexpr int RAWN = RH * RAWW;            // the 13 region rows,
+constexpr int RAW_BYTES = 5 * RAWN * 8;    // the 5 components, FP64
 static_assert(TX == 32, "one warp per tile row");
 static_assert(THREADS == 8 * 32 && TY + 1 == 8, "x face rows + 1 warp, y face rows = warps");
 }  // namespace fz
@@ -293,12 +299,19 @@ __device__ __forceinline__ void fused_face(const FusedTile &s, int rcL, int fL, 
 // store_lu keeps LU; want_lam adds the GetDt maxima of the inner cells (GlobalDt_block.hpp:31-66)
 // and writes their FP32 primitives (the last UpdateFluidStates a caller can read).
 // The tile (bx, by) of the block, run by one CTA of fz::THREADS threads with a FusedTile of
-// dynamic shared memory; dt the stage's time step (used when do_rk).
-template <bool LLF>
+// dynamic shared memory; dt the stage's time step (used when do_rk). RAW: phase A reads the state
+// from the shared-memory box `raw` (fz::RAWW cells per row, the tile's region starting at column
+// ox, written by a TMA copy) instead of UI; after_a() is called by every thread once phase A's
+// reads of it are done (the persistent kernel's next copy starts there).
+struct NoHook {
+    __device__ void operator()() const {}
+};
+template <bool LLF, bool RAW = false, class AfterA = NoHook>
 __device__ __forceinline__ void fused_stage_tile(const Geo &g, const DevFields &f, const FusedK &k,
                                                  const double *__restrict__ UI, const double *__restrict__ Uprev,
                                                  double *__restrict__ Uout, int flag, double dt, int do_rk, int store_lu,
-                                                 int want_lam, int bx, int by) {
+                                                 int want_lam, int bx, int by, const double *raw = nullptr, int ox = 0,
+                                                 AfterA after_a = AfterA()) {
     extern __shared__ float4 fz_smem[];
     FusedTile &s = *reinterpret_cast<FusedTile *>(fz_smem);
     __shared__ float red[2][fz::THREADS / 32];
@@ -325,8 +338,17 @@ __device__ __forceinline__ void fused_stage_tile(const Geo &g, const DevFields &
         const int i = g.Bx + x0 + c, j = g.By + y0 + r;
         if (i >= g.Xmax || j >= g.Ymax) continue;
         const long long id = (long long)j * g.Xmax + i;
-        const fp2 rho = split_d(UI[id]), mx = split_d(UI[P + id]), my = split_d(UI[2 * P + id]);
-        const fp2 mz = split_d(UI[3 * P + id]), en = split_d(UI[4 * P + id]);
+        double u5[5];
+        if constexpr (RAW) {
+            const int q = (r + fz::HW) * fz::RAWW + (c + fz::HW + ox);
+#pragma unroll
+            for (int n = 0; n < 5; n++) u5[n] = raw[n * fz::RAWN + q];
+        } else {
+#pragma unroll
+            for (int n = 0; n < 5; n++) u5[n] = UI[n * P + id];
+        }
+        const fp2 rho = split_d(u5[0]), mx = split_d(u5[1]), my = split_d(u5[2]);
+        const fp2 mz = split_d(u5[3]), en = split_d(u5[4]);
         // 1 / rho as a pair: r0 the rounded reciprocal, 1 - rho r0 its exact residual
         const float r0 = __frcp_rn(rho.h);
         const float re = fmaf(-rho.l, r0, fmaf(-rho.h, r0, 1.0f));
@@ -392,6 +414,7 @@ __device__ __forceinline__ void fused_stage_tile(const Geo &g, const DevFields &
         if (lane == 0) red[0][warp] = lamx, red[1][warp] = lamy;
     }
     __syncthreads();
+    after_a();
     if (want_lam && tid == 0) {
         float a = red[0][0], b = red[1][0];
         for (int q = 1; q < fz::THREADS / 32; q++) a = fmaxf(a, red[0][q]), b = fmaxf(b, red[1][q]);
@@ -491,6 +514,94 @@ __global__ void __launch_bounds__(fz::THREADS, 2)
     if (guard && step_done(f)) return;
     fused_stage_tile<LLF>(g, f, k, UI, Uprev, Uout, flag, dt_dev ? dt_dev[0] : dt_arg, do_rk, store_lu, want_lam,
                           blockIdx.x, blockIdx.y);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Persistent form with the state staged by TMA. Each CTA loops over tiles (t = blockIdx.x,
+// + gridDim.x, ...); the FP64 state of a tile's region arrives in shared memory through one
+// cp.async.bulk.tensor.3d copy (a 40 x 13 x 5 box of the handle's SoA state: x from an even
+// column, y, component), signalled on an mbarrier, and the copy of the next tile starts as soon as
+// phase A of the current one has read the box, so it overlaps the face sweeps and the RK stage.
+// Waits are bounded: a copy that does not arrive sets the error word ERR_TMA and the CTA returns.
+// ---------------------------------------------------------------------------------------------
+static_assert(fz::RAWW == FUSED_BOX_X && fz::RH == FUSED_BOX_Y, "TMA box of the host-side tensor maps");
+
+__host__ __device__ constexpr size_t fused_raw_offset() { return (sizeof(FusedTile) + 127) / 128 * 128; }
+// dynamic shared memory of the TMA form: the tile, 128 bytes of slack to align the box, the box,
+// the mbarrier
+__host__ __device__ constexpr size_t fused_tma_smem() { return fused_raw_offset() + 128 + fz::RAW_BYTES + 16; }
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(dst), "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// the region of tile (bx, by) starts at column Bx + 32 bx - 3; the box at that column rounded
+// down to even (16-byte aligned x coordinate), ox the offset of the region in the box
+__device__ __forceinline__ int fused_box_x(const Geo &g, int bx) { return (g.Bx + bx * fz::TX - fz::HW) & ~1; }
+
+template <bool LLF>
+__global__ void __launch_bounds__(fz::THREADS, 2)
+    k_fused_stage_tma(Geo g, DevFields f, FusedK k, const __grid_constant__ CUtensorMap tmap,
+                      const double *__restrict__ UI, const double *__restrict__ Uprev, double *__restrict__ Uout,
+                      int flag, double dt_arg, const double *__restrict__ dt_dev, int do_rk, int store_lu, int want_lam,
+                      int guard, int ntx, int ntiles) {
+    if (guard && step_done(f)) return;
+    extern __shared__ float4 fz_smem[];
+    const unsigned base = smem_u32(fz_smem);
+    const unsigned box = (base + (unsigned)fused_raw_offset() + 127u) & ~127u;
+    const unsigned bar = box + fz::RAW_BYTES;
+    const double *raw = reinterpret_cast<const double *>(reinterpret_cast<const char *>(fz_smem) + (box - base));
+    const double dt = dt_dev ? dt_dev[0] : dt_arg;
+    auto issue = [&](int t) {
+        const int bx = t % ntx, by = t / ntx;
+        mbar_expect_tx(bar, fz::RAW_BYTES);
+        tma_load_3d(box, &tmap, fused_box_x(g, bx), g.By + by * fz::TY - fz::HW, 0, bar);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the barrier, seen by the copy engine
+        if ((int)blockIdx.x < ntiles) issue(blockIdx.x);
+    }
+    __syncthreads();
+    unsigned parity = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        bool ok = false;
+        for (int it = 0; it < (1 << 22) && !ok; it++) ok = mbar_try_wait(bar, parity);
+        parity ^= 1u;
+        if (__syncthreads_or(!ok)) {  // the same decision in every thread of the CTA
+            if (threadIdx.x == 0) atomicOr(&f.err[ERR_TMA], 1);
+            return;
+        }
+        const int bx = t % ntx, by = t / ntx, tn = t + (int)gridDim.x;
+        auto next = [&]() {  // phase A has read the box: the next tile's copy may overwrite it
+            if (threadIdx.x == 0 && tn < ntiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(tn);
+            }
+        };
+        fused_stage_tile<LLF, true>(g, f, k, UI, Uprev, Uout, flag, dt, do_rk, store_lu, want_lam, bx, by, raw,
+                                    g.Bx + bx * fz::TX - fz::HW - fused_box_x(g, bx), next);
+        __syncthreads();  // phase C's reads of the tile arrays before the next phase A writes them
+    }
 }
 
 // Ghost cells of a 2D block: 2 By rows of Xmax cells and 2 Bx columns of the Yi inner rows.

@@ -150,6 +150,22 @@ struct Inst {
         if constexpr (MIXED && !COP) {
             const Geo &g = c.g;
             const dim3 grid((g.Xi + fz::TX - 1) / fz::TX, (g.Yi + fz::TY - 1) / fz::TY, 1);
+            const int which = UI == c.f.U ? 0 : (UI == c.f.U1 ? 1 : (UI == c.f.U2 ? 2 : -1));
+            const CUtensorMap *tm = which >= 0 ? static_cast<const CUtensorMap *>(c.tmap[which]) : nullptr;
+            if (tm && c.nsm > 0) {  // persistent CTAs, the state staged by TMA
+                const int ntiles = (int)(grid.x * grid.y);
+                const int nb = ntiles < 2 * c.nsm ? ntiles : 2 * c.nsm;
+                const size_t sm = fused_tma_smem();
+                if (c.artificial == XFG_LLF)
+                    k_fused_stage_tma<true><<<nb, fz::THREADS, sm, c.st>>>(g, c.f, fused_consts(c), *tm, UI, Uprev, Uout,
+                                                                          flag, 0.0, dt_dev, do_rk, store_lu, want_lam,
+                                                                          guard, (int)grid.x, ntiles);
+                else
+                    k_fused_stage_tma<false><<<nb, fz::THREADS, sm, c.st>>>(g, c.f, fused_consts(c), *tm, UI, Uprev, Uout,
+                                                                           flag, 0.0, dt_dev, do_rk, store_lu, want_lam,
+                                                                           guard, (int)grid.x, ntiles);
+                return;
+            }
             const size_t smem = sizeof(FusedTile);
             if (c.artificial == XFG_LLF)
                 k_fused_stage<true><<<grid, fz::THREADS, smem, c.st>>>(g, c.f, fused_consts(c), UI, Uprev, Uout, flag,
@@ -162,9 +178,14 @@ struct Inst {
     static int fused_prepare() {
         if constexpr (MIXED && !COP) {
             const int smem = (int)sizeof(FusedTile);
+            const int smt = (int)fused_tma_smem();
             cudaError_t e = cudaFuncSetAttribute(k_fused_stage<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(k_fused_stage<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_fused_stage_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smt);
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_fused_stage_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smt);
             return (int)e;
         }
         return 0;

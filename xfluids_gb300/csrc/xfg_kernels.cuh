@@ -18,7 +18,7 @@ namespace xfg {
 constexpr int kThreads = 128;
 
 // error words in DevFields::err
-enum { ERR_STATE = 0, ERR_PRIM = 1, ERR_I = 2, ERR_J = 3, ERR_K = 4, ERR_NWORDS = 8 };
+enum { ERR_STATE = 0, ERR_PRIM = 1, ERR_I = 2, ERR_J = 3, ERR_K = 4, ERR_TMA = 5, ERR_NWORDS = 8 };
 
 namespace XFG_KNS {
 

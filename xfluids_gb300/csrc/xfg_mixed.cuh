@@ -13,6 +13,21 @@
 namespace xfg {
 namespace XFG_KNS {
 
+// FP64 -> FP32 rounded to nearest even by integer operations (the conversion instruction runs on
+// the FP64 pipe, the mixture path's bottleneck): exact for results in the FP32 normal range;
+// magnitudes below 2^-126 give a signed zero, 2^128 and above an infinity, NaN a NaN.
+__device__ __forceinline__ float d2f_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned e = (hi >> 20) & 0x7ffu, sgn = hi & 0x80000000u, mh = hi & 0xfffffu;
+    unsigned fb = ((e - 896u) << 23) + ((mh << 3) | (lo >> 29));  // exponent rebiased, top 23 bits
+    const unsigned rem = lo & 0x1fffffffu;                         // the 29 bits dropped
+    fb += (rem > 0x10000000u || (rem == 0x10000000u && (fb & 1u))) ? 1u : 0u;  // a carry is the next binade
+    fb = e < 897u ? 0u : fb;
+    fb = e > 1150u ? ((e == 0x7ffu && (mh | lo)) ? 0x7fc00000u : 0x7f800000u) : fb;
+    return __uint_as_float(sgn | fb);
+}
+
 // Mixture thermodynamics of the mixed form with the species folded into one polynomial.
 // h(T) = sum_n y_n h_n(T) and Cp(T) = sum_n y_n Cp_n(T) are linear in the species, and the
 // temperature ranges of both tables do not depend on the species (JANAF breaks at 1000 K, NASA-9
@@ -73,7 +88,7 @@ __device__ __forceinline__ void cop_cell_terms_mixed(const DevThermo &th, double
 #pragma unroll
     for (int n = 0; n < NS; n++) h[n] = enthalpy(th, T, n);
     const double q2 = u * u + v * v + w * w;
-    const double CpT_R = Cp * T / (wi * kRu);
+    const double CpT_R = Cp * T * rcp_nr(wi * kRu);
     const double RN = th.Ri[NCOP];
     const double g1 = gm - 1.0;
     xc[id] = gm;
@@ -84,7 +99,8 @@ __device__ __forceinline__ void cop_cell_terms_mixed(const DevThermo &th, double
 }
 
 // get_T (Mixing_device.h:171-193): the same clamped Newton iteration and stopping test on the
-// folded mixture polynomials; returns T and the mixture Cp at T.
+// folded mixture polynomials, the step f / f' with the refined reciprocal of f'; returns T and the
+// mixture Cp at T.
 template <int NS>
 __device__ double newton_T_folded(const DevThermo &t, const double *yi, double e, double T0, double &Cp_out) {
     FoldedThermo<NS> ft;
@@ -100,7 +116,7 @@ __device__ double newton_T_folded(const DevThermo &t, const double *yi, double e
         }
         double f = h - Rm * T - e;
         double df_ = Cp - Rm;
-        double df = fmin(f / (df_ + 1.0e-30), 1e-3 * T);
+        double df = fmin(f * rcp_nr(df_ + 1.0e-30), 1e-3 * T);
         df = fmax(df, -1e-2 * T);
         T = T - df;
         if (fabs(df) <= 1.0e-6) break;
@@ -112,7 +128,9 @@ __device__ double newton_T_folded(const DevThermo &t, const double *yi, double e
 }
 
 // Primitive recovery of the mixed form. Single gas: from the FP64 state converted once to FP32.
-// Mixture: the FP64 recovery of k_states (Newton in FP64), followed by the FP32 copies.
+// Mixture: the FP64 recovery of k_states (Newton in FP64, refined reciprocals instead of
+// divisions), sqrt(rho) and 1 / sqrt(rho) for the faces' Roe weights, the FP32 copies converted by
+// integer operations, the sound speed in FP32.
 template <bool COP, int NS>
 __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields &f, const DevThermo &th,
                                                   double *__restrict__ UI, int ghost, int want_lam, long long id,
@@ -140,14 +158,14 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             double U[E];
 #pragma unroll
             for (int n = 0; n < E; n++) U[n] = UI[n * P + id];
-            const double rhod = U[0], rho1 = 1.0 / rhod;
+            const double rhod = U[0], rho1 = rcp_nr(rhod);
             double yi[NS];
             if (ghost) {
                 yi[NCOP] = 0.0;
                 double sum = 0.0;
 #pragma unroll
                 for (int s = 0; s < NCOP; s++) yi[s] = U[s + 5] * rho1, sum += yi[s];
-                sum = 1.0 / sum;
+                sum = rcp_nr(sum);
 #pragma unroll
                 for (int s = 0; s < NCOP; s++) {
                     yi[s] *= sum;
@@ -166,19 +184,24 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             const double T = newton_T_folded<NS>(th, yi, tme, f.T[id], Cp);
             const double pd = rhod * Rm * T;
             const double wi = mix_W_inv<NS>(th, yi);
-            const double gmx = Cp / (Cp - kRu * wi);
+            const double gmx = Cp * rcp_nr(Cp - kRu * wi);
             const double gamma = gmx > 1.0 ? gmx : -1.0;
             const double Hd = (U[4] + pd) * rho1;
-            const double cd = sqrt(gamma * pd * rho1);
-            f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd, f.c[id] = cd;
+            // sqrt(rho) and 1 / sqrt(rho) for the Roe weights of the mixed faces (face_state_mixed)
+            const double isr = rsqrt_nr(rhod);
+            f.sr[id] = rhod * isr, f.isr[id] = isr;
+            f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd;
             f.e[id] = tme, f.gamma[id] = gamma, f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
-            if (f.Tf) f.Tf[id] = (float)T;  // viscous schemes: the heat flux's FP32 temperature
+            if (f.Tf) f.Tf[id] = d2f_rn(T);  // viscous schemes: the heat flux's FP32 temperature
             if (f.xc) cop_cell_terms_mixed<NS>(th, T, Cp, gmx, wi, ud, vd, wd, Hd, pd, rho1, f.xc, P, id);
 #pragma unroll
-            for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = (float)yi[s];
+            for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = d2f_rn(yi[s]);
 #pragma unroll
-            for (int n = 0; n < E; n++) Uf[n] = (float)U[n];
-            rho = (float)rhod, u = (float)ud, v = (float)vd, w = (float)wd, p = (float)pd, H = (float)Hd, c = (float)cd;
+            for (int n = 0; n < E; n++) Uf[n] = d2f_rn(U[n]);
+            rho = d2f_rn(rhod), u = d2f_rn(ud), v = d2f_rn(vd), w = d2f_rn(wd), p = d2f_rn(pd), H = d2f_rn(Hd);
+            // the sound speed feeds only the FP32 face primitives (LLF maxima, dt): FP32
+            c = sqrtf(d2f_rn(gamma) * p / rho);
+            f.c[id] = (double)c;
         }
 #pragma unroll
         for (int n = 0; n < E; n++) f.Uf[n * P + id] = Uf[n];
@@ -303,6 +326,85 @@ __device__ __forceinline__ float project_r(const float *lrow, int n, const float
     return acc;
 }
 
+// Roe state of a mixture face for the mixed form: the quantities of face_state's mixture branch
+// (MARCO_ROE, Eigen_callback.h:87-91 and Utils_device.hpp:42-140: Roe averages, the pressure-
+// derivative corrections of the multi-component sound speed, the MARCO_PREEIGEN terms), in FP64
+// with the per-cell sqrt(rho) and 1 / sqrt(rho) of k_states_mixed (D = sqrt(rho_r / rho_l) and
+// sqrt(rho_l rho_r) without a square root, p / rho = p (1 / sqrt(rho))^2), the refined reciprocals
+// of rcp_nr for the five divisions and rsqrt_nr for c and 1 / c; the results rounded to FP32 by
+// integer operations. The same mathematics as face_state, another FP64 rounding.
+template <int NS>
+__device__ __forceinline__ void face_state_mixed(const DevFields &f, long long P, long long l, long long r,
+                                                 FaceStateT<float, NS> &F) {
+    constexpr int NCOP = NS - 1;
+    const double srl = f.sr[l], srr = f.sr[r], isl = f.isr[l], isr = f.isr[r];
+    const double rl = f.rho[l], rr = f.rho[r];
+    const double ul = f.u[l], ur = f.u[r], vl = f.v[l], vr = f.v[r], wl = f.w[l], wr = f.w[r];
+    const double Hl = f.H[l], Hr = f.H[r], pl = f.p[l], pr = f.p[r];
+    const double D = srr * isl;                 // sqrt(rho_r / rho_l)
+    const double D1 = srl * rcp_nr(srl + srr);  // 1 / (D + 1)
+    auto roe = [&](double a, double b) { return fma(D, b, a) * D1; };  // (a + D b) / (1 + D)
+    const double _u = roe(ul, ur), _v = roe(vl, vr), _w = roe(wl, wr), _H = roe(Hl, Hr), _P = roe(pl, pr);
+    const double _rho = srl * srr;
+    double yl[NS], yr[NS], yi[NS];
+#pragma unroll
+    for (int n = 0; n < NS; n++) {
+        yl[n] = f.y[n * P + l], yr[n] = f.y[n * P + r];
+        yi[n] = roe(yl[n], yr[n]);
+    }
+    const double *xc = f.xc;
+    const double gl = xc[l], gr = xc[r];
+    const double _dpdrho = roe(xc[P + l], xc[P + r]);
+    const double el = xc[2 * P + l], er = xc[2 * P + r];
+    double dpdrhoi[NCOP > 0 ? NCOP : 1], drhoi[NCOP > 0 ? NCOP : 1];
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) {
+        dpdrhoi[n] = roe(xc[(3 + n) * P + l], xc[(3 + n) * P + r]);
+        drhoi[n] = rr * yr[n] - rl * yl[n];
+    }
+    const double Gamma0 = roe(gl, gr);
+    const double du = ur - ul, dv = vr - vl, dw = wr - wl;
+    const double _prho = roe(pl * isl * isl, pr * isr * isr) + 0.5 * D * D1 * D1 * (du * du + dv * dv + dw * dw);
+    const double _dpdE = roe(gl - 1.0, gr - 1.0);
+    const double _dpde = ((gl - 1.0) * rl + D * ((gr - 1.0) * rr)) * D1;
+    const double dp = pr - pl, drho = rr - rl, de = er - el;
+    double S1 = 0.0, S2 = 0.0, SY = 0.0;
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) {
+        const double t = dpdrhoi[n] * drhoi[n];
+        S1 += t, S2 += t * t;
+    }
+    const double temp1 = dp - ((_dpdrho * drho + _dpde * de) + S1);
+    const double den = ((_dpdrho * _dpdrho * drho * drho + _dpde * de * _dpde * de) + S2) + 1e-19;
+    const double temp = temp1 * rcp_nr(den);
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) SY += yi[n] * dpdrhoi[n];
+    const double _dpdE_new = _dpdE + _dpdE * _dpdE * de * _rho * temp;
+    const double _dpdrho_new = _dpdrho + _dpdrho * _dpdrho * drho * temp;
+    const double csqr = (_dpdrho_new + _dpdE_new * _prho) + SY;
+    const double b1 = _dpdE_new * rcp_nr(csqr);
+    const double inv_dpdE = rcp_nr(_dpdE_new);
+    double b3 = 0.0;
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) {
+        const double z = -(dpdrhoi[n] + dpdrhoi[n] * dpdrhoi[n] * drhoi[n] * temp) * inv_dpdE;
+        F.z[n] = d2f_rn(z);
+        b3 += yi[n] * z;
+    }
+    b3 *= b1;
+    const double c2w = (0.0 < csqr) ? 0.0 : 1.0;
+    const double c2 = Gamma0 * _P * _rho * c2w + (1.0 - c2w) * csqr;
+    const double q2 = _u * _u + _v * _v + _w * _w;
+    const double rc = rsqrt_nr(c2);
+    const double b2 = (1.0 + b1 * q2) - b1 * _H;
+    F._u = d2f_rn(_u), F._v = d2f_rn(_v), F._w = d2f_rn(_w), F._H = d2f_rn(_H), F._P = d2f_rn(_P);
+    F._rho = d2f_rn(_rho), F.c2 = d2f_rn(c2), F.b1 = d2f_rn(b1), F.b3 = d2f_rn(b3), F.q2 = d2f_rn(q2);
+    F._c = d2f_rn(c2 * rc), F._c1 = d2f_rn(rc), F.b2 = d2f_rn(b2);
+    F.ent0 = d2f_rn(((1.0 - b2) - b3) * (csqr * inv_dpdE));
+#pragma unroll
+    for (int n = 0; n < NS; n++) F._yi[n] = d2f_rn(yi[n]);
+}
+
 // FP32 characteristic WENO flux at face (i+1/2) of direction D (same structure as k_faces).
 template <int D, bool COP, int NS, int ORDER>
 __device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &f, const DevThermo &th, int artificial,
@@ -337,17 +439,7 @@ __device__ __forceinline__ void faces_mixed_body(const Geo &g, const DevFields &
         F._c1 = 1.0f / F._c;
         F.ent0 = (1.0f - F.b2 - F.b3) / F.b1;
     } else {
-        FaceState<NS> Fd;
-        double G0;
-        face_state<COP, NS, false>(g, f, th, idl, idr, Fd, G0);
-        F._u = (float)Fd._u, F._v = (float)Fd._v, F._w = (float)Fd._w, F._H = (float)Fd._H;
-        F._P = (float)Fd._P, F._rho = (float)Fd._rho, F.c2 = (float)Fd.c2, F.b1 = (float)Fd.b1;
-        F.b3 = (float)Fd.b3, F.q2 = (float)Fd.q2, F._c = (float)Fd._c, F.b2 = (float)Fd.b2, F._c1 = (float)Fd._c1;
-        F.ent0 = (float)Fd.ent0;
-#pragma unroll
-        for (int s = 0; s < NS; s++) F._yi[s] = (float)Fd._yi[s];
-#pragma unroll
-        for (int s = 0; s < (NS > 1 ? NS - 1 : 1); s++) F.z[s] = (float)Fd.z[s];
+        face_state_mixed<NS>(f, P, idl, idr, F);
     }
     const float un = D == 0 ? F._u : (D == 1 ? F._v : F._w);
     const float *__restrict__ Fl = f.Ff[D];

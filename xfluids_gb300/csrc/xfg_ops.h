@@ -11,6 +11,9 @@
 
 namespace xfg {
 
+// box of the fused stage's TMA copy of the state (columns, rows; all 5 components)
+constexpr int FUSED_BOX_X = 40, FUSED_BOX_Y = 13;
+
 struct LaunchCtx {
     Geo g;
     DevFields f;
@@ -23,6 +26,10 @@ struct LaunchCtx {
     int precision;                     // xfg_precision
     double cfl;                        // CFLnumber (positivity limiter)
     int viscous;                       // xfg_scheme.viscous
+    // fused mixed stage staged by TMA: host copies of the CUtensorMap of the state buffers U, U1,
+    // U2 (null when the block's row pitch does not allow a tensor map), and the SM count
+    const void *tmap[3];
+    int nsm;
 };
 
 struct Ops {

@@ -34,6 +34,10 @@ from .ensemble import Ensemble
 from .mesh import make_scheme
 
 
+# error code of a request retired because its time stopped advancing (dt = 0)
+STALLED = 30000
+
+
 @dataclass
 class Request:
     rid: int
@@ -50,6 +54,7 @@ class Request:
     steps: int = 0
     t: float = 0.0
     error: int = 0
+    t_seen: float = -1.0            # the time reported after the previous chunk
     result: np.ndarray = field(default=None, repr=False)
 
     @property
@@ -153,9 +158,13 @@ class Server:
             clock = now()
             for slot in list(running):
                 st = self.ens.status(slot)
-                if st["done"] or st["error"] or st["t"] >= running[slot].t_end:
+                # a request whose time did not move over a whole chunk (dt = 0: an infinite wave
+                # speed) would never finish: it is retired with error STALLED
+                stalled = not (st["done"] or st["error"]) and st["t"] <= running[slot].t_seen
+                running[slot].t_seen = st["t"]
+                if st["done"] or st["error"] or stalled or st["t"] >= running[slot].t_end:
                     r = running.pop(slot)
-                    r.done, r.steps, r.t, r.error = clock, st["steps"], st["t"], st["error"]
+                    r.done, r.steps, r.t, r.error = clock, st["steps"], st["t"], STALLED if stalled else st["error"]
                     if self.keep:
                         r.result = self.ens.get_state(slot)
                     self.ens.remove(slot)

@@ -44,10 +44,12 @@ def single_grid(b, s, th, U, T, steps, device=0, transport=None):
         f.initialize()
         f.time = 0.0
         st, t, k, ms = f.advance_timed(steps)
+        phases = f.time_phases()  # device ms per phase of one more step, summed over its stages
     finally:
         f.close()
     cells = b.X_inner * b.Y_inner * b.Z_inner
-    return {"status": st, "t": t, "steps": k, "ms": ms, "cells": cells, "cell_updates_per_s": cells * k / (ms * 1e-3)}
+    return {"status": st, "t": t, "steps": k, "ms": ms, "cells": cells, "cell_updates_per_s": cells * k / (ms * 1e-3),
+            "phases_ms_per_step": phases}
 
 
 def ensemble(members, steps, precision, device=0, tune=False):
