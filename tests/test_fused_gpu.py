@@ -159,8 +159,8 @@ def test_fused_launches_and_phases(cuda_lib):
 
 @pytest.mark.parametrize("name", ["vortex200x90", "riemann40_roe_inflow", "riemann48_outflow"])
 def test_tma_staged_kernel_equals_one_tile_per_cta(name, cuda_lib, monkeypatch):
-    """Blocks with an even Xmax run the persistent kernel whose state arrives by TMA copies
-    (k_fused_stage_tma); XFG_FUSED_TMA=0 at handle creation selects the one-tile-per-CTA kernel.
+    """With XFG_FUSED_TMA=1 at handle creation, blocks with an even Xmax run the persistent kernel
+    whose state arrives by TMA copies (k_fused_stage_tma) instead of the one-tile-per-CTA kernel.
     Both compute every tile with the same instructions from the same values: the states after
     free-running steps (LU included, through a stage-API step) are bitwise equal."""
     make = (lambda: _vortex(200, 90)) if name == "vortex200x90" else CASES[name]

@@ -153,12 +153,14 @@ static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // TMA maps of the fused stage's state buffers (k_fused_stage_tma): each a 3D tensor (Xmax, Ymax,
 // 5 components) of FP64 with row stride Xmax and component stride P cells, copied as boxes of
-// FUSED_BOX_X x FUSED_BOX_Y x 5. A map needs 16-byte strides, so Xmax even; an odd Xmax (or
-// XFG_FUSED_TMA=0 in the environment) keeps the one-tile-per-CTA kernel. cuTensorMapEncodeTiled is
-// taken through the runtime's driver entry point, so the library links no libcuda.
+// FUSED_BOX_X x FUSED_BOX_Y x 5. A map needs 16-byte strides, so Xmax even. The persistent TMA
+// kernel is opt-in (XFG_FUSED_TMA=1 in the environment at xfg_create): it computes the same bits as
+// the one-tile-per-CTA kernel but measured 6 % slower (its barrier waits outweigh the load latency
+// it hides). cuTensorMapEncodeTiled is taken through the runtime's driver entry point, so the
+// library links no libcuda.
 static bool make_fused_tmaps(xfg_handle *h) {
     const char *env = std::getenv("XFG_FUSED_TMA");
-    if ((env && env[0] == '0') || h->bl.Xmax % 2 || h->bl.DimZ) return false;
+    if (!(env && env[0] == '1') || h->bl.Xmax % 2 || h->bl.DimZ) return false;
     static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult q;
@@ -292,7 +294,8 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
             if (dims[d]) nf += 2 * E;                             // Ff, Fwf
     }
     const size_t stage_elems = (size_t)h->N * (E > NS ? E : NS);
-    const size_t small = 8192;                                  // small words; transport table at +4096
+    // small words; transport tables at +4096 and +6144; scaled thermo table at +8192
+    const size_t small = 8192 + align_up(THERMO_SC_DOUBLES * sizeof(double), 256);
     size_t bytes = nd * arr8 + nf * arr4 + align_up(stage_elems * 8, 256) + small;
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->pool, bytes);
@@ -356,6 +359,17 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     for (int q = 0; q < XFG_MAX_SPECIES * 6; q++) th.Hib[q] = thermal->Hib[q];
     th.nasa = scheme->thermo ? 1 : 0;
     th.ncop_gamma = scheme->ncop_gamma;
+    std::vector<double> hsc(THERMO_SC_DOUBLES);
+    if (scheme->cop) {  // the mixed form's scaled enthalpy tables
+        scaled_thermo_table(th, hsc.data());
+        double *d = (double *)(p + 8192);
+        th.hsc = d;
+        if (cudaMemcpyAsync(d, hsc.data(), THERMO_SC_DOUBLES * sizeof(double), cudaMemcpyHostToDevice, h->st) !=
+            cudaSuccess) {
+            xfg_destroy(h);
+            return fail(-2, "upload of the thermo tables failed");
+        }
+    }
     h->ctx.st = h->st;
     h->ctx.artificial = scheme->artificial_type;
     h->ctx.ghost = scheme->ghost_species;

@@ -46,7 +46,41 @@ struct DevThermo {
     double Hib[XFG_MAX_SPECIES * 6];
     int nasa;
     double ncop_gamma;
+    const double *hsc;  // mixed mixtures: device copy of scaled_thermo_table (THERMO_SC_DOUBLES)
 };
+
+// Enthalpy polynomials scaled by R_n for the mixed form, per species n and temperature range rg
+// (JANAF: rg 0 above 1000 K, 1 below; NASA-9: nasa_range), 8 coefficients at (n * 3 + rg) * 8:
+//   JANAF   h_n = T (c0 + T (c1 + T (c2 + T (c3 + T c4)))) + c5,
+//           c = R_n (a0, a1 / 2, a2 / 3, a3 / 4, a4 / 5, a5) (HeatCapacity / get_Enthalpy_JANAF);
+//   NASA-9  h_n = c0 / T + c1 ln T + T (c2 + T (c3 + T (c4 + T (c5 + T c6)))) + c7,
+//           c = R_n (-a0, a1, a2, a3 / 2, a4 / 3, a5 / 4, a6 / 5, b0);
+// then Cp_n(200 K) at THERMO_SC_CP200 + n (the tables' linear extrapolation below 200 K). The
+// same polynomials as enthalpy() / heat_capacity() with the constant factors applied once.
+constexpr int THERMO_SC_CP200 = XFG_MAX_SPECIES * 3 * 8;
+constexpr int THERMO_SC_DOUBLES = THERMO_SC_CP200 + XFG_MAX_SPECIES;
+inline void scaled_thermo_table(const DevThermo &t, double *out) {
+    for (int q = 0; q < THERMO_SC_DOUBLES; q++) out[q] = 0.0;
+    for (int n = 0; n < XFG_MAX_SPECIES; n++) {
+        const double R = t.Ri[n];
+        for (int rg = 0; rg < (t.nasa ? 3 : 2); rg++) {
+            const double *a = t.Hia + n * 21 + rg;
+            double *c = out + (n * 3 + rg) * 8;
+            if (t.nasa) {
+                c[0] = -R * a[0], c[1] = R * a[3], c[2] = R * a[6], c[3] = R * (0.5 * a[9]);
+                c[4] = R * (a[12] / 3.0), c[5] = R * (0.25 * a[15]), c[6] = R * (0.2 * a[18]), c[7] = R * t.Hib[n * 6 + rg];
+            } else {
+                c[0] = R * a[0], c[1] = R * (0.5 * a[3]), c[2] = R * (a[6] / 3.0), c[3] = R * (0.25 * a[9]);
+                c[4] = R * (0.2 * a[12]), c[5] = R * a[15];
+            }
+        }
+        const double T = 200.0;
+        const double *a = t.Hia + n * 21 + (t.nasa ? 0 : 1);  // the range holding 200 K
+        out[THERMO_SC_CP200 + n] =
+            t.nasa ? R * ((a[0] / T + a[3]) / T + a[6] + (a[9] + (a[12] + (a[15] + a[18] * T) * T) * T) * T)
+                   : R * (a[0] + (a[3] + (a[6] + (a[9] + a[12] * T) * T) * T) * T);
+    }
+}
 
 // Geometry of a block, x fastest.
 struct Geo {

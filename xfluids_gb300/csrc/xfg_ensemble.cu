@@ -187,6 +187,7 @@ struct xfg_ensemble {
     double *ddt = nullptr;                // device dtbuf of all slots (8 doubles each)
     double *hdt = nullptr;                // pinned mirror
     int *derr = nullptr;                  // device error words (8 ints each)
+    double *dhsc = nullptr;               // mixtures: the scaled enthalpy tables (DevThermo::hsc)
     int *herr = nullptr;
     std::vector<int> order;               // active slots in launch order
     int nblk[PH_N] = {0};
@@ -423,6 +424,14 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
     if (err == cudaSuccess) err = cudaEventCreate(&e->ev[1]);
     if (err == cudaSuccess) err = cudaMemsetAsync(e->ddt, 0, sizeof(double) * 8 * capacity, e->st);
     if (err == cudaSuccess) err = cudaMemsetAsync(e->derr, 0, sizeof(int) * 8 * capacity, e->st);
+    if (err == cudaSuccess && scheme->cop) {  // the mixed form's scaled enthalpy tables
+        std::vector<double> hsc(THERMO_SC_DOUBLES);
+        scaled_thermo_table(e->th, hsc.data());
+        err = cudaMalloc(&e->dhsc, sizeof(double) * THERMO_SC_DOUBLES);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(e->dhsc, hsc.data(), sizeof(double) * THERMO_SC_DOUBLES, cudaMemcpyHostToDevice, e->st);
+        e->th.hsc = e->dhsc;
+    }
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->st);
     if (err != cudaSuccess) {
         xfg_ensemble_destroy(e);
@@ -457,7 +466,7 @@ int xfg_ensemble_destroy(xfg_ensemble *e) {
     if (e->graph) cudaGraphExecDestroy(e->graph);
     for (auto &v : e->ev)
         if (v) cudaEventDestroy(v);
-    cudaFree(e->pool), cudaFree(e->dm), cudaFree(e->doff), cudaFree(e->ddt), cudaFree(e->derr);
+    cudaFree(e->pool), cudaFree(e->dm), cudaFree(e->doff), cudaFree(e->ddt), cudaFree(e->derr), cudaFree(e->dhsc);
     if (e->hdt) cudaFreeHost(e->hdt);
     if (e->herr) cudaFreeHost(e->herr);
     if (e->st) cudaStreamDestroy(e->st);

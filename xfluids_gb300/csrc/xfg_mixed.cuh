@@ -31,51 +31,71 @@ __device__ __forceinline__ float d2f_rn(double x) {
 // Mixture thermodynamics of the mixed form with the species folded into one polynomial.
 // h(T) = sum_n y_n h_n(T) and Cp(T) = sum_n y_n Cp_n(T) are linear in the species, and the
 // temperature ranges of both tables do not depend on the species (JANAF breaks at 1000 K, NASA-9
-// at 1000 / 6000 K), so within a range the mixture has coefficients
-// A_c = sum_n y_n R_n a_{n,c} (and the enthalpy constant B = sum_n y_n R_n b_n), folded once per
-// cell and range: each Newton iteration is one polynomial (and one log for NASA-9) instead of NS.
-// Below 200 K (the tables' linear extrapolation) the per-species functions are used. Same
-// mathematics as the reference's sums, different rounding: the mixed form only.
+// at 1000 / 6000 K), so within a range the mixture enthalpy has the coefficients
+// H_c = sum_n y_n c_{n,c} of the R_n-scaled species tables (DevThermo::hsc) and Cp = dh/dT those
+// times their powers; folded once per cell and range: each Newton iteration is one polynomial (and
+// one log for NASA-9) instead of NS. Below 200 K (the tables' linear extrapolation) the
+// per-species functions are used. Same mathematics as the reference's sums, different rounding:
+// the mixed form only.
+__device__ __forceinline__ int thermo_range(bool nasa, double T) { return nasa ? nasa_range(T) : (T > 1000.0 ? 0 : 1); }
+
 template <int NS>
 struct FoldedThermo {
-    double A[7], Hs[7], B;  // Cp coefficients; enthalpy coefficients A_c / (power of T they multiply)
+    double H[8], A[7];  // enthalpy coefficients (layout of DevThermo::hsc); Cp coefficients
     int rg = -9;
     __device__ __forceinline__ bool fold(const DevThermo &t, const double *yi, double T) {
-        const int r = t.nasa ? nasa_range(T) : (T > 1000.0 ? 0 : 1);
+        const int r = thermo_range(t.nasa, T);
         if (r < 0) return false;
         if (r == rg) return true;
         rg = r;
+        const int nc = t.nasa ? 8 : 6;
 #pragma unroll
-        for (int c = 0; c < 7; c++) A[c] = 0.0;
-        B = 0.0;
+        for (int c = 0; c < 8; c++) H[c] = 0.0;
 #pragma unroll
         for (int n = 0; n < NS; n++) {
-            const double w = yi[n] * t.Ri[n];
-            const double *a = t.Hia + n * 21 + r;
+            const double *c = t.hsc + (n * 3 + r) * 8;
 #pragma unroll
-            for (int c = 0; c < 7; c++) A[c] = fma(w, a[3 * c], A[c]);
-            B = fma(w, t.nasa ? t.Hib[n * 6 + r] : a[15], B);
+            for (int q = 0; q < 8; q++)
+                if (q < nc) H[q] = fma(yi[n], c[q], H[q]);
         }
-        if (t.nasa) {
-            Hs[0] = A[0], Hs[1] = A[1], Hs[2] = A[2], Hs[3] = A[3] * 0.5, Hs[4] = A[4] * kOT;
-            Hs[5] = A[5] * 0.25, Hs[6] = A[6] * 0.2;
-        } else {
-            Hs[0] = A[0], Hs[1] = A[1] * 0.5, Hs[2] = A[2] * kOT, Hs[3] = A[3] * 0.25, Hs[4] = A[4] * 0.2;
+        if (t.nasa) {  // Cp = -H0 / T^2 + H1 / T + H2 + 2 H3 T + 3 H4 T^2 + 4 H5 T^3 + 5 H6 T^4
+            A[0] = -H[0], A[1] = H[1], A[2] = H[2], A[3] = 2.0 * H[3], A[4] = 3.0 * H[4], A[5] = 4.0 * H[5];
+            A[6] = 5.0 * H[6];
+        } else {       // Cp = H0 + 2 H1 T + 3 H2 T^2 + 4 H3 T^3 + 5 H4 T^4
+            A[0] = H[0], A[1] = 2.0 * H[1], A[2] = 3.0 * H[2], A[3] = 4.0 * H[3], A[4] = 5.0 * H[4];
         }
         return true;
     }
     // h and Cp of the mixture at T >= 200 K within the folded range
     __device__ __forceinline__ void eval(bool nasa, double T, double &h, double &Cp) const {
         if (nasa) {
-            const double iT = 1.0 / T;
+            const double iT = rcp_nr(T);
             Cp = fma(fma(A[0], iT, A[1]), iT, fma(fma(fma(fma(A[6], T, A[5]), T, A[4]), T, A[3]), T, A[2]));
-            h = fma(-Hs[0], iT, fma(Hs[1], log(T), fma(fma(fma(fma(fma(Hs[6], T, Hs[5]), T, Hs[4]), T, Hs[3]), T, Hs[2]), T, B)));
+            h = fma(H[0], iT, fma(H[1], log(T), fma(fma(fma(fma(fma(H[6], T, H[5]), T, H[4]), T, H[3]), T, H[2]), T, H[7])));
         } else {
             Cp = fma(fma(fma(fma(A[4], T, A[3]), T, A[2]), T, A[1]), T, A[0]);
-            h = fma(fma(fma(fma(fma(Hs[4], T, Hs[3]), T, Hs[2]), T, Hs[1]), T, Hs[0]), T, B);
+            h = fma(fma(fma(fma(fma(H[4], T, H[3]), T, H[2]), T, H[1]), T, H[0]), T, H[5]);
         }
     }
 };
+
+// The species enthalpies h_n(T) of the mixed form from the scaled tables: one range test, one log
+// and one reciprocal (NASA-9) for all species, the extrapolation below 200 K as one FMA.
+template <int NS>
+__device__ __forceinline__ void species_enthalpies_mixed(const DevThermo &t, double T0, double *h) {
+    const double T = fmax(T0, 200.0), dT = fmin(T0 - 200.0, 0.0);
+    const bool nasa = t.nasa;
+    int rg = thermo_range(nasa, T);
+    rg = rg < 0 ? 0 : rg;
+    const double lT = nasa ? log(T) : 0.0, iT = nasa ? rcp_nr(T) : 0.0;
+#pragma unroll
+    for (int n = 0; n < NS; n++) {
+        const double *c = t.hsc + (n * 3 + rg) * 8;
+        const double hp = nasa ? fma(c[0], iT, fma(c[1], lT, fma(fma(fma(fma(fma(c[6], T, c[5]), T, c[4]), T, c[3]), T, c[2]), T, c[7])))
+                               : fma(fma(fma(fma(fma(c[4], T, c[3]), T, c[2]), T, c[1]), T, c[0]), T, c[5]);
+        h[n] = fma(t.hsc[THERMO_SC_CP200 + n], dT, hp);
+    }
+}
 
 // cop_cell_terms for the mixed form (the same terms, no reference rounding to keep): gamma and 1/rho
 // from the caller, one reciprocal of the mixture R instead of a division per term.
@@ -85,8 +105,7 @@ __device__ __forceinline__ void cop_cell_terms_mixed(const DevThermo &th, double
                                                      double *xc, long long P, long long id) {
     constexpr int NCOP = NS - 1;
     double h[NS];
-#pragma unroll
-    for (int n = 0; n < NS; n++) h[n] = enthalpy(th, T, n);
+    species_enthalpies_mixed<NS>(th, T, h);
     const double q2 = u * u + v * v + w * w;
     const double CpT_R = Cp * T * rcp_nr(wi * kRu);
     const double RN = th.Ri[NCOP];

@@ -115,10 +115,10 @@ class Server:
     def close(self):
         self.ens.close()
 
-    def run(self, trace=None, realtime=True, max_chunks=None):
+    def run(self, trace=None, realtime=True, max_chunks=None, progress=None):
         """Serve the submitted requests (and `trace`, Requests sorted by arrival) until all are
         done, or for at most `max_chunks` chunks. realtime=False replays the arrivals in order
-        without waiting for the wall clock (tests)."""
+        without waiting for the wall clock (tests). progress(server) is called after each chunk."""
         if trace is not None:
             self.pending.extend(trace)
         pending, waiting, running = self.pending, self.waiting, self.running
@@ -168,6 +168,8 @@ class Server:
                     if self.keep:
                         r.result = self.ens.get_state(slot)
                     self.ens.remove(slot)
+            if progress is not None:
+                progress(self)
         self.elapsed0 = now()
         return trace
 
