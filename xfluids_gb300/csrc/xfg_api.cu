@@ -282,13 +282,13 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     if (scheme->viscous && !mixed) nd += 9 + 2;                 // velocity derivatives, mu, kappa
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;  // single-gas fast path extras
     if (fast1) nd += 2 + 3 * (block->DimX + block->DimY + block->DimZ);
-    const bool mixcop = scheme->cop && mixed;                    // mixed mixtures: sqrt(rho), 1/sqrt(rho)
-    if (mixcop) nd += 2;
+    const bool mixcop = scheme->cop && mixed;
     for (int d = 0; d < 3; d++)
         if (dims[d] && !mixed) nd += 2 * E;                       // F, Fw
     size_t nf = 0;
     if (mixed) {
         nf = E + 7;
+        if (mixcop) nf += NS + 3 + (NS - 1);                     // FP32 y and sound-speed terms
         if (scheme->viscous) nf += 9 + 2 + 1;                    // FP32 derivatives, mu, kappa, T
         for (int d = 0; d < 3; d++)
             if (dims[d]) nf += 2 * E;                             // Ff, Fwf
@@ -317,7 +317,6 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
     if (scheme->cop) f.y = take8(NS), f.xc = take8(3 + (NS - 1));
     if (scheme->viscous && !mixed) f.vde = take8(9), f.mu = take8(1), f.kappa = take8(1);
-    if (mixcop) f.sr = take8(1), f.isr = take8(1);
     if (fast1) {
         f.sr = take8(1), f.isr = take8(1);
         for (int d = 0; d < 3; d++)
@@ -328,6 +327,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     if (mixed) {
         f.Uf = take4(E);
         f.primf = take4(7);
+        if (mixcop) f.yf = take4(NS), f.xcf = take4(3 + (NS - 1));
         if (scheme->viscous) f.vdef = take4(9), f.muf = take4(1), f.kappaf = take4(1), f.Tf = take4(1);
         for (int d = 0; d < 3; d++)
             if (dims[d]) f.Ff[d] = take4(E), f.Fwf[d] = take4(E);

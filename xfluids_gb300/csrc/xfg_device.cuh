@@ -119,6 +119,7 @@ struct DevFields {
     float *primf;              // FP32 rho, u, v, w, H, p, c (7 components, mixed form)
     float *Fwf[3];             // FP32 face fluxes (mixed form)
     double *sr, *isr;          // sqrt(rho) and 1/sqrt(rho) per cell (single-gas FP64 fast path)
+    float *yf, *xcf;           // mixed mixtures: FP32 copies of y (NS) and of xc (3 + NCOP)
     double *eab[3];            // |u_d - c|, |u_d|, |u_d + c| per cell and direction (same path)
     double *vde;               // viscous: the 9 cell-centre velocity derivatives (ducx..dwcz)
     double *mu, *kappa;        // viscous: mixture viscosity and thermal conductivity per cell
@@ -509,8 +510,18 @@ __device__ __forceinline__ T wenocu6(const T *pp, const T *mm, T dl) {
     return (temf + temm) * T(kSix);
 }
 
+// Hardware FP32 reciprocal approximation (rcp.approx.ftz.f32, about 1 ulp) for the nonlinear
+// weights of the FP32 WENO forms, where it replaces IEEE divisions.
+__device__ __forceinline__ float rcp_approx_f(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // FP32 form: the same candidates and smoothness indicators; the weights use the division form
-// d_k / s_k^2 (equal to the product form) so that s^4 cannot overflow single precision.
+// d_k / s_k^2 (equal to the product form) so that s^4 cannot overflow single precision, scaled by
+// the smallest s: d_k (s_min / s_k)^2 lies in [0, d_k] whatever the scale of the data, and the
+// reciprocals are the hardware approximation.
 __device__ __forceinline__ float weno5_body(float v1, float v2, float v3, float v4, float v5) {
     float a1;
     a1 = v1 - 2.0f * v2 + v3;
@@ -526,8 +537,10 @@ __device__ __forceinline__ float weno5_body(float v1, float v2, float v3, float 
     a1 = 3.0f * v3 - 4.0f * v4 + v5;
     s3 += 3.0f * a1 * a1;
     s1 += 1.0E-6f, s2 += 1.0E-6f, s3 += 1.0E-6f;
-    float w1 = 0.1f / (s1 * s1), w2 = 0.6f / (s2 * s2), w3 = 0.3f / (s3 * s3);
-    float tw = 1.0f / (w1 + w2 + w3);
+    const float sm = fminf(s1, fminf(s2, s3));
+    const float r1 = sm * rcp_approx_f(s1), r2 = sm * rcp_approx_f(s2), r3 = sm * rcp_approx_f(s3);
+    const float w1 = 0.1f * r1 * r1, w2 = 0.6f * r2 * r2, w3 = 0.3f * r3 * r3;
+    const float tw = rcp_approx_f(w1 + w2 + w3);
     return tw * (w1 * (2.0f * v1 - 7.0f * v2 + 11.0f * v3) + w2 * (-v2 + 5.0f * v3 + 2.0f * v4) +
                  w3 * (2.0f * v3 + 5.0f * v4 - v5));
 }
@@ -572,8 +585,44 @@ __device__ __forceinline__ T weno7_body(T v1, T v2, T v3, T v4, T v5, T v6, T v7
     T q3 = T(3.0 / 12.0) * v4 + T(13.0 / 12.0) * v5 - T(5.0 / 12.0) * v6 + T(1.0 / 12.0) * v7;
     return W0 * q0 + W1 * q1 + W2 * q2 + W3 * q3;
 }
+// FP32 form of weno7_body: the same indicators and candidates; the weights C_k / (eps + S_k)^2
+// scaled by the smallest (eps + S_k), as in the FP32 WENO5, with hardware reciprocals.
+__device__ __forceinline__ float weno7_body_f(float v1, float v2, float v3, float v4, float v5, float v6, float v7) {
+    const float ep = 1.0e-7f;
+    const float S10 = (-2.0f / 6.0f) * v1 + (9.0f / 6.0f) * v2 - (18.0f / 6.0f) * v3 + (11.0f / 6.0f) * v4;
+    const float S11 = (1.0f / 6.0f) * v2 - v3 + (3.0f / 6.0f) * v4 + (2.0f / 6.0f) * v5;
+    const float S12 = (-2.0f / 6.0f) * v3 - (3.0f / 6.0f) * v4 + v5 - (1.0f / 6.0f) * v6;
+    const float S13 = (-11.0f / 6.0f) * v4 + (18.0f / 6.0f) * v5 - (9.0f / 6.0f) * v6 + (2.0f / 6.0f) * v7;
+    const float S20 = -v1 + 4.0f * v2 - 5.0f * v3 + 2.0f * v4;
+    const float S21 = v3 - 2.0f * v4 + v5;
+    const float S22 = v4 - 2.0f * v5 + v6;
+    const float S23 = 2.0f * v4 - 5.0f * v5 + 4.0f * v6 - v7;
+    const float S30 = -v1 + 3.0f * v2 - 3.0f * v3 + v4;
+    const float S31 = -v2 + 3.0f * v3 - 3.0f * v4 + v5;
+    const float S32 = -v3 + 3.0f * v4 - 3.0f * v5 + v6;
+    const float S33 = -v4 + 3.0f * v5 - 3.0f * v6 + v7;
+    const float k13 = 13.0f / 12.0f, k1043 = 1043.0f / 960.0f, k112 = 1.0f / 12.0f;
+    const float e0 = ep + (S10 * S10 + k13 * S20 * S20 + k1043 * S30 * S30 + k112 * S10 * S30);
+    const float e1 = ep + (S11 * S11 + k13 * S21 * S21 + k1043 * S31 * S31 + k112 * S11 * S31);
+    const float e2 = ep + (S12 * S12 + k13 * S22 * S22 + k1043 * S32 * S32 + k112 * S12 * S32);
+    const float e3 = ep + (S13 * S13 + k13 * S23 * S23 + k1043 * S33 * S33 + k112 * S13 * S33);
+    const float em = fminf(fminf(e0, e1), fminf(e2, e3));
+    const float r0 = em * rcp_approx_f(e0), r1 = em * rcp_approx_f(e1);
+    const float r2 = em * rcp_approx_f(e2), r3 = em * rcp_approx_f(e3);
+    const float a0 = (1.0f / 35.0f) * r0 * r0, a1 = (12.0f / 35.0f) * r1 * r1;
+    const float a2 = (18.0f / 35.0f) * r2 * r2, a3 = (4.0f / 35.0f) * r3 * r3;
+    const float isum = 1.0f / (a0 + a1 + a2 + a3);
+    const float q0 = (-3.0f / 12.0f) * v1 + (13.0f / 12.0f) * v2 - (23.0f / 12.0f) * v3 + (25.0f / 12.0f) * v4;
+    const float q1 = (1.0f / 12.0f) * v2 - (5.0f / 12.0f) * v3 + (13.0f / 12.0f) * v4 + (3.0f / 12.0f) * v5;
+    const float q2 = (-1.0f / 12.0f) * v3 + (7.0f / 12.0f) * v4 + (7.0f / 12.0f) * v5 - (1.0f / 12.0f) * v6;
+    const float q3 = (3.0f / 12.0f) * v4 + (13.0f / 12.0f) * v5 - (5.0f / 12.0f) * v6 + (1.0f / 12.0f) * v7;
+    return (a0 * q0 + a1 * q1 + a2 * q2 + a3 * q3) * isum;
+}
 template <class T>
 __device__ __forceinline__ T weno7(const T *pp, const T *mm) {
+    if constexpr (sizeof(T) == 4)
+        return weno7_body_f(pp[0], pp[1], pp[2], pp[3], pp[4], pp[5], pp[6]) +
+               weno7_body_f(mm[7], mm[6], mm[5], mm[4], mm[3], mm[2], mm[1]);
     T tp = weno7_body(pp[0], pp[1], pp[2], pp[3], pp[4], pp[5], pp[6]);
     T tm = weno7_body(mm[7], mm[6], mm[5], mm[4], mm[3], mm[2], mm[1]);
     return tp + tm;

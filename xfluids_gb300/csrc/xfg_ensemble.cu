@@ -220,10 +220,9 @@ size_t member_bytes(const xfg_block &b, int cop, int ns, bool mixed) {
     size_t nd = 3 * E + 12;                                    // U, U1, LU, primitives
     if (cop) nd += ns + 3 + (ns - 1);                          // y, per-cell sound-speed terms
     if (mixed && !cop && two_d(b)) nd += 5;                    // U2 of the fused stages
-    if (mixed && cop) nd += 2;                                 // sqrt(rho), 1/sqrt(rho) of the mixed faces
     if (!mixed) nd += 2 * E * dims + (cop ? 0 : 2 + 3 * dims); // F, Fw; single gas: sqrt(rho), 1/sqrt(rho), |lambda|
     size_t bytes = nd * P * 8;
-    if (mixed) bytes += (size_t)(E + 7 + 2 * E * dims) * up(P * 4, 256);
+    if (mixed) bytes += (size_t)(E + 7 + 2 * E * dims + (cop ? ns + 3 + (ns - 1) : 0)) * up(P * 4, 256);
     return bytes + 1024;                                       // lam + small words
 }
 
@@ -249,8 +248,8 @@ void carve(Member &m, char *base, const xfg_block &b, int cop, int ns, bool mixe
                 if (dims[d]) f.eab[d] = t8(3);
         }
     } else {
-        if (cop) f.sr = t8(1), f.isr = t8(1);
         f.Uf = t4(E), f.primf = t4(7);
+        if (cop) f.yf = t4(ns), f.xcf = t4(3 + (ns - 1));
         for (int d = 0; d < 3; d++)
             if (dims[d]) f.Ff[d] = t4(E), f.Fwf[d] = t4(E);
     }

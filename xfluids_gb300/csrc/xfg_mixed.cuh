@@ -97,42 +97,53 @@ __device__ __forceinline__ void species_enthalpies_mixed(const DevThermo &t, dou
     }
 }
 
-// cop_cell_terms for the mixed form (the same terms, no reference rounding to keep): gamma and 1/rho
-// from the caller, one reciprocal of the mixture R instead of a division per term.
+// cop_cell_terms for the mixed form (the same terms, no reference rounding to keep): gamma from
+// the caller, one reciprocal of the mixture R instead of a division per term, e = E / rho - |u|^2 / 2
+// (the caller's internal energy, equal to H - |u|^2 / 2 - p / rho); each term also as FP32 (xcf) for
+// the FP32 Roe averages of face_state_mixed.
 template <int NS>
 __device__ __forceinline__ void cop_cell_terms_mixed(const DevThermo &th, double T, double Cp, double gm, double wi,
-                                                     double u, double v, double w, double H, double p, double rho1,
-                                                     double *xc, long long P, long long id) {
+                                                     double u, double v, double w, double e, double *xc,
+                                                     float *xcf, long long P, long long id) {
     constexpr int NCOP = NS - 1;
     double h[NS];
     species_enthalpies_mixed<NS>(th, T, h);
     const double q2 = u * u + v * v + w * w;
-    const double CpT_R = Cp * T * rcp_nr(wi * kRu);
+    const double CpT_R = Cp * T * rcp_nr(wi * kRu);  // Cp T / R
     const double RN = th.Ri[NCOP];
     const double g1 = gm - 1.0;
-    xc[id] = gm;
-    xc[P + id] = g1 * (0.5 * q2 - h[NCOP] + RN * CpT_R);
-    xc[2 * P + id] = H - 0.5 * q2 - p * rho1;
+    double t[3 + (NCOP > 0 ? NCOP : 1)];
+    t[0] = gm;
+    t[1] = g1 * (0.5 * q2 - h[NCOP] + RN * CpT_R);
+    t[2] = e;
 #pragma unroll
-    for (int n = 0; n < NCOP; n++) xc[(3 + n) * P + id] = g1 * ((h[NCOP] - h[n]) + (th.Ri[n] - RN) * CpT_R);
+    for (int n = 0; n < NCOP; n++) t[3 + n] = g1 * ((h[NCOP] - h[n]) + (th.Ri[n] - RN) * CpT_R);
+#pragma unroll
+    for (int q = 0; q < 3 + NCOP; q++) xc[q * P + id] = t[q], xcf[q * P + id] = d2f_rn(t[q]);
 }
 
 // get_T (Mixing_device.h:171-193): the same clamped Newton iteration and stopping test on the
 // folded mixture polynomials, the step f / f' with the refined reciprocal of f'; returns T and the
 // mixture Cp at T.
+// h and Cp of the mixture by the per-species functions (below 200 K, or a temperature outside the
+// tables): a called function, so that the rare path costs the iteration nothing when not taken
 template <int NS>
-__device__ double newton_T_folded(const DevThermo &t, const double *yi, double e, double T0, double &Cp_out) {
+__device__ __noinline__ void mix_h_cp_species(const DevThermo &t, const double *yi, double T, double &h, double &Cp) {
+    h = mix_h<NS>(t, yi, T);
+    Cp = mix_Cp<NS>(t, yi, T);
+}
+
+template <int NS>
+__device__ __forceinline__ double newton_T_folded(const DevThermo &t, const double *yi, double Rm, double e,
+                                                  double T0, double &Cp_out) {
     FoldedThermo<NS> ft;
     double T = T0;
-    const double Rm = mix_R<NS>(t, yi);
     for (int it = 1; it < 101; it++) {
         double h, Cp;
-        if (T >= 200.0 && ft.fold(t, yi, T)) {
+        if (T >= 200.0 && ft.fold(t, yi, T))
             ft.eval(t.nasa, T, h, Cp);
-        } else {
-            h = mix_h<NS>(t, yi, T);
-            Cp = mix_Cp<NS>(t, yi, T);
-        }
+        else
+            mix_h_cp_species<NS>(t, yi, T, h, Cp);
         double f = h - Rm * T - e;
         double df_ = Cp - Rm;
         double df = fmin(f * rcp_nr(df_ + 1.0e-30), 1e-3 * T);
@@ -142,14 +153,14 @@ __device__ double newton_T_folded(const DevThermo &t, const double *yi, double e
     }
     double h;
     if (T >= 200.0 && ft.fold(t, yi, T)) ft.eval(t.nasa, T, h, Cp_out);
-    else Cp_out = mix_Cp<NS>(t, yi, T);
+    else mix_h_cp_species<NS>(t, yi, T, h, Cp_out);
     return T;
 }
 
 // Primitive recovery of the mixed form. Single gas: from the FP64 state converted once to FP32.
 // Mixture: the FP64 recovery of k_states (Newton in FP64, refined reciprocals instead of
-// divisions), sqrt(rho) and 1 / sqrt(rho) for the faces' Roe weights, the FP32 copies converted by
-// integer operations, the sound speed in FP32.
+// divisions) and the FP64 cell terms of the sound speed, their FP32 copies (and those of y) for the
+// faces' FP32 Roe averages, converted by integer operations; the sound speed in FP32.
 template <bool COP, int NS>
 __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields &f, const DevThermo &th,
                                                   double *__restrict__ UI, int ghost, int want_lam, long long id,
@@ -198,23 +209,19 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             }
             const double ud = U[1] * rho1, vd = U[2] * rho1, wd = U[3] * rho1;
             const double tme = U[4] * rho1 - 0.5 * (ud * ud + vd * vd + wd * wd);
-            const double Rm = mix_R<NS>(th, yi);
+            const double wi = mix_W_inv<NS>(th, yi), Rm = wi * kRu;  // sum y_n / W_n; the mixture R
             double Cp;
-            const double T = newton_T_folded<NS>(th, yi, tme, f.T[id], Cp);
+            const double T = newton_T_folded<NS>(th, yi, Rm, tme, f.T[id], Cp);
             const double pd = rhod * Rm * T;
-            const double wi = mix_W_inv<NS>(th, yi);
-            const double gmx = Cp * rcp_nr(Cp - kRu * wi);
+            const double gmx = Cp * rcp_nr(Cp - Rm);
             const double gamma = gmx > 1.0 ? gmx : -1.0;
             const double Hd = (U[4] + pd) * rho1;
-            // sqrt(rho) and 1 / sqrt(rho) for the Roe weights of the mixed faces (face_state_mixed)
-            const double isr = rsqrt_nr(rhod);
-            f.sr[id] = rhod * isr, f.isr[id] = isr;
             f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd;
             f.e[id] = tme, f.gamma[id] = gamma, f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
             if (f.Tf) f.Tf[id] = d2f_rn(T);  // viscous schemes: the heat flux's FP32 temperature
-            if (f.xc) cop_cell_terms_mixed<NS>(th, T, Cp, gmx, wi, ud, vd, wd, Hd, pd, rho1, f.xc, P, id);
+            cop_cell_terms_mixed<NS>(th, T, Cp, gmx, wi, ud, vd, wd, tme, f.xc, f.xcf, P, id);
 #pragma unroll
-            for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = d2f_rn(yi[s]);
+            for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = d2f_rn(yi[s]), f.yf[s * P + id] = yf[s];
 #pragma unroll
             for (int n = 0; n < E; n++) Uf[n] = d2f_rn(U[n]);
             rho = d2f_rn(rhod), u = d2f_rn(ud), v = d2f_rn(vd), w = d2f_rn(wd), p = d2f_rn(pd), H = d2f_rn(Hd);
@@ -347,81 +354,80 @@ __device__ __forceinline__ float project_r(const float *lrow, int n, const float
 
 // Roe state of a mixture face for the mixed form: the quantities of face_state's mixture branch
 // (MARCO_ROE, Eigen_callback.h:87-91 and Utils_device.hpp:42-140: Roe averages, the pressure-
-// derivative corrections of the multi-component sound speed, the MARCO_PREEIGEN terms), in FP64
-// with the per-cell sqrt(rho) and 1 / sqrt(rho) of k_states_mixed (D = sqrt(rho_r / rho_l) and
-// sqrt(rho_l rho_r) without a square root, p / rho = p (1 / sqrt(rho))^2), the refined reciprocals
-// of rcp_nr for the five divisions and rsqrt_nr for c and 1 / c; the results rounded to FP32 by
-// integer operations. The same mathematics as face_state, another FP64 rounding.
+// derivative correction of the multi-component sound speed, the MARCO_PREEIGEN terms) in FP32,
+// except the jumps across the face. The correction temp = (dp - dp/drho drho - dp/de de -
+// sum dp/drho_n drho_n) / den is a second-order residual of first-order jumps: from jumps of
+// FP32-rounded states its rounding would be eps / |jump| relative, while jumps taken in FP64 and
+// then rounded leave it, and the sound speed it corrects, at FP32 rounding (eps) like the other
+// averages. So the jumps of rho, p, e, u, v, w and rho_n come from the FP64 states (11 FP64
+// operations a face), everything else from the FP32 copies of k_states_mixed.
 template <int NS>
 __device__ __forceinline__ void face_state_mixed(const DevFields &f, long long P, long long l, long long r,
                                                  FaceStateT<float, NS> &F) {
     constexpr int NCOP = NS - 1;
-    const double srl = f.sr[l], srr = f.sr[r], isl = f.isr[l], isr = f.isr[r];
-    const double rl = f.rho[l], rr = f.rho[r];
-    const double ul = f.u[l], ur = f.u[r], vl = f.v[l], vr = f.v[r], wl = f.w[l], wr = f.w[r];
-    const double Hl = f.H[l], Hr = f.H[r], pl = f.p[l], pr = f.p[r];
-    const double D = srr * isl;                 // sqrt(rho_r / rho_l)
-    const double D1 = srl * rcp_nr(srl + srr);  // 1 / (D + 1)
-    auto roe = [&](double a, double b) { return fma(D, b, a) * D1; };  // (a + D b) / (1 + D)
-    const double _u = roe(ul, ur), _v = roe(vl, vr), _w = roe(wl, wr), _H = roe(Hl, Hr), _P = roe(pl, pr);
-    const double _rho = srl * srr;
-    double yl[NS], yr[NS], yi[NS];
+    const float *pf = f.primf, *yf = f.yf, *xf = f.xcf;
+    const float rl = pf[l], rr = pf[r];
+    const float D = sqrtf(rr / rl);
+    const float D1 = 1.0f / (D + 1.0f);
+    auto roe = [&](float a, float b) { return fmaf(D, b, a) * D1; };  // (a + D b) / (1 + D)
+    const float _u = roe(pf[P + l], pf[P + r]), _v = roe(pf[2 * P + l], pf[2 * P + r]);
+    const float _w = roe(pf[3 * P + l], pf[3 * P + r]), _H = roe(pf[4 * P + l], pf[4 * P + r]);
+    const float pl = pf[5 * P + l], pr = pf[5 * P + r], _P = roe(pl, pr);
+    const float _rho = sqrtf(rr * rl);
+    float yi[NS];
 #pragma unroll
-    for (int n = 0; n < NS; n++) {
-        yl[n] = f.y[n * P + l], yr[n] = f.y[n * P + r];
-        yi[n] = roe(yl[n], yr[n]);
-    }
-    const double *xc = f.xc;
-    const double gl = xc[l], gr = xc[r];
-    const double _dpdrho = roe(xc[P + l], xc[P + r]);
-    const double el = xc[2 * P + l], er = xc[2 * P + r];
-    double dpdrhoi[NCOP > 0 ? NCOP : 1], drhoi[NCOP > 0 ? NCOP : 1];
-#pragma unroll
-    for (int n = 0; n < NCOP; n++) {
-        dpdrhoi[n] = roe(xc[(3 + n) * P + l], xc[(3 + n) * P + r]);
-        drhoi[n] = rr * yr[n] - rl * yl[n];
-    }
-    const double Gamma0 = roe(gl, gr);
-    const double du = ur - ul, dv = vr - vl, dw = wr - wl;
-    const double _prho = roe(pl * isl * isl, pr * isr * isr) + 0.5 * D * D1 * D1 * (du * du + dv * dv + dw * dw);
-    const double _dpdE = roe(gl - 1.0, gr - 1.0);
-    const double _dpde = ((gl - 1.0) * rl + D * ((gr - 1.0) * rr)) * D1;
-    const double dp = pr - pl, drho = rr - rl, de = er - el;
-    double S1 = 0.0, S2 = 0.0, SY = 0.0;
+    for (int n = 0; n < NS; n++) yi[n] = roe(yf[n * P + l], yf[n * P + r]);
+    const float gl = xf[l], gr = xf[r];
+    const float _dpdrho = roe(xf[P + l], xf[P + r]);
+    float dpdrhoi[NCOP > 0 ? NCOP : 1], drhoi[NCOP > 0 ? NCOP : 1];
+    // the jumps, from the FP64 states
+    const double rl64 = f.rho[l], rr64 = f.rho[r];
+    const float drho = d2f_rn(rr64 - rl64), dp = d2f_rn(f.p[r] - f.p[l]);
+    const float de = d2f_rn(f.xc[2 * P + r] - f.xc[2 * P + l]);
+    const float du = d2f_rn(f.u[r] - f.u[l]), dv = d2f_rn(f.v[r] - f.v[l]), dw = d2f_rn(f.w[r] - f.w[l]);
 #pragma unroll
     for (int n = 0; n < NCOP; n++) {
-        const double t = dpdrhoi[n] * drhoi[n];
+        dpdrhoi[n] = roe(xf[(3 + n) * P + l], xf[(3 + n) * P + r]);
+        drhoi[n] = d2f_rn(fma(rr64, f.y[n * P + r], -(rl64 * f.y[n * P + l])));
+    }
+    const float Gamma0 = roe(gl, gr);
+    const float _prho = roe(pl / rl, pr / rr) + 0.5f * D * D1 * D1 * (du * du + dv * dv + dw * dw);
+    const float _dpdE = roe(gl - 1.0f, gr - 1.0f);
+    const float _dpde = ((gl - 1.0f) * rl + D * ((gr - 1.0f) * rr)) * D1;
+    float S1 = 0.0f, S2 = 0.0f, SY = 0.0f;
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) {
+        const float t = dpdrhoi[n] * drhoi[n];
         S1 += t, S2 += t * t;
     }
-    const double temp1 = dp - ((_dpdrho * drho + _dpde * de) + S1);
-    const double den = ((_dpdrho * _dpdrho * drho * drho + _dpde * de * _dpde * de) + S2) + 1e-19;
-    const double temp = temp1 * rcp_nr(den);
+    const float temp1 = dp - ((_dpdrho * drho + _dpde * de) + S1);
+    const float den = ((_dpdrho * _dpdrho * drho * drho + _dpde * de * _dpde * de) + S2) + 1e-19f;
+    const float temp = temp1 / den;
 #pragma unroll
     for (int n = 0; n < NCOP; n++) SY += yi[n] * dpdrhoi[n];
-    const double _dpdE_new = _dpdE + _dpdE * _dpdE * de * _rho * temp;
-    const double _dpdrho_new = _dpdrho + _dpdrho * _dpdrho * drho * temp;
-    const double csqr = (_dpdrho_new + _dpdE_new * _prho) + SY;
-    const double b1 = _dpdE_new * rcp_nr(csqr);
-    const double inv_dpdE = rcp_nr(_dpdE_new);
-    double b3 = 0.0;
+    const float _dpdE_new = _dpdE + _dpdE * _dpdE * de * _rho * temp;
+    const float _dpdrho_new = _dpdrho + _dpdrho * _dpdrho * drho * temp;
+    const float csqr = (_dpdrho_new + _dpdE_new * _prho) + SY;
+    const float b1 = _dpdE_new / csqr;
+    const float inv_dpdE = 1.0f / _dpdE_new;
+    float b3 = 0.0f;
 #pragma unroll
     for (int n = 0; n < NCOP; n++) {
-        const double z = -(dpdrhoi[n] + dpdrhoi[n] * dpdrhoi[n] * drhoi[n] * temp) * inv_dpdE;
-        F.z[n] = d2f_rn(z);
+        const float z = -(dpdrhoi[n] + dpdrhoi[n] * dpdrhoi[n] * drhoi[n] * temp) * inv_dpdE;
+        F.z[n] = z;
         b3 += yi[n] * z;
     }
     b3 *= b1;
-    const double c2w = (0.0 < csqr) ? 0.0 : 1.0;
-    const double c2 = Gamma0 * _P * _rho * c2w + (1.0 - c2w) * csqr;
-    const double q2 = _u * _u + _v * _v + _w * _w;
-    const double rc = rsqrt_nr(c2);
-    const double b2 = (1.0 + b1 * q2) - b1 * _H;
-    F._u = d2f_rn(_u), F._v = d2f_rn(_v), F._w = d2f_rn(_w), F._H = d2f_rn(_H), F._P = d2f_rn(_P);
-    F._rho = d2f_rn(_rho), F.c2 = d2f_rn(c2), F.b1 = d2f_rn(b1), F.b3 = d2f_rn(b3), F.q2 = d2f_rn(q2);
-    F._c = d2f_rn(c2 * rc), F._c1 = d2f_rn(rc), F.b2 = d2f_rn(b2);
-    F.ent0 = d2f_rn(((1.0 - b2) - b3) * (csqr * inv_dpdE));
+    const float c2w = (0.0f < csqr) ? 0.0f : 1.0f;
+    const float c2 = Gamma0 * _P * _rho * c2w + (1.0f - c2w) * csqr;
+    const float q2 = _u * _u + _v * _v + _w * _w;
+    const float b2 = (1.0f + b1 * q2) - b1 * _H;
+    F._u = _u, F._v = _v, F._w = _w, F._H = _H, F._P = _P, F._rho = _rho;
+    F.c2 = c2, F.b1 = b1, F.b3 = b3, F.q2 = q2, F.b2 = b2;
+    F._c = sqrtf(c2), F._c1 = 1.0f / F._c;
+    F.ent0 = ((1.0f - b2) - b3) * (csqr * inv_dpdE);
 #pragma unroll
-    for (int n = 0; n < NS; n++) F._yi[n] = d2f_rn(yi[n]);
+    for (int n = 0; n < NS; n++) F._yi[n] = yi[n];
 }
 
 // FP32 characteristic WENO flux at face (i+1/2) of direction D (same structure as k_faces).
