@@ -278,7 +278,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     // layout of the pool
     size_t nd = 3 * E + 12 + (scheme->cop ? NS : 0);           // U, U1, LU, primitives, y
     if (h->fused) nd += E;                                      // U2, the fused stages' third buffer
-    if (scheme->cop) nd += 3 + (NS - 1);                        // per-cell sound-speed terms
+    if (scheme->cop && !mixed) nd += 3 + (NS - 1);              // per-cell sound-speed terms
     if (scheme->viscous && !mixed) nd += 9 + 2;                 // velocity derivatives, mu, kappa
     const bool fast1 = !scheme->cop && scheme->precision == XFG_FP64;  // single-gas fast path extras
     if (fast1) nd += 2 + 3 * (block->DimX + block->DimY + block->DimZ);
@@ -295,7 +295,7 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     }
     const size_t stage_elems = (size_t)h->N * (E > NS ? E : NS);
     // small words; transport tables at +4096 and +6144; scaled thermo table at +8192
-    const size_t small = 8192 + align_up(THERMO_SC_DOUBLES * sizeof(double), 256);
+    const size_t small = 8192 + align_up(THERMO_SC_BYTES, 256);
     size_t bytes = nd * arr8 + nf * arr4 + align_up(stage_elems * 8, 256) + small;
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&h->pool, bytes);
@@ -315,7 +315,8 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     if (h->fused) f.U2 = take8(E);
     f.rho = take8(1), f.u = take8(1), f.v = take8(1), f.w = take8(1), f.p = take8(1), f.H = take8(1);
     f.c = take8(1), f.T = take8(1), f.gamma = take8(1), f.e = take8(1), f.Cp = take8(1), f.R = take8(1);
-    if (scheme->cop) f.y = take8(NS), f.xc = take8(3 + (NS - 1));
+    if (scheme->cop) f.y = take8(NS);
+    if (scheme->cop && !mixed) f.xc = take8(3 + (NS - 1));
     if (scheme->viscous && !mixed) f.vde = take8(9), f.mu = take8(1), f.kappa = take8(1);
     if (fast1) {
         f.sr = take8(1), f.isr = take8(1);
@@ -360,12 +361,16 @@ int xfg_create(const xfg_block *block, const xfg_scheme *scheme, const xfg_therm
     th.nasa = scheme->thermo ? 1 : 0;
     th.ncop_gamma = scheme->ncop_gamma;
     std::vector<double> hsc(THERMO_SC_DOUBLES);
-    if (scheme->cop) {  // the mixed form's scaled enthalpy tables
+    std::vector<char> hb(THERMO_SC_BYTES);
+    if (scheme->cop) {  // the mixed form's scaled enthalpy tables, FP64 then FP32
         scaled_thermo_table(th, hsc.data());
+        std::memcpy(hb.data(), hsc.data(), THERMO_SC_DOUBLES * sizeof(double));
+        float *hf = (float *)(hb.data() + THERMO_SC_DOUBLES * sizeof(double));
+        for (int q = 0; q < THERMO_SC_DOUBLES; q++) hf[q] = (float)hsc[q];
         double *d = (double *)(p + 8192);
         th.hsc = d;
-        if (cudaMemcpyAsync(d, hsc.data(), THERMO_SC_DOUBLES * sizeof(double), cudaMemcpyHostToDevice, h->st) !=
-            cudaSuccess) {
+        th.hscf = (const float *)(d + THERMO_SC_DOUBLES);
+        if (cudaMemcpyAsync(d, hb.data(), THERMO_SC_BYTES, cudaMemcpyHostToDevice, h->st) != cudaSuccess) {
             xfg_destroy(h);
             return fail(-2, "upload of the thermo tables failed");
         }

@@ -47,6 +47,7 @@ struct DevThermo {
     int nasa;
     double ncop_gamma;
     const double *hsc;  // mixed mixtures: device copy of scaled_thermo_table (THERMO_SC_DOUBLES)
+    const float *hscf;  // the same table rounded to FP32 (the FP32 sound-speed cell terms)
 };
 
 // Enthalpy polynomials scaled by R_n for the mixed form, per species n and temperature range rg
@@ -59,6 +60,8 @@ struct DevThermo {
 // same polynomials as enthalpy() / heat_capacity() with the constant factors applied once.
 constexpr int THERMO_SC_CP200 = XFG_MAX_SPECIES * 3 * 8;
 constexpr int THERMO_SC_DOUBLES = THERMO_SC_CP200 + XFG_MAX_SPECIES;
+// device bytes of the table in both precisions (the FP32 copy follows the FP64 one)
+constexpr int THERMO_SC_BYTES = THERMO_SC_DOUBLES * 12;
 inline void scaled_thermo_table(const DevThermo &t, double *out) {
     for (int q = 0; q < THERMO_SC_DOUBLES; q++) out[q] = 0.0;
     for (int n = 0; n < XFG_MAX_SPECIES; n++) {
@@ -119,7 +122,7 @@ struct DevFields {
     float *primf;              // FP32 rho, u, v, w, H, p, c (7 components, mixed form)
     float *Fwf[3];             // FP32 face fluxes (mixed form)
     double *sr, *isr;          // sqrt(rho) and 1/sqrt(rho) per cell (single-gas FP64 fast path)
-    float *yf, *xcf;           // mixed mixtures: FP32 copies of y (NS) and of xc (3 + NCOP)
+    float *yf, *xcf;           // mixed mixtures: FP32 y (NS) and sound-speed cell terms (3 + NCOP)
     double *eab[3];            // |u_d - c|, |u_d|, |u_d + c| per cell and direction (same path)
     double *vde;               // viscous: the 9 cell-centre velocity derivatives (ducx..dwcz)
     double *mu, *kappa;        // viscous: mixture viscosity and thermal conductivity per cell
@@ -160,6 +163,13 @@ __device__ __forceinline__ double rcp_nr(double x) {
     r = fma(r, e, r);
     e = fma(-x, r, 1.0);
     return fma(r, e, r);
+}
+// One refinement step only: about 2^-40 relative, enough for a Newton step whose iteration
+// continues until the step itself is below the tolerance.
+__device__ __forceinline__ double rcp_nr1(double x) {
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+    return fma(r, fma(-x, r, 1.0), r);
 }
 __device__ __forceinline__ double rsqrt_nr(double x) {
     double y;

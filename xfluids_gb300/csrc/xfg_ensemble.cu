@@ -218,7 +218,7 @@ size_t member_bytes(const xfg_block &b, int cop, int ns, bool mixed) {
     const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
     const int dims = b.DimX + b.DimY + b.DimZ, E = cop ? ns + 4 : 5;
     size_t nd = 3 * E + 12;                                    // U, U1, LU, primitives
-    if (cop) nd += ns + 3 + (ns - 1);                          // y, per-cell sound-speed terms
+    if (cop) nd += ns + (mixed ? 0 : 3 + (ns - 1));           // y, per-cell sound-speed terms (FP64 form)
     if (mixed && !cop && two_d(b)) nd += 5;                    // U2 of the fused stages
     if (!mixed) nd += 2 * E * dims + (cop ? 0 : 2 + 3 * dims); // F, Fw; single gas: sqrt(rho), 1/sqrt(rho), |lambda|
     size_t bytes = nd * P * 8;
@@ -238,7 +238,8 @@ void carve(Member &m, char *base, const xfg_block &b, int cop, int ns, bool mixe
     if (mixed && !cop && two_d(b)) f.U2 = t8(5);
     f.rho = t8(1), f.u = t8(1), f.v = t8(1), f.w = t8(1), f.p = t8(1), f.H = t8(1);
     f.c = t8(1), f.T = t8(1), f.gamma = t8(1), f.e = t8(1), f.Cp = t8(1), f.R = t8(1);
-    if (cop) f.y = t8(ns), f.xc = t8(3 + (ns - 1));
+    if (cop) f.y = t8(ns);
+    if (cop && !mixed) f.xc = t8(3 + (ns - 1));
     if (!mixed) {
         for (int d = 0; d < 3; d++)
             if (dims[d]) f.F[d] = t8(E), f.Fw[d] = t8(E);
@@ -425,11 +426,15 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
     if (err == cudaSuccess) err = cudaMemsetAsync(e->derr, 0, sizeof(int) * 8 * capacity, e->st);
     if (err == cudaSuccess && scheme->cop) {  // the mixed form's scaled enthalpy tables
         std::vector<double> hsc(THERMO_SC_DOUBLES);
+        std::vector<char> hb(THERMO_SC_BYTES);
         scaled_thermo_table(e->th, hsc.data());
-        err = cudaMalloc(&e->dhsc, sizeof(double) * THERMO_SC_DOUBLES);
-        if (err == cudaSuccess)
-            err = cudaMemcpyAsync(e->dhsc, hsc.data(), sizeof(double) * THERMO_SC_DOUBLES, cudaMemcpyHostToDevice, e->st);
+        std::memcpy(hb.data(), hsc.data(), THERMO_SC_DOUBLES * sizeof(double));
+        float *hf = (float *)(hb.data() + THERMO_SC_DOUBLES * sizeof(double));
+        for (int q = 0; q < THERMO_SC_DOUBLES; q++) hf[q] = (float)hsc[q];
+        err = cudaMalloc(&e->dhsc, THERMO_SC_BYTES);
+        if (err == cudaSuccess) err = cudaMemcpyAsync(e->dhsc, hb.data(), THERMO_SC_BYTES, cudaMemcpyHostToDevice, e->st);
         e->th.hsc = e->dhsc;
+        e->th.hscf = (const float *)(e->dhsc + THERMO_SC_DOUBLES);
     }
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->st);
     if (err != cudaSuccess) {

@@ -4,8 +4,9 @@
 // the flux splitting, the WENO smoothness indicators and weights run in FP32 on FP32 copies of
 // U, of the physical fluxes and of the face primitives written by k_states_mixed. The FP32 right-
 // hand side is accumulated into the FP64 state by the RK stage. The multi-component temperature
-// Newton iteration and the multi-component Roe sound speed (the near-degenerate mixture
-// eigensystem) stay FP64.
+// Newton iteration stays FP64, and so do the jumps across a face from which the multi-component
+// Roe sound speed's near-degenerate correction is formed (face_state_mixed); the rest of the
+// mixture Roe state is FP32.
 #pragma once
 
 #include "xfg_kernels.cuh"
@@ -79,52 +80,40 @@ struct FoldedThermo {
     }
 };
 
-// The species enthalpies h_n(T) of the mixed form from the scaled tables: one range test, one log
-// and one reciprocal (NASA-9) for all species, the extrapolation below 200 K as one FMA.
+// cop_cell_terms for the mixed form, in FP32: the faces' Roe state averages these terms in FP32
+// (face_state_mixed), so they are formed from the FP32 values of T, Cp, gamma and R with the FP32
+// copy of the scaled species tables; e = E / rho - |u|^2 / 2 (equal to H - |u|^2 / 2 - p / rho) is
+// the caller's. The species sums (h_N - h_n) + (R_n - R_N) Cp T / R cancel by a factor of a few at
+// most for the tables here (formation enthalpies included), so the terms carry FP32 rounding.
 template <int NS>
-__device__ __forceinline__ void species_enthalpies_mixed(const DevThermo &t, double T0, double *h) {
-    const double T = fmax(T0, 200.0), dT = fmin(T0 - 200.0, 0.0);
-    const bool nasa = t.nasa;
-    int rg = thermo_range(nasa, T);
-    rg = rg < 0 ? 0 : rg;
-    const double lT = nasa ? log(T) : 0.0, iT = nasa ? rcp_nr(T) : 0.0;
+__device__ __forceinline__ void cop_cell_terms_mixed(const DevThermo &th, float T0, float Cp, float gm, float R,
+                                                     float u, float v, float w, float e, float *xcf, long long P,
+                                                     long long id) {
+    constexpr int NCOP = NS - 1;
+    const float *tab = th.hscf;
+    const float T = fmaxf(T0, 200.0f), dT = fminf(T0 - 200.0f, 0.0f);
+    const bool nasa = th.nasa;
+    int rg = nasa ? (T >= 1000.0f && T < 6000.0f ? 1 : (T < 1000.0f ? 0 : 2)) : (T > 1000.0f ? 0 : 1);
+    const float lT = nasa ? logf(T) : 0.0f, iT = nasa ? 1.0f / T : 0.0f;
+    float h[NS];
 #pragma unroll
     for (int n = 0; n < NS; n++) {
-        const double *c = t.hsc + (n * 3 + rg) * 8;
-        const double hp = nasa ? fma(c[0], iT, fma(c[1], lT, fma(fma(fma(fma(fma(c[6], T, c[5]), T, c[4]), T, c[3]), T, c[2]), T, c[7])))
-                               : fma(fma(fma(fma(fma(c[4], T, c[3]), T, c[2]), T, c[1]), T, c[0]), T, c[5]);
-        h[n] = fma(t.hsc[THERMO_SC_CP200 + n], dT, hp);
+        const float *c = tab + (n * 3 + rg) * 8;
+        const float hp = nasa ? fmaf(c[0], iT, fmaf(c[1], lT, fmaf(fmaf(fmaf(fmaf(fmaf(c[6], T, c[5]), T, c[4]), T, c[3]), T, c[2]), T, c[7])))
+                              : fmaf(fmaf(fmaf(fmaf(fmaf(c[4], T, c[3]), T, c[2]), T, c[1]), T, c[0]), T, c[5]);
+        h[n] = fmaf(tab[THERMO_SC_CP200 + n], dT, hp);
     }
+    const float q2 = u * u + v * v + w * w;
+    const float CpT_R = Cp * T0 / R;
+    const float RN = (float)th.Ri[NCOP];
+    const float g1 = gm - 1.0f;
+    xcf[id] = gm;
+    xcf[P + id] = g1 * (0.5f * q2 - h[NCOP] + RN * CpT_R);
+    xcf[2 * P + id] = e;
+#pragma unroll
+    for (int n = 0; n < NCOP; n++) xcf[(3 + n) * P + id] = g1 * ((h[NCOP] - h[n]) + ((float)th.Ri[n] - RN) * CpT_R);
 }
 
-// cop_cell_terms for the mixed form (the same terms, no reference rounding to keep): gamma from
-// the caller, one reciprocal of the mixture R instead of a division per term, e = E / rho - |u|^2 / 2
-// (the caller's internal energy, equal to H - |u|^2 / 2 - p / rho); each term also as FP32 (xcf) for
-// the FP32 Roe averages of face_state_mixed.
-template <int NS>
-__device__ __forceinline__ void cop_cell_terms_mixed(const DevThermo &th, double T, double Cp, double gm, double wi,
-                                                     double u, double v, double w, double e, double *xc,
-                                                     float *xcf, long long P, long long id) {
-    constexpr int NCOP = NS - 1;
-    double h[NS];
-    species_enthalpies_mixed<NS>(th, T, h);
-    const double q2 = u * u + v * v + w * w;
-    const double CpT_R = Cp * T * rcp_nr(wi * kRu);  // Cp T / R
-    const double RN = th.Ri[NCOP];
-    const double g1 = gm - 1.0;
-    double t[3 + (NCOP > 0 ? NCOP : 1)];
-    t[0] = gm;
-    t[1] = g1 * (0.5 * q2 - h[NCOP] + RN * CpT_R);
-    t[2] = e;
-#pragma unroll
-    for (int n = 0; n < NCOP; n++) t[3 + n] = g1 * ((h[NCOP] - h[n]) + (th.Ri[n] - RN) * CpT_R);
-#pragma unroll
-    for (int q = 0; q < 3 + NCOP; q++) xc[q * P + id] = t[q], xcf[q * P + id] = d2f_rn(t[q]);
-}
-
-// get_T (Mixing_device.h:171-193): the same clamped Newton iteration and stopping test on the
-// folded mixture polynomials, the step f / f' with the refined reciprocal of f'; returns T and the
-// mixture Cp at T.
 // h and Cp of the mixture by the per-species functions (below 200 K, or a temperature outside the
 // tables): a called function, so that the rare path costs the iteration nothing when not taken
 template <int NS>
@@ -133,6 +122,10 @@ __device__ __noinline__ void mix_h_cp_species(const DevThermo &t, const double *
     Cp = mix_Cp<NS>(t, yi, T);
 }
 
+// get_T (Mixing_device.h:171-193): the same clamped Newton iteration and stopping test on the
+// folded mixture polynomials (Rm the mixture R), the step f / f' with a once-refined reciprocal of
+// f' (the iteration goes on until the step is below 1e-6 K, so the step needs no more); returns T
+// and the mixture Cp at T.
 template <int NS>
 __device__ __forceinline__ double newton_T_folded(const DevThermo &t, const double *yi, double Rm, double e,
                                                   double T0, double &Cp_out) {
@@ -146,7 +139,7 @@ __device__ __forceinline__ double newton_T_folded(const DevThermo &t, const doub
             mix_h_cp_species<NS>(t, yi, T, h, Cp);
         double f = h - Rm * T - e;
         double df_ = Cp - Rm;
-        double df = fmin(f * rcp_nr(df_ + 1.0e-30), 1e-3 * T);
+        double df = fmin(f * rcp_nr1(df_ + 1.0e-30), 1e-3 * T);
         df = fmax(df, -1e-2 * T);
         T = T - df;
         if (fabs(df) <= 1.0e-6) break;
@@ -219,7 +212,8 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd;
             f.e[id] = tme, f.gamma[id] = gamma, f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
             if (f.Tf) f.Tf[id] = d2f_rn(T);  // viscous schemes: the heat flux's FP32 temperature
-            cop_cell_terms_mixed<NS>(th, T, Cp, gmx, wi, ud, vd, wd, tme, f.xc, f.xcf, P, id);
+            cop_cell_terms_mixed<NS>(th, d2f_rn(T), d2f_rn(Cp), d2f_rn(gmx), d2f_rn(Rm), d2f_rn(ud), d2f_rn(vd),
+                                     d2f_rn(wd), d2f_rn(tme), f.xcf, P, id);
 #pragma unroll
             for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = d2f_rn(yi[s]), f.yf[s * P + id] = yf[s];
 #pragma unroll
@@ -383,7 +377,7 @@ __device__ __forceinline__ void face_state_mixed(const DevFields &f, long long P
     // the jumps, from the FP64 states
     const double rl64 = f.rho[l], rr64 = f.rho[r];
     const float drho = d2f_rn(rr64 - rl64), dp = d2f_rn(f.p[r] - f.p[l]);
-    const float de = d2f_rn(f.xc[2 * P + r] - f.xc[2 * P + l]);
+    const float de = d2f_rn(f.e[r] - f.e[l]);
     const float du = d2f_rn(f.u[r] - f.u[l]), dv = d2f_rn(f.v[r] - f.v[l]), dw = d2f_rn(f.w[r] - f.w[l]);
 #pragma unroll
     for (int n = 0; n < NCOP; n++) {
