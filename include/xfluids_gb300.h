@@ -249,10 +249,11 @@ typedef struct xfg_ensemble xfg_ensemble;
 /* Create an ensemble with `capacity` member slots and a device pool of pool_bytes from which the
  * members are sub-allocated (admission by HBM budget). scheme: single gas (cop = 0) or a mixture of
  * 5 species (cop = 1, num_species = 5, thermal holding its tables; GhostSpecies and NASA-9 / JANAF
- * as the single-grid path), inviscid, ROE, LLF or GLF (running maxima per member), WENO5 /
- * WENO-CU6 / WENO7, positivity limiter on or off, precision XFG_FP64 or XFG_MIXED. The batched
- * kernels of each gas model and form are compiled with the contraction flags of the single-grid
- * kernels, so a member advances as the same block alone in a handle would. */
+ * as the single-grid path; inviscid, or viscous stress / heat conduction with the transport data
+ * of xfg_ensemble_set_transport), ROE, LLF or GLF (running maxima per member), WENO5 / WENO-CU6 /
+ * WENO7, positivity limiter on or off, precision XFG_FP64 or XFG_MIXED. The batched kernels of
+ * each gas model and form are compiled with the contraction flags of the single-grid kernels, so a
+ * member advances as the same block alone in a handle would. */
 int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *scheme, const xfg_thermal *thermal,
                         int device, xfg_ensemble **out);
 int xfg_ensemble_destroy(xfg_ensemble *e);
@@ -261,6 +262,10 @@ int xfg_ensemble_destroy(xfg_ensemble *e);
  * block under the given scheme (single gas or mixture). */
 size_t xfg_ensemble_member_bytes(const xfg_block *block, int precision);
 size_t xfg_ensemble_member_bytes_for(const xfg_block *block, const xfg_scheme *scheme);
+
+/* Viscous mixture ensembles: the fitted transport data of the species, shared by every member
+ * (as xfg_set_transport for one handle); required before the first xfg_ensemble_advance. */
+int xfg_ensemble_set_transport(xfg_ensemble *e, const xfg_transport *tr);
 
 /* Admit a member: state U (AoS, host or device), target time; runs BoundaryCondition(U) and
  * UpdateStates(U) for it (main.cpp:45-47). Returns 0 and *slot, 1 when no slot is free, 2 when the

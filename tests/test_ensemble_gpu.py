@@ -324,3 +324,59 @@ def test_mixture_members_equal_single_grid_runs(cuda_lib, order, prec):
             assert np.all(ens <= 3.0 * own + 1e-9), (slot, own, ens)
     finally:
         e.close()
+
+
+@pytest.mark.parametrize("prec", [FP64, MIXED], ids=["fp64", "mixed"])
+def test_viscous_mixture_members_equal_single_grid_runs(cuda_lib, prec):
+    """Viscous stress and heat conduction in the ensemble (Visc | Visc_Heat | Visc_Diffu, the
+    reference's fitted transport data): 3D mixing layers and a 2D walled block advanced together
+    equal the same blocks advanced alone with xfg_set_transport (FP64 to 1e-12; mixed members are
+    checked against the FP64 single-grid runs as in the inviscid mixture test)."""
+    import os
+    import helpers as H
+    z = np.load(os.path.join(H.GOLDEN, "visc_mixing5_12x8x6_janaf_w5.npz"))
+    tr = H.transport_of(z)
+    s, th, ms = _mixture_members(5)
+    s.viscous = 7
+    s.precision = prec
+    E = s.Emax
+    nsteps = 3
+    pool = sum(Ensemble.member_bytes(b, prec, scheme=s) for b, _, _ in ms) + 4096 * len(ms)
+    e = Ensemble(s, capacity=len(ms), pool_bytes=pool, thermal=th)
+
+    def alone_run(precision):
+        s.precision = precision
+        f = Fluid(b, s, th)
+        f.set_transport(tr)
+        f.InitialU(U, T)
+        f.initialize()
+        out = f.advance(nsteps), f.get("U").reshape(-1).copy()
+        f.close()
+        s.precision = prec
+        return out
+
+    try:
+        slots = [e.add(b, U, 1e300, T=T) for b, U, T in ms]
+        assert None not in slots
+        from xfluids_gb300.abi import XfgError
+        with pytest.raises(XfgError):
+            e.advance(1)                  # no transport data yet
+        e.set_transport(tr)
+        st, _ = e.advance(nsteps)
+        assert st == 0
+        for (b, U, T), slot in zip(ms, slots):
+            (st1, t_ref, n_ref), ref = alone_run(prec)
+            info = e.status(slot)
+            assert st1 == 0 and info["error"] == 0 and info["steps"] == n_ref
+            assert info["t"] == pytest.approx(t_ref, rel=1e-13 if prec == FP64 else MIXED_T_TOL, abs=0)
+            got = e.get_state(slot)
+            err = normwise(got, ref, E).max()
+            print(f"viscous member {slot} {b.X_inner}x{b.Y_inner}x{b.Z_inner}: normwise vs alone {err:.3e}")
+            if prec == FP64:
+                assert err <= PARITY_TOL, (slot, err)
+                continue
+            (_, t64, _), r64 = alone_run(FP64)
+            own, ens = _l1_rel(ref, r64, E), _l1_rel(got, r64, E)
+            assert np.all(ens <= 3.0 * own + 1e-9), (slot, own, ens)
+    finally:
+        e.close()

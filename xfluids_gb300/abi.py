@@ -166,6 +166,7 @@ def lib():
         "xfg_ensemble_add_checkpoint": [P, C.POINTER(Block), C.c_char_p, D, P, pi],
         "xfg_checkpoint_write": [P, C.c_char_p, I, D, C.c_float],
         "xfg_set_transport": [P, C.POINTER(Transport)],
+        "xfg_ensemble_set_transport": [P, C.POINTER(Transport)],
         "xfg_checkpoint_read": [P, C.c_char_p, pi, pd, C.POINTER(C.c_float)],
         "xfg_ensemble_get_option": [P, I, pi],
         "xfg_ensemble_active": [P],

@@ -220,6 +220,39 @@ int validate_block_scheme(const xfg_block *b, const xfg_scheme *s, const xfg_the
         return fail(-1, "block too elongated for the face launches (Z_inner or, in 3D, Y_inner above 65534)");
     return 0;
 }
+int pack_transport(const xfg_transport *tr, int ns, std::vector<double> &t, std::vector<float> &tf) {
+    if (tr->num_species != ns) return fail(-1, "transport data for %d species, the scheme has %d", tr->num_species, ns);
+    t.assign(8 * ns + 2 * ns * ns + ns, 0.0);
+    for (int k = 0; k < ns; k++)
+        for (int q = 0; q < XFG_FIT_ORDER; q++) {
+            t[4 * k + q] = tr->visc[k * XFG_FIT_ORDER + q];
+            t[4 * ns + 4 * k + q] = tr->therm[k * XFG_FIT_ORDER + q];
+        }
+    for (int k = 0; k < ns; k++)
+        for (int i = 0; i < ns; i++) {
+            const double Wk = tr->species_chara[k * XFG_SPCH + 6], Wi = tr->species_chara[i * XFG_SPCH + 6];
+            t[8 * ns + k * ns + i] = std::pow(Wi / Wk, 0.25);
+            t[8 * ns + ns * ns + k * ns + i] = std::pow(1.0 + Wk / Wi, -0.5);
+        }
+    for (int k = 0; k < ns; k++) {
+        const double sid = tr->species_chara[k * XFG_SPCH + 8];
+        if (!(sid >= 0.0 && sid < ns)) return fail(-1, "species id %g out of range", sid);
+        t[8 * ns + 2 * ns * ns + k] = sid;
+    }
+    tf.assign(8 * ns + 2 * ns * ns, 0.0f);
+    for (int k = 0; k < ns; k++) {
+        const int ik = (int)t[8 * ns + 2 * ns * ns + k];
+        for (int q = 0; q < XFG_FIT_ORDER; q++) {
+            tf[4 * k + q] = (float)t[4 * ik + q];
+            tf[4 * ns + 4 * k + q] = (float)t[4 * ns + 4 * ik + q];
+        }
+        for (int i = 0; i < ns; i++) {
+            tf[8 * ns + k * ns + i] = (float)t[8 * ns + k * ns + i];
+            tf[8 * ns + ns * ns + k * ns + i] = (float)(t[8 * ns + ns * ns + k * ns + i] * 0.5 / std::sqrt(2.0));
+        }
+    }
+    return 0;
+}
 }  // namespace xfg
 
 extern "C" {
@@ -445,39 +478,9 @@ int xfg_set_state(xfg_handle *h, const double *U_aos, const double *T) {
 int xfg_set_transport(xfg_handle *h, const xfg_transport *tr) {
     if (!h || !tr) return fail(-1, "null argument");
     if (!h->sc.viscous) return fail(-1, "the scheme has no viscous fluxes (xfg_scheme.viscous = 0)");
-    const int ns = h->NS;
-    if (tr->num_species != ns) return fail(-1, "transport data for %d species, the scheme has %d", tr->num_species, ns);
-    std::vector<double> t(8 * ns + 2 * ns * ns + ns);
-    for (int k = 0; k < ns; k++)
-        for (int q = 0; q < XFG_FIT_ORDER; q++) {
-            t[4 * k + q] = tr->visc[k * XFG_FIT_ORDER + q];
-            t[4 * ns + 4 * k + q] = tr->therm[k * XFG_FIT_ORDER + q];
-        }
-    for (int k = 0; k < ns; k++)
-        for (int i = 0; i < ns; i++) {
-            const double Wk = tr->species_chara[k * XFG_SPCH + 6], Wi = tr->species_chara[i * XFG_SPCH + 6];
-            t[8 * ns + k * ns + i] = std::pow(Wi / Wk, 0.25);
-            t[8 * ns + ns * ns + k * ns + i] = std::pow(1.0 + Wk / Wi, -0.5);
-        }
-    for (int k = 0; k < ns; k++) {
-        const double sid = tr->species_chara[k * XFG_SPCH + 8];
-        if (!(sid >= 0.0 && sid < ns)) return fail(-1, "species id %g out of range", sid);
-        t[8 * ns + 2 * ns * ns + k] = sid;
-    }
-    // FP32 table of the mixed form, species already resolved through SID: visc[4*ns], therm[4*ns],
-    // wa[ns*ns], wb[ns*ns] * 0.5 / sqrt(2)
-    std::vector<float> tf(8 * ns + 2 * ns * ns);
-    for (int k = 0; k < ns; k++) {
-        const int ik = (int)t[8 * ns + 2 * ns * ns + k];
-        for (int q = 0; q < XFG_FIT_ORDER; q++) {
-            tf[4 * k + q] = (float)t[4 * ik + q];
-            tf[4 * ns + 4 * k + q] = (float)t[4 * ns + 4 * ik + q];
-        }
-        for (int i = 0; i < ns; i++) {
-            tf[8 * ns + k * ns + i] = (float)t[8 * ns + k * ns + i];
-            tf[8 * ns + ns * ns + k * ns + i] = (float)(t[8 * ns + ns * ns + k * ns + i] * 0.5 / std::sqrt(2.0));
-        }
-    }
+    std::vector<double> t;
+    std::vector<float> tf;
+    if (int rc = pack_transport(tr, h->NS, t, tf)) return rc;
     CK(cudaSetDevice(h->device));
     CK(cudaMemcpyAsync((void *)h->ctx.f.trf, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice, h->st));
     CK(cudaMemcpyAsync((void *)h->ctx.f.tr, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));

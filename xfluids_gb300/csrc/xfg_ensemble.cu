@@ -188,6 +188,9 @@ struct xfg_ensemble {
     double *hdt = nullptr;                // pinned mirror
     int *derr = nullptr;                  // device error words (8 ints each)
     double *dhsc = nullptr;               // mixtures: the scaled enthalpy tables (DevThermo::hsc)
+    double *dtr = nullptr;                // viscous mixtures: transport tables, FP64 then FP32
+    float *dtrf = nullptr;
+    bool transport_ready = false;         // xfg_ensemble_set_transport called
     int *herr = nullptr;
     std::vector<int> order;               // active slots in launch order
     int nblk[PH_N] = {0};
@@ -213,8 +216,9 @@ size_t row_len(const xfg_ensemble *e) { return 3 * (size_t)e->capacity + 1; }
 bool two_d(const xfg_block &b) { return b.DimX && b.DimY && !b.DimZ; }
 
 // Device bytes of one member: the single-grid arrays of its gas model (ns species, 1 for a single
-// gas) and form, as xfg_create lays them out, without the viscous and transpose arrays.
-size_t member_bytes(const xfg_block &b, int cop, int ns, bool mixed) {
+// gas) and form, as xfg_create lays them out (viscous mixtures: the velocity derivatives, mu and
+// kappa), without the transpose arrays.
+size_t member_bytes(const xfg_block &b, int cop, int ns, bool mixed, int visc) {
     const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
     const int dims = b.DimX + b.DimY + b.DimZ, E = cop ? ns + 4 : 5;
     size_t nd = 3 * E + 12;                                    // U, U1, LU, primitives
@@ -222,11 +226,13 @@ size_t member_bytes(const xfg_block &b, int cop, int ns, bool mixed) {
     if (mixed && !cop && two_d(b)) nd += 5;                    // U2 of the fused stages
     if (!mixed) nd += 2 * E * dims + (cop ? 0 : 2 + 3 * dims); // F, Fw; single gas: sqrt(rho), 1/sqrt(rho), |lambda|
     size_t bytes = nd * P * 8;
-    if (mixed) bytes += (size_t)(E + 7 + 2 * E * dims + (cop ? ns + 3 + (ns - 1) : 0)) * up(P * 4, 256);
+    if (mixed) bytes += (size_t)(E + 7 + 2 * E * dims + (cop ? ns + 3 + (ns - 1) : 0) + (visc ? 9 + 3 : 0)) * up(P * 4, 256);
+    if (visc && !mixed) bytes += (size_t)(9 + 2) * P * 8;
     return bytes + 1024;                                       // lam + small words
 }
 
-void carve(Member &m, char *base, const xfg_block &b, int cop, int ns, bool mixed) {
+void carve(Member &m, char *base, const xfg_block &b, int cop, int ns, bool mixed, int visc, const double *tr,
+           const float *trf) {
     const size_t N = (size_t)b.Xmax * b.Ymax * b.Zmax, P = up(N, 64);
     const int dims[3] = {b.DimX, b.DimY, b.DimZ}, E = cop ? ns + 4 : 5;
     char *p = base;
@@ -248,12 +254,16 @@ void carve(Member &m, char *base, const xfg_block &b, int cop, int ns, bool mixe
             for (int d = 0; d < 3; d++)
                 if (dims[d]) f.eab[d] = t8(3);
         }
+        if (visc) f.vde = t8(9), f.mu = t8(1), f.kappa = t8(1);
     } else {
         f.Uf = t4(E), f.primf = t4(7);
         if (cop) f.yf = t4(ns), f.xcf = t4(3 + (ns - 1));
+        if (visc) f.vdef = t4(9), f.muf = t4(1), f.kappaf = t4(1), f.Tf = t4(1);
         for (int d = 0; d < 3; d++)
             if (dims[d]) f.Ff[d] = t4(E), f.Fwf[d] = t4(E);
     }
+    if (visc) f.tr = tr, f.trf = trf;  // the ensemble's transport tables
+    m.visc = visc;
     f.lam = (unsigned long long *)p;
     m.glf = (unsigned long long *)(p + 64);
     Geo &g = m.g;
@@ -288,6 +298,22 @@ int blocks_of(const Member &m, int ph, int ltx) {
     if (ph == PH_FUSED)
         return m.fused ? ((g.Xi + fz::TX - 1) / fz::TX) * ((g.Yi + fz::TY - 1) / fz::TY) : 0;
     if (ph == PH_GLAM) return m.fused ? gb(fused_ghost_cells(g)) : 0;
+    if (ph >= PH_VCELL && ph <= PH_VF2) {
+        if (!m.visc) return 0;
+        const int dims[3] = {g.dimx, g.dimy, g.dimz};
+        if (ph == PH_VCELL)
+            return gb((long long)(g.dimx ? g.Xi + 4 : 1) * (g.dimy ? g.Yi + 4 : 1) * (g.dimz ? g.Zi + 4 : 1));
+        if (ph <= PH_VBC2) {
+            const int d = ph - PH_VBC0;
+            const long long nb[3] = {(long long)g.Bx * g.Ymax * g.Zmax, (long long)g.By * g.Xmax * g.Zmax,
+                                     (long long)g.Bz * g.Xmax * g.Ymax};
+            return dims[d] ? gb(nb[d]) : 0;
+        }
+        const int d = ph - PH_VF0;
+        const long long nf[3] = {(long long)(g.Xi + 1) * g.Yi * g.Zi, (long long)g.Xi * (g.Yi + 1) * g.Zi,
+                                 (long long)g.Xi * g.Yi * (g.Zi + 1)};
+        return dims[d] ? gb(nf[d]) : 0;
+    }
     if (m.fused && ph >= PH_STATES && ph <= PH_DIV) return 0;  // done by the fused tiles
     switch (ph) {
     case PH_BC0: return g.dimx ? gb((long long)g.Bx * g.Ymax * g.Zmax) : 0;
@@ -370,6 +396,15 @@ void launch_step(xfg_ensemble *e) {
                     ops->faces(e->dm, tab(e, PH_F0 + d), e->nblk[PH_F0 + d], n, e->th, d, order, flag, art, st);
         }
         if (e->sc.positivity) ops->pp(e->dm, tab(e, PH_DIV), e->nblk[PH_DIV], n, flag, st);
+        if (e->sc.viscous && e->nblk[PH_VCELL]) {  // ConVenction_block.hpp:419-566, the single grid's order
+            const int heat = (e->sc.viscous & 2) ? 1 : 0;
+            ops->vderiv(e->dm, tab(e, PH_VCELL), e->nblk[PH_VCELL], n, st);
+            for (int d = 0; d < 3; d++)
+                if (e->nblk[PH_VBC0 + d]) ops->vderiv_bc(e->dm, tab(e, PH_VBC0 + d), e->nblk[PH_VBC0 + d], n, d, st);
+            ops->transport(e->dm, tab(e, PH_VCELL), e->nblk[PH_VCELL], n, e->th, heat, st);
+            for (int d = 0; d < 3; d++)
+                if (e->nblk[PH_VF0 + d]) ops->visc(e->dm, tab(e, PH_VF0 + d), e->nblk[PH_VF0 + d], n, d, heat, st);
+        }
         ops->div_rk(e->dm, tab(e, PH_DIV), e->nblk[PH_DIV], n, flag, st);
     }
 }
@@ -385,7 +420,10 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
     if (scheme->precision != XFG_FP64 && scheme->precision != XFG_MIXED)
         return efail(-1, "ensemble precision must be XFG_FP64 or XFG_MIXED%s");
     if (scheme->positivity != 0 && scheme->positivity != 1) return efail(-1, "positivity must be 0 or 1%s");
-    if (scheme->viscous) return efail(-1, "the ensemble engine serves inviscid members%s");
+    if (scheme->viscous < 0 || scheme->viscous > 7 || (scheme->viscous && !(scheme->viscous & 1)))
+        return efail(-1, "viscous must be Visc | Visc_Heat << 1 | Visc_Diffu << 2%s");
+    if (scheme->viscous && !scheme->cop)
+        return efail(-1, "viscous fluxes need a mixture (cop = 1): the single-gas states compute no temperature%s");
     if (scheme->scheme_order < 5 || scheme->scheme_order > 7) return efail(-1, "scheme_order must be 5, 6 or 7%s");
     const int ns = scheme->cop ? scheme->num_species : 1;
     if (scheme->cop && (!thermal || thermal->num_species != ns))
@@ -436,6 +474,15 @@ int xfg_ensemble_create(int capacity, size_t pool_bytes, const xfg_scheme *schem
         e->th.hsc = e->dhsc;
         e->th.hscf = (const float *)(e->dhsc + THERMO_SC_DOUBLES);
     }
+    if (err == cudaSuccess && scheme->viscous) {  // transport tables, filled by xfg_ensemble_set_transport
+        const int ns = e->NS;
+        const size_t nd = 8 * ns + 2 * ns * ns + ns, nf = 8 * ns + 2 * ns * ns;
+        err = cudaMalloc(&e->dtr, nd * sizeof(double) + nf * sizeof(float));
+        if (err == cudaSuccess) {
+            e->dtrf = (float *)(e->dtr + nd);
+            err = cudaMemsetAsync(e->dtr, 0, nd * sizeof(double) + nf * sizeof(float), e->st);
+        }
+    }
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->st);
     if (err != cudaSuccess) {
         xfg_ensemble_destroy(e);
@@ -471,6 +518,7 @@ int xfg_ensemble_destroy(xfg_ensemble *e) {
     for (auto &v : e->ev)
         if (v) cudaEventDestroy(v);
     cudaFree(e->pool), cudaFree(e->dm), cudaFree(e->doff), cudaFree(e->ddt), cudaFree(e->derr), cudaFree(e->dhsc);
+    cudaFree(e->dtr);
     if (e->hdt) cudaFreeHost(e->hdt);
     if (e->herr) cudaFreeHost(e->herr);
     if (e->st) cudaStreamDestroy(e->st);
@@ -479,13 +527,27 @@ int xfg_ensemble_destroy(xfg_ensemble *e) {
 }
 
 size_t xfg_ensemble_member_bytes(const xfg_block *block, int precision) {
-    return block ? member_bytes(*block, 0, 1, precision == XFG_MIXED) : 0;
+    return block ? member_bytes(*block, 0, 1, precision == XFG_MIXED, 0) : 0;
+}
+
+int xfg_ensemble_set_transport(xfg_ensemble *e, const xfg_transport *tr) {
+    if (!e || !tr) return efail(-1, "null argument%s");
+    if (!e->sc.viscous) return efail(-1, "the scheme has no viscous fluxes (xfg_scheme.viscous = 0)%s");
+    std::vector<double> t;
+    std::vector<float> tf;
+    if (int rc = pack_transport(tr, e->NS, t, tf)) return rc;
+    ECK(cudaSetDevice(e->device));
+    ECK(cudaMemcpyAsync(e->dtr, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, e->st));
+    ECK(cudaMemcpyAsync(e->dtrf, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice, e->st));
+    ECK(cudaStreamSynchronize(e->st));
+    e->transport_ready = true;
+    return 0;
 }
 
 size_t xfg_ensemble_member_bytes_for(const xfg_block *block, const xfg_scheme *scheme) {
     if (!block || !scheme) return 0;
     return member_bytes(*block, scheme->cop ? 1 : 0, scheme->cop ? scheme->num_species : 1,
-                        scheme->precision == XFG_MIXED);
+                        scheme->precision == XFG_MIXED, scheme->cop ? scheme->viscous : 0);
 }
 
 int xfg_ensemble_add(xfg_ensemble *e, const xfg_block *block, const double *U_aos, double target_t, int *slot) {
@@ -502,13 +564,13 @@ int xfg_ensemble_add_t(xfg_ensemble *e, const xfg_block *block, const double *U_
         if (!e->hm[q].active && e->m_len[q] == 0) { s = q; break; }
     if (s < 0) return 1;  // no free slot
     const bool mixed = e->sc.precision == XFG_MIXED;
-    const size_t need = member_bytes(*block, e->sc.cop, e->NS, mixed);
+    const size_t need = member_bytes(*block, e->sc.cop, e->NS, mixed, e->sc.viscous);
     size_t off = 0;
     if (!e->alloc.alloc(need, &off)) return 2;  // no memory: admission waits
     ECK(cudaSetDevice(e->device));
     Member &m = e->hm[s];
     std::memset(&m, 0, sizeof m);
-    carve(m, e->pool + off, *block, e->sc.cop, e->NS, mixed);
+    carve(m, e->pool + off, *block, e->sc.cop, e->NS, mixed, e->sc.viscous, e->dtr, e->dtrf);
     m.f.dtbuf = e->ddt + 8 * s;
     m.f.err = e->derr + 8 * s;
     m.active = 1;
@@ -557,6 +619,7 @@ int xfg_ensemble_remove(xfg_ensemble *e, int slot) {
 
 int xfg_ensemble_advance(xfg_ensemble *e, int nsteps, int use_graph, float *device_ms) {
     if (!e) return efail(-1, "null ensemble%s");
+    if (e->sc.viscous && !e->transport_ready) return efail(-1, "viscous scheme: call xfg_ensemble_set_transport first%s");
     ECK(cudaSetDevice(e->device));
     if (e->dirty) {
         int rc = rebuild(e);

@@ -14,6 +14,7 @@
 #include "xfg_kernels.cuh"
 #include "xfg_mixed.cuh"
 #include "xfg_ops.h"
+#include "xfg_viscous.cuh"
 
 namespace xfg {
 
@@ -26,13 +27,20 @@ struct EnsMember {
     int active;
     int ltx;    // face tile of this member: 2^ltx faces along x by kThreads >> ltx across
     int fused;  // 2D single-gas member of a mixed WENO5 LLF / Roe ensemble: its stages run as fused tiles
+    int visc;   // xfg_scheme.viscous of a mixture member (0: inviscid)
     unsigned long long *glf;  // GLF running maxima (9 words in the member's small-word area)
 };
 
 // phases with a block table; PH_FALL holds three entries per member (x, y, z face sweeps of the
 // fused face launch), the others one. PH_FUSED: the 32 x 7 tiles of the fused mixed stage
-// (xfg_fused.cuh) of the fused members, PH_GLAM: their ghost cells' dt maxima.
-enum { PH_BC0, PH_BC1, PH_BC2, PH_STATES, PH_F0, PH_F1, PH_F2, PH_DIV, PH_FALL, PH_FUSED, PH_GLAM, PH_N };
+// (xfg_fused.cuh) of the fused members, PH_GLAM: their ghost cells' dt maxima. Viscous members:
+// PH_VCELL the cells of the velocity derivatives and the transport coefficients ([B-2, inner+B+2)
+// in every active direction), PH_VBC0..2 the derivatives' ghost layers, PH_VF0..2 the faces of the
+// viscous fluxes.
+enum {
+    PH_BC0, PH_BC1, PH_BC2, PH_STATES, PH_F0, PH_F1, PH_F2, PH_DIV, PH_FALL, PH_FUSED, PH_GLAM,
+    PH_VCELL, PH_VBC0, PH_VBC1, PH_VBC2, PH_VF0, PH_VF1, PH_VF2, PH_N
+};
 
 // Launchers of the per-member phases of one (gas model, form). Every launcher covers `nblk`
 // blocks of the phase's table `tab` over the n members of `M` (n3 = 3 n entries for faces_all).
@@ -48,6 +56,12 @@ struct EnsOps {
     void (*glf)(const EnsMember *M, const int *tab, unsigned nblk, int n, cudaStream_t st);
     void (*pp)(const EnsMember *M, const int *tab, unsigned nblk, int n, int flag, cudaStream_t st);
     void (*div_rk)(const EnsMember *M, const int *tab, unsigned nblk, int n, int flag, cudaStream_t st);
+    // viscous mixtures (null for a single gas): ConVenction_block.hpp:419-566 over the members
+    void (*vderiv)(const EnsMember *M, const int *tab, unsigned nblk, int n, cudaStream_t st);
+    void (*vderiv_bc)(const EnsMember *M, const int *tab, unsigned nblk, int n, int d, cudaStream_t st);
+    void (*transport)(const EnsMember *M, const int *tab, unsigned nblk, int n, const DevThermo &th, int heat,
+                      cudaStream_t st);
+    void (*visc)(const EnsMember *M, const int *tab, unsigned nblk, int n, int d, int heat, cudaStream_t st);
 };
 
 // Registry (xfg_ensemble.cu): tables per (cop, ns, precision); a face override replaces the face
@@ -243,6 +257,50 @@ __global__ void __launch_bounds__(kThreads) kb_glf(const EnsMember *__restrict__
 
 // Launchers of one (gas model, form); the table registered by Registrar, or the face launchers
 // alone by FacesRegistrar.
+// Viscous stress and heat conduction of the mixture members (xfg_viscous.cuh bodies, FP64 or the
+// mixed form's FP32), in the single grid's order: derivatives, their ghost layers, transport
+// coefficients, face fluxes.
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_vderiv(const EnsMember *__restrict__ M, const int *__restrict__ off,
+                                                      int n) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const EnsMember &m = M[mi];
+    if (member_done(m)) return;
+    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    if constexpr (MIXED) vderiv_f32_body(m.g, m.f, t);
+    else vderiv_body(m.g, m.f, t);
+}
+template <int D, bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_vderiv_bc(const EnsMember *__restrict__ M, const int *__restrict__ off,
+                                                         int n) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const EnsMember &m = M[mi];
+    if (member_done(m)) return;
+    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    if constexpr (MIXED) vderiv_bc_body<D, float>(m.g, m.f, m.f.vdef, t);
+    else vderiv_bc_body<D, double>(m.g, m.f, m.f.vde, t);
+}
+template <int NS, bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_transport(const EnsMember *__restrict__ M, const int *__restrict__ off,
+                                                         int n, DevThermo th, int heat) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const EnsMember &m = M[mi];
+    if (member_done(m)) return;
+    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    if constexpr (MIXED) transport_f32_body<NS>(m.g, m.f, th, heat, t);
+    else transport_body<NS>(m.g, m.f, th, heat, t);
+}
+template <int D, int E, bool MIXED>
+__global__ void __launch_bounds__(kThreads) kb_visc(const EnsMember *__restrict__ M, const int *__restrict__ off,
+                                                    int n, int heat) {
+    const int mi = member_of_block(off, n, blockIdx.x);
+    const EnsMember &m = M[mi];
+    if (member_done(m)) return;
+    const long long t = (long long)(blockIdx.x - off[mi]) * blockDim.x + threadIdx.x;
+    if constexpr (MIXED) visc_f32_body<D, E>(m.g, m.f, heat, t);
+    else visc_body<D, E, double>(m.g, m.f, m.f.Fw[D], heat, t);
+}
+
 template <bool COP, int NS, bool MIXED>
 struct EnsInst {
     static constexpr int E = Sys<COP, NS>::E;
@@ -297,9 +355,29 @@ struct EnsInst {
     static void div_rk(const EnsMember *M, const int *tab, unsigned nb, int n, int flag, cudaStream_t st) {
         kb_div_rk<E, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n, flag);
     }
+    static void vderiv(const EnsMember *M, const int *tab, unsigned nb, int n, cudaStream_t st) {
+        kb_vderiv<MIXED><<<nb, kThreads, 0, st>>>(M, tab, n);
+    }
+    static void vderiv_bc(const EnsMember *M, const int *tab, unsigned nb, int n, int d, cudaStream_t st) {
+        if (d == 0) kb_vderiv_bc<0, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n);
+        else if (d == 1) kb_vderiv_bc<1, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n);
+        else kb_vderiv_bc<2, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n);
+    }
+    static void transport(const EnsMember *M, const int *tab, unsigned nb, int n, const DevThermo &th, int heat,
+                          cudaStream_t st) {
+        kb_transport<NS, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n, th, heat);
+    }
+    static void visc(const EnsMember *M, const int *tab, unsigned nb, int n, int d, int heat, cudaStream_t st) {
+        if (d == 0) kb_visc<0, E, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n, heat);
+        else if (d == 1) kb_visc<1, E, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n, heat);
+        else kb_visc<2, E, MIXED><<<nb, kThreads, 0, st>>>(M, tab, n, heat);
+    }
     static const EnsOps *table(int prec) {
         static EnsOps t[3];
-        t[prec] = EnsOps{COP ? 1 : 0, NS, prec, bc, states, faces, faces_all, glf, pp, div_rk};
+        if constexpr (COP)
+            t[prec] = EnsOps{1, NS, prec, bc, states, faces, faces_all, glf, pp, div_rk, vderiv, vderiv_bc, transport, visc};
+        else
+            t[prec] = EnsOps{0, NS, prec, bc, states, faces, faces_all, glf, pp, div_rk, nullptr, nullptr, nullptr, nullptr};
         return &t[prec];
     }
 };

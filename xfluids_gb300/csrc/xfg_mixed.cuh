@@ -67,6 +67,12 @@ struct FoldedThermo {
         }
         return true;
     }
+    // h of the mixture at T >= 200 K within the folded range
+    __device__ __forceinline__ double eval_h(bool nasa, double T) const {
+        if (nasa)
+            return fma(H[0], rcp_nr(T), fma(H[1], log(T), fma(fma(fma(fma(fma(H[6], T, H[5]), T, H[4]), T, H[3]), T, H[2]), T, H[7])));
+        return fma(fma(fma(fma(fma(H[4], T, H[3]), T, H[2]), T, H[1]), T, H[0]), T, H[5]);
+    }
     // h and Cp of the mixture at T >= 200 K within the folded range
     __device__ __forceinline__ void eval(bool nasa, double T, double &h, double &Cp) const {
         if (nasa) {
@@ -122,6 +128,43 @@ __device__ __noinline__ void mix_h_cp_species(const DevThermo &t, const double *
     Cp = mix_Cp<NS>(t, yi, T);
 }
 
+// The folded mixture polynomials in FP32 (the FP32 copy of the scaled tables), T >= 200 K.
+template <int NS>
+struct FoldedThermo32 {
+    float H[8], A[7];
+    int rg = -9;
+    __device__ __forceinline__ void fold(const DevThermo &t, const float *yf, int r) {
+        if (r == rg) return;
+        rg = r;
+        const int nc = t.nasa ? 8 : 6;
+#pragma unroll
+        for (int c = 0; c < 8; c++) H[c] = 0.0f;
+#pragma unroll
+        for (int n = 0; n < NS; n++) {
+            const float *c = t.hscf + (n * 3 + r) * 8;
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+                if (q < nc) H[q] = fmaf(yf[n], c[q], H[q]);
+        }
+        if (t.nasa) {
+            A[0] = -H[0], A[1] = H[1], A[2] = H[2], A[3] = 2.0f * H[3], A[4] = 3.0f * H[4], A[5] = 4.0f * H[5];
+            A[6] = 5.0f * H[6];
+        } else {
+            A[0] = H[0], A[1] = 2.0f * H[1], A[2] = 3.0f * H[2], A[3] = 4.0f * H[3], A[4] = 5.0f * H[4];
+        }
+    }
+    __device__ __forceinline__ void eval(bool nasa, float T, float &h, float &Cp) const {
+        if (nasa) {
+            const float iT = 1.0f / T;
+            Cp = fmaf(fmaf(A[0], iT, A[1]), iT, fmaf(fmaf(fmaf(fmaf(A[6], T, A[5]), T, A[4]), T, A[3]), T, A[2]));
+            h = fmaf(H[0], iT, fmaf(H[1], logf(T), fmaf(fmaf(fmaf(fmaf(fmaf(H[6], T, H[5]), T, H[4]), T, H[3]), T, H[2]), T, H[7])));
+        } else {
+            Cp = fmaf(fmaf(fmaf(fmaf(A[4], T, A[3]), T, A[2]), T, A[1]), T, A[0]);
+            h = fmaf(fmaf(fmaf(fmaf(fmaf(H[4], T, H[3]), T, H[2]), T, H[1]), T, H[0]), T, H[5]);
+        }
+    }
+};
+
 // get_T (Mixing_device.h:171-193): the same clamped Newton iteration and stopping test on the
 // folded mixture polynomials (Rm the mixture R), the step f / f' with a once-refined reciprocal of
 // f' (the iteration goes on until the step is below 1e-6 K, so the step needs no more); returns T
@@ -148,6 +191,54 @@ __device__ __forceinline__ double newton_T_folded(const DevThermo &t, const doub
     if (T >= 200.0 && ft.fold(t, yi, T)) ft.eval(t.nasa, T, h, Cp_out);
     else mix_h_cp_species<NS>(t, yi, T, h, Cp_out);
     return T;
+}
+
+// Temperature of the mixed form: the clamped Newton iteration of get_T run in FP32 on the FP32
+// folded polynomials until its step is below 1e-5 T, then one FP64 Newton step on the FP64 folded
+// polynomial with the FP32 derivative. The FP32 iterate is within ~1e-3 K of the root (the FP32
+// rounding of h - R T - e), so the FP64 step lands within ~1e-10 K of it (the error of a Newton
+// step is about (h'' / 2 (h' - R)) times the squared distance, ~1e-4 / K here; a step of up to
+// 2e-5 T is accepted), inside the reference's 1e-6 K tolerance. Returns T and the mixture Cp at the FP32 iterate (FP32 accuracy, for gamma and
+// the cell terms, which are FP32 downstream);
+// below 200 K, across a table range, or without FP32 convergence in 30 iterations it returns the
+// FP64 iteration's result instead (newton_T_folded).
+template <int NS>
+__device__ __forceinline__ double newton_T_mixed(const DevThermo &t, const double *yi, double Rm, double e,
+                                                 double T0, double &Cp_out) {
+    float yf[NS];
+#pragma unroll
+    for (int n = 0; n < NS; n++) yf[n] = d2f_rn(yi[n]);
+    const float Rf = d2f_rn(Rm), ef = d2f_rn(e);
+    const bool nasa = t.nasa;
+    FoldedThermo32<NS> ft;
+    float T = d2f_rn(T0), Cp = 0.0f;
+    bool ok = false;
+    for (int it = 0; it < 30; it++) {
+        const int r = thermo_range(nasa, T);
+        if (!(T >= 200.0f) || r < 0) break;
+        ft.fold(t, yf, r);
+        float h;
+        ft.eval(nasa, T, h, Cp);
+        float df = fminf((h - Rf * T - ef) / (Cp - Rf + 1.0e-30f), 1e-3f * T);
+        df = fmaxf(df, -1e-2f * T);
+        T -= df;
+        if (fabsf(df) <= 1.0e-5f * T) {
+            ok = T >= 200.0f && thermo_range(nasa, T) == r;
+            break;
+        }
+    }
+    if (ok) {  // one FP64 step, with the FP32 derivative
+        FoldedThermo<NS> fd;
+        const double Td = T;
+        if (fd.fold(t, yi, Td)) {
+            const double df = (fd.eval_h(nasa, Td) - Rm * Td - e) * rcp_nr1((double)(Cp - Rf));
+            if (fabs(df) <= 2.0e-5 * Td) {
+                Cp_out = Cp;
+                return Td - df;
+            }
+        }
+    }
+    return newton_T_folded<NS>(t, yi, Rm, e, T0, Cp_out);
 }
 
 // Primitive recovery of the mixed form. Single gas: from the FP64 state converted once to FP32.
@@ -204,16 +295,17 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
             const double tme = U[4] * rho1 - 0.5 * (ud * ud + vd * vd + wd * wd);
             const double wi = mix_W_inv<NS>(th, yi), Rm = wi * kRu;  // sum y_n / W_n; the mixture R
             double Cp;
-            const double T = newton_T_folded<NS>(th, yi, Rm, tme, f.T[id], Cp);
+            const double T = newton_T_mixed<NS>(th, yi, Rm, tme, f.T[id], Cp);
             const double pd = rhod * Rm * T;
-            const double gmx = Cp * rcp_nr(Cp - Rm);
-            const double gamma = gmx > 1.0 ? gmx : -1.0;
+            // gamma feeds only FP32 quantities (the sound speed, the cell terms): FP32 from the FP32 Cp
+            const float Cpf = d2f_rn(Cp), Rf = d2f_rn(Rm), gmx = Cpf / (Cpf - Rf);
+            const double gamma = gmx > 1.0f ? (double)gmx : -1.0;
             const double Hd = (U[4] + pd) * rho1;
             f.rho[id] = rhod, f.u[id] = ud, f.v[id] = vd, f.w[id] = wd, f.p[id] = pd, f.H[id] = Hd;
             f.e[id] = tme, f.gamma[id] = gamma, f.T[id] = T, f.Cp[id] = Cp, f.R[id] = Rm;
             if (f.Tf) f.Tf[id] = d2f_rn(T);  // viscous schemes: the heat flux's FP32 temperature
-            cop_cell_terms_mixed<NS>(th, d2f_rn(T), d2f_rn(Cp), d2f_rn(gmx), d2f_rn(Rm), d2f_rn(ud), d2f_rn(vd),
-                                     d2f_rn(wd), d2f_rn(tme), f.xcf, P, id);
+            cop_cell_terms_mixed<NS>(th, d2f_rn(T), Cpf, gmx, Rf, d2f_rn(ud), d2f_rn(vd), d2f_rn(wd), d2f_rn(tme),
+                                     f.xcf, P, id);
 #pragma unroll
             for (int s = 0; s < NS; s++) f.y[s * P + id] = yi[s], yf[s] = d2f_rn(yi[s]), f.yf[s * P + id] = yf[s];
 #pragma unroll

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <initializer_list>
+#include <vector>
 
 #include "xfg_device.cuh"
 
@@ -70,6 +71,13 @@ void set_last_error(const char *msg);
 // switches in range, Bwidth against the scheme's stencil, consistent sizes, the face launches'
 // grid limits. Returns 0 or -1 with the message set.
 int validate_block_scheme(const xfg_block *b, const xfg_scheme *s, const xfg_thermal *t);
+
+// Device transport tables of a viscous mixture from the caller's fits (xfg_transport), shared by
+// xfg_set_transport and xfg_ensemble_set_transport: FP64 t = visc[4 ns], therm[4 ns],
+// wa[ns ns] = (W_i / W_k)^0.25, wb[ns ns] = (1 + W_k / W_i)^-0.5, sid[ns]; FP32 tf = the same with
+// the species resolved through sid and wb scaled by 0.5 / sqrt(2). Returns 0, or -1 with the error
+// text set.
+int pack_transport(const xfg_transport *tr, int ns, std::vector<double> &t, std::vector<float> &tf);
 
 // Registry filled by the instantiation units.
 const Ops *find_ops(int cop, int ns, int order, int precision);

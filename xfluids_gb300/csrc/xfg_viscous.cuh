@@ -19,6 +19,9 @@ namespace XFG_KNS {
 enum { V_DUCX, V_DVCX, V_DWCX, V_DUCY, V_DVCY, V_DWCY, V_DUCZ, V_DVCZ, V_DWCZ };
 constexpr double kVTwle = 1.0 / 12.0, kVTwfr = 1.0 / 24.0, kVSxtn = 1.0 / 16.0;
 
+// Each kernel below is a device body (one thread's work, t its index in the launch) and a
+// single-grid wrapper; the ensemble engine runs the same bodies per member (xfg_ensemble.cuh).
+
 // device transport table (doubles): visc[NS*4], therm[NS*4], wa[NS*NS] = (W_j/W_k)^0.25,
 // wb[NS*NS] = (1 + W_k/W_j)^-0.5, sid[NS]; offsets for a given NS
 struct TrView {
@@ -28,11 +31,9 @@ struct TrView {
 };
 
 // one thread per cell of [B-2, inner+B+2) in every active direction
-static __global__ void __launch_bounds__(kThreads) k_vderiv(Geo g, DevFields f, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void vderiv_body(const Geo &g, const DevFields &f, long long t) {
     const int r0[3] = {g.dimx ? g.Bx - 2 : 0, g.dimy ? g.By - 2 : 0, g.dimz ? g.Bz - 2 : 0};
     const int nx = g.dimx ? g.Xi + 4 : 1, ny = g.dimy ? g.Yi + 4 : 1, nz = g.dimz ? g.Zi + 4 : 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nx * ny * nz) return;
     const int i = (int)(t % nx) + r0[0];
     const long long r = t / nx;
@@ -57,14 +58,16 @@ static __global__ void __launch_bounds__(kThreads) k_vderiv(Geo g, DevFields f, 
             f.vde[(3 * d + c) * P + id] = val;
         }
 }
+static __global__ void __launch_bounds__(kThreads) k_vderiv(Geo g, DevFields f, int guard) {
+    if (guard && step_done(f)) return;
+    vderiv_body(g, f, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // The mixed form's derivatives: the same fourth-order differences in FP32 from the form's FP32
 // velocities (primf components 1..3), written as FP32.
-static __global__ void __launch_bounds__(kThreads) k_vderiv_f32(Geo g, DevFields f, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void vderiv_f32_body(const Geo &g, const DevFields &f, long long t) {
     const int r0[3] = {g.dimx ? g.Bx - 2 : 0, g.dimy ? g.By - 2 : 0, g.dimz ? g.Bz - 2 : 0};
     const int nx = g.dimx ? g.Xi + 4 : 1, ny = g.dimy ? g.Yi + 4 : 1, nz = g.dimz ? g.Zi + 4 : 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nx * ny * nz) return;
     const int i = (int)(t % nx) + r0[0];
     const long long r = t / nx;
@@ -85,16 +88,18 @@ static __global__ void __launch_bounds__(kThreads) k_vderiv_f32(Geo g, DevFields
             f.vdef[(3 * d + c) * P + id] = val;
         }
 }
+static __global__ void __launch_bounds__(kThreads) k_vderiv_f32(Geo g, DevFields f, int guard) {
+    if (guard && step_done(f)) return;
+    vderiv_f32_body(g, f, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // ghost layers of direction D: the four derivative components its flux reads
 template <int D, class VT>
-__global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, VT *__restrict__ vde, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void vderiv_bc_body(const Geo &g, const DevFields &f, VT *__restrict__ vde, long long t) {
     const int bw = D == 0 ? g.Bx : (D == 1 ? g.By : g.Bz);
     const int inner = D == 0 ? g.Xi : (D == 1 ? g.Yi : g.Zi);
     const int nmax = D == 0 ? g.Xmax : (D == 1 ? g.Ymax : g.Zmax);
     const int ta = D == 0 ? g.Ymax : g.Xmax, tb = D == 2 ? g.Ymax : g.Zmax;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)bw * ta * tb) return;
     const int gl = (int)(t % bw);
     const long long r = t / bw;
@@ -139,6 +144,11 @@ __global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, VT *
             }
     }
 }
+template <int D, class VT>
+__global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, VT *__restrict__ vde, int guard) {
+    if (guard && step_done(f)) return;
+    vderiv_bc_body<D, VT>(g, f, vde, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // mixture viscosity (Wilke) and thermal conductivity on the cells k_visc reads: [B-2, inner+B+2)
 // in every active direction. Per cell one ln T, NS viscosity fits, and the Wilke weights
@@ -146,10 +156,9 @@ __global__ void __launch_bounds__(kThreads) k_vderiv_bc(Geo g, DevFields f, VT *
 // sqrt(mu_k) * (1 / sqrt(mu_i)): NS square roots and reciprocals instead of NS^2 pow calls, a
 // difference of a few ulp (the fits themselves go through exp and log).
 template <int NS>
-__global__ void __launch_bounds__(kThreads) k_transport(Geo g, DevFields f, DevThermo th, int heat, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void transport_body(const Geo &g, const DevFields &f, const DevThermo &th, int heat,
+                                               long long t) {
     const int nx = g.dimx ? g.Xi + 4 : 1, ny = g.dimy ? g.Yi + 4 : 1, nz = g.dimz ? g.Zi + 4 : 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nx * ny * nz) return;
     const int i0 = (int)(t % nx) + (g.dimx ? g.Bx - 2 : 0);
     const long long r = t / nx;
@@ -197,15 +206,19 @@ __global__ void __launch_bounds__(kThreads) k_transport(Geo g, DevFields f, DevT
     f.mu[id] = mu;
     if (heat) f.kappa[id] = kap;
 }
+template <int NS>
+__global__ void __launch_bounds__(kThreads) k_transport(Geo g, DevFields f, DevThermo th, int heat, int guard) {
+    if (guard && step_done(f)) return;
+    transport_body<NS>(g, f, th, heat, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // The mixed form's transport: the same sums in FP32 (mu and kappa to ~1e-6 relative; the fits lose
 // about one decade to cancellation), from the FP32 table trf (species resolved, PHI's constant
 // 0.5 / sqrt(2) folded into wb), written as FP32 for k_visc_f32.
 template <int NS>
-__global__ void __launch_bounds__(kThreads) k_transport_f32(Geo g, DevFields f, DevThermo th, int heat, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void transport_f32_body(const Geo &g, const DevFields &f, const DevThermo &th, int heat,
+                                                   long long t) {
     const int nx = g.dimx ? g.Xi + 4 : 1, ny = g.dimy ? g.Yi + 4 : 1, nz = g.dimz ? g.Zi + 4 : 1;
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nx * ny * nz) return;
     const int i0 = (int)(t % nx) + (g.dimx ? g.Bx - 2 : 0);
     const long long r = t / nx;
@@ -250,14 +263,17 @@ __global__ void __launch_bounds__(kThreads) k_transport_f32(Geo g, DevFields f, 
     f.muf[id] = mu;
     if (heat) f.kappaf[id] = kap;
 }
+template <int NS>
+__global__ void __launch_bounds__(kThreads) k_transport_f32(Geo g, DevFields f, DevThermo th, int heat, int guard) {
+    if (guard && step_done(f)) return;
+    transport_f32_body<NS>(g, f, th, heat, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // viscous stress and heat-conduction flux at the faces i+1/2 of direction D, subtracted from the
 // FP64 face fluxes (the mixed form runs k_visc_f32)
 template <int D, int E, class FT>
-__global__ void __launch_bounds__(kThreads) k_visc(Geo g, DevFields f, FT *__restrict__ Fw, int heat, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void visc_body(const Geo &g, const DevFields &f, FT *__restrict__ Fw, int heat, long long t) {
     const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nfx * nfy * nfz) return;
     const int i = (int)(t % nfx) + g.Bx - (D == 0 ? 1 : 0);
     const long long r = t / nfx;
@@ -303,16 +319,19 @@ __global__ void __launch_bounds__(kThreads) k_visc(Geo g, DevFields f, FT *__res
     Fw[4 * P + id] = (FT)((double)Fw[4 * P + id] - F4);
     // component 0 and the species: minus zero (the reference subtracts 0.0 and the zero diffusion)
 }
+template <int D, int E, class FT>
+__global__ void __launch_bounds__(kThreads) k_visc(Geo g, DevFields f, FT *__restrict__ Fw, int heat, int guard) {
+    if (guard && step_done(f)) return;
+    visc_body<D, E, FT>(g, f, Fw, heat, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
 
 // The mixed form's viscous and heat-conduction face flux: k_visc's terms in FP32 from the form's
 // FP32 velocities (primf), derivatives, mu, kappa and T, subtracted from the FP32 face fluxes.
 // FP32 rounding of u (~6e-8 |u|) moves the stress by far less than the FP32 convective flux's own
 // rounding.
 template <int D, int E>
-__global__ void __launch_bounds__(kThreads) k_visc_f32(Geo g, DevFields f, int heat, int guard) {
-    if (guard && step_done(f)) return;
+__device__ __forceinline__ void visc_f32_body(const Geo &g, const DevFields &f, int heat, long long t) {
     const int nfx = g.Xi + (D == 0 ? 1 : 0), nfy = g.Yi + (D == 1 ? 1 : 0), nfz = g.Zi + (D == 2 ? 1 : 0);
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)nfx * nfy * nfz) return;
     const int i = (int)(t % nfx) + g.Bx - (D == 0 ? 1 : 0);
     const long long r = t / nfx;
@@ -352,6 +371,11 @@ __global__ void __launch_bounds__(kThreads) k_visc_f32(Geo g, DevFields f, int h
     Fw[2 * P + id] -= fv[1];
     Fw[3 * P + id] -= fv[2];
     Fw[4 * P + id] -= F4;
+}
+template <int D, int E>
+__global__ void __launch_bounds__(kThreads) k_visc_f32(Geo g, DevFields f, int heat, int guard) {
+    if (guard && step_done(f)) return;
+    visc_f32_body<D, E>(g, f, heat, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 }  // namespace XFG_KNS

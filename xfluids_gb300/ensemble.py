@@ -42,6 +42,11 @@ class Ensemble:
         except Exception:
             pass
 
+    def set_transport(self, transport):
+        """Fitted transport data shared by the members of a viscous mixture ensemble (xfg_transport,
+        thermo.transport_from_arrays / transport.fit_transport); needed before the first advance."""
+        check(lib().xfg_ensemble_set_transport(self._e, C.byref(transport)))
+
     @staticmethod
     def member_bytes(block: Block, precision, scheme: Scheme = None) -> int:
         """Pool bytes of one member: a single gas of this precision, or a member under `scheme`."""
