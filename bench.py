@@ -593,15 +593,22 @@ def run_gpu_arm(args, world, rank, local):
     f2.advance(1)
     f2.synchronize()
     d.barrier()
+    parts = np.zeros(4)  # wall seconds of the four calls (each returns after its work is done)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
+        ta = time.perf_counter()
         f2.InitialU(host.array)            # H2D of the step's input state
+        tb = time.perf_counter()
         f2.initialize()
+        tc = time.perf_counter()
         f2.advance(1)
+        td = time.perf_counter()
         f2.get("U", out=host.array)         # D2H of the step's result into the pinned buffer
+        parts += (tb - ta, tc - tb, td - tc, time.perf_counter() - td)
     el = time.perf_counter() - t0
     el = d.max(el)
     e2e_value = d.sum(n * n * e2e_steps) / el
+    e2e_parts = parts
     bytes_state = U0.size * 8
     f2.close()
     host.close()
@@ -681,7 +688,9 @@ def run_gpu_arm(args, world, rank, local):
                    "l2": "inputs larger than L2 (state 670 MB)"},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_state,
                 "d2h_bytes_per_step": bytes_state, "steps": e2e_steps,
-                "path": "xfg_set_state(pinned host U) + BoundaryCondition + UpdateFluidStates + xfg_advance(1) + xfg_get_array(U)"},
+                "path": "xfg_set_state(pinned host U) + BoundaryCondition + UpdateFluidStates + xfg_advance(1) + xfg_get_array(U)",
+                "ms_per_step_by_call": {k: float(v) * 1e3 / e2e_steps for k, v in
+                                        zip(("set_state", "boundary_and_states", "advance", "get_array"), e2e_parts)}},
         "gpu_launches": launches,
         "roofline": {"bound": "fp64", "kernel": "k_faces<x> (FP64 characteristic WENO5 face flux)",
                      "achieved": achieved / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
