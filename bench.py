@@ -591,6 +591,12 @@ def run_gpu_arm(args, world, rank, local):
     e2e_steps = max(1, min(args.steps, 3))
     f2, _, _ = setup(0)
     f2.advance(1)
+    # one untimed pass of the whole sequence: the first call of each kernel loads its module
+    f2.InitialU(host.array)
+    f2.initialize()
+    f2.advance(1)
+    f2.get("U", out=host.array)
+    host.array[:] = U0.reshape(-1)
     f2.synchronize()
     d.barrier()
     parts = np.zeros(4)  # wall seconds of the four calls (each returns after its work is done)
@@ -604,7 +610,9 @@ def run_gpu_arm(args, world, rank, local):
         f2.advance(1)
         td = time.perf_counter()
         f2.get("U", out=host.array)         # D2H of the step's result into the pinned buffer
-        parts += (tb - ta, tc - tb, td - tc, time.perf_counter() - td)
+        it = (tb - ta, tc - tb, td - tc, time.perf_counter() - td)
+        parts += it
+        progress("e2e step: " + ", ".join(f"{1e3 * x:.1f}" for x in it) + " ms (set_state, states, advance, get)")
     el = time.perf_counter() - t0
     el = d.max(el)
     e2e_value = d.sum(n * n * e2e_steps) / el
