@@ -40,6 +40,22 @@ TRANSPORT_TABLES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tes
 # DRAM bytes per face of the FP64 x-face kernel: 674.2 MB read + 152.8 MB written in one ncu
 # capture of the 2048^2 vortex (4.196 M faces); traffic grows with the faces of a launch
 NCU_FACE_BYTES_FP64 = (674.218496e6 + 152.813568e6) / (2049 * 2048)
+# Warp instructions per cell and stage of the fused mixed stage kernel: 2979 thread instructions
+# per cell (sass__inst_executed_per_opcode summed) / 32, ncu capture of the 2048^2 vortex
+NCU_FUSED_WARP_INSTR_PER_CELL = 2979.0 / 32.0
+
+
+def issue_roofline(device, cells, launch_ms, sm_mhz):
+    """The fused mixed stage against the bound it meets, instruction issue: its warp instructions
+    per launch (the ncu count per cell times the cells) over the launch time, against one warp
+    instruction per cycle on each of the 4 schedulers of every SM at the measured SM clock."""
+    import torch
+    nsm = torch.cuda.get_device_properties(device).multi_processor_count
+    achieved = cells * NCU_FUSED_WARP_INSTR_PER_CELL / (launch_ms * 1e-3)
+    peak = nsm * 4 * sm_mhz * 1e6
+    return {"bound": "instruction issue", "kernel": "k_fused_stage", "achieved": achieved, "peak": peak,
+            "unit": "warp instructions/s", "frac": achieved / peak, "warp_instructions_per_cell": NCU_FUSED_WARP_INSTR_PER_CELL,
+            "sms": nsm, "sm_mhz": sm_mhz}
 
 
 def hbm_context(traffic_bytes, launch_ms, peaks_path=os.path.join(ROOT, "MEASURED_PEAKS.json")):
@@ -719,7 +735,8 @@ def run_gpu_arm(args, world, rank, local):
                                "frac": FLOPS_PER_CELL_UPDATE / 3.0 * n * n / (mixed_face_ms * 1e-3) / peaks["fp32_flops"],
                                "note": "algorithmic flops of one RK stage (the oracle's count, a third of a "
                                        "cell-update's) over the launch time; peak: measured scalar FP32 FMA chain"},
-                  "fp32_peak_tflops": peaks["fp32_flops"] / 1e12},
+                  "fp32_peak_tflops": peaks["fp32_flops"] / 1e12,
+                  "issue_roofline": issue_roofline(local, n * n, mixed_face_ms, peaks["sm_clock_mhz"])},
         "ensemble": ens or None,
         "serving": serving,
         "mixing_layer": mixing,
