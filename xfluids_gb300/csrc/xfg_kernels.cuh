@@ -335,28 +335,15 @@ static __global__ void __launch_bounds__(kThreads) k_glf(Geo g, DevFields f, uns
 // rounding of every operation before it, so the mixture branch is written with round-to-nearest
 // operations the compiler never contracts into an FMA (pm / pa / ps), in the reference's operation
 // order; units built with --fmad=false get the same bits, and units that contract the rest of
-// the face (projections, WENO, back-projection) keep this state exact.
-// PIN = false (the mixed form, which has no reference rounding to keep) lets the compiler contract.
-template <bool PIN>
-__device__ __forceinline__ double pm(double a, double b) {
-    if constexpr (PIN) return __dmul_rn(a, b);
-    else return a * b;
-}
-template <bool PIN>
-__device__ __forceinline__ double pa(double a, double b) {
-    if constexpr (PIN) return __dadd_rn(a, b);
-    else return a + b;
-}
-template <bool PIN>
-__device__ __forceinline__ double ps(double a, double b) {
-    if constexpr (PIN) return __dsub_rn(a, b);
-    else return a - b;
-}
+// the face (projections, WENO, back-projection) keep this state exact. (The mixed form builds its
+// own mixture Roe state, face_state_mixed in xfg_mixed.cuh.)
+__device__ __forceinline__ double pm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double pa(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ps(double a, double b) { return __dsub_rn(a, b); }
 
-template <bool COP, int NS, bool PIN = true>
+template <bool COP, int NS>
 __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, const DevThermo &th, long long l,
                                            long long r, FaceState<NS> &F, double &Gamma0) {
-    constexpr bool Q = PIN;
     const long long P = g.pitch;
     const double rl = f.rho[l], rr = f.rho[r];
     const double ul = f.u[l], ur = f.u[r], vl = f.v[l], vr = f.v[r], wl = f.w[l], wr = f.w[r];
@@ -383,10 +370,10 @@ __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, con
         F.ent0 = (1.0 - F.b2 - F.b3) / F.b1;
     } else {
         constexpr int NCOP = NS - 1;
-        auto roe = [&](double a, double b) { return pm<Q>(pa<Q>(a, pm<Q>(D, b)), D1); };  // (a + D b) D1
+        auto roe = [&](double a, double b) { return pm(pa(a, pm(D, b)), D1); };  // (a + D b) D1
         F._u = roe(ul, ur), F._v = roe(vl, vr), F._w = roe(wl, wr);
         F._H = roe(Hl, Hr), F._P = roe(pl, pr);
-        F._rho = sqrt(pm<Q>(rr, rl));
+        F._rho = sqrt(pm(rr, rl));
         double yl[NS], yr[NS];
 #pragma unroll
         for (int n = 0; n < NS; n++) {
@@ -404,48 +391,46 @@ __device__ __forceinline__ void face_state(const Geo &g, const DevFields &f, con
 #pragma unroll
         for (int n = 0; n < NCOP; n++) {
             dpdrhoi[n] = roe(xc[(3 + n) * P + l], xc[(3 + n) * P + r]);
-            drhoi[n] = ps<Q>(pm<Q>(rr, yr[n]), pm<Q>(rl, yl[n]));
+            drhoi[n] = ps(pm(rr, yr[n]), pm(rl, yl[n]));
         }
         Gamma0 = roe(gl, gr);
-        const double du = ps<Q>(ur, ul), dv = ps<Q>(vr, vl), dw = ps<Q>(wr, wl);
-        const double _prho = pa<Q>(pm<Q>(pa<Q>(pl / rl, pm<Q>(D, pr / rr)), D1),
-                                pm<Q>(pm<Q>(pm<Q>(pm<Q>(0.5, D), D1), D1), pa<Q>(pa<Q>(pm<Q>(du, du), pm<Q>(dv, dv)), pm<Q>(dw, dw))));
-        const double _dpdE = roe(ps<Q>(gl, 1.0), ps<Q>(gr, 1.0));
-        const double _dpde = pm<Q>(pa<Q>(pm<Q>(ps<Q>(gl, 1.0), rl), pm<Q>(D, pm<Q>(ps<Q>(gr, 1.0), rr))), D1);
-        const double dp = ps<Q>(pr, pl), drho = ps<Q>(rr, rl), de = ps<Q>(er, el);
+        const double du = ps(ur, ul), dv = ps(vr, vl), dw = ps(wr, wl);
+        const double _prho = pa(pm(pa(pl / rl, pm(D, pr / rr)), D1),
+                                pm(pm(pm(pm(0.5, D), D1), D1), pa(pa(pm(du, du), pm(dv, dv)), pm(dw, dw))));
+        const double _dpdE = roe(ps(gl, 1.0), ps(gr, 1.0));
+        const double _dpde = pm(pa(pm(ps(gl, 1.0), rl), pm(D, pm(ps(gr, 1.0), rr))), D1);
+        const double dp = ps(pr, pl), drho = ps(rr, rl), de = ps(er, el);
         double S1 = 0.0, S2 = 0.0, SY = 0.0;
 #pragma unroll
         for (int n = 0; n < NCOP; n++) {
-            S1 = pa<Q>(S1, pm<Q>(dpdrhoi[n], drhoi[n]));
-            S2 = pa<Q>(S2, pm<Q>(pm<Q>(pm<Q>(dpdrhoi[n], drhoi[n]), dpdrhoi[n]), drhoi[n]));
+            S1 = pa(S1, pm(dpdrhoi[n], drhoi[n]));
+            S2 = pa(S2, pm(pm(pm(dpdrhoi[n], drhoi[n]), dpdrhoi[n]), drhoi[n]));
         }
-        const double temp1 = ps<Q>(dp, pa<Q>(pa<Q>(pm<Q>(_dpdrho, drho), pm<Q>(_dpde, de)), S1));
-        const double den = pa<Q>(pa<Q>(pa<Q>(pm<Q>(pm<Q>(pm<Q>(_dpdrho, _dpdrho), drho), drho), pm<Q>(pm<Q>(pm<Q>(_dpde, de), _dpde), de)), S2),
+        const double temp1 = ps(dp, pa(pa(pm(_dpdrho, drho), pm(_dpde, de)), S1));
+        const double den = pa(pa(pa(pm(pm(pm(_dpdrho, _dpdrho), drho), drho), pm(pm(pm(_dpde, de), _dpde), de)), S2),
                               1e-19);
         const double temp = temp1 / den;
 #pragma unroll
-        for (int n = 0; n < NCOP; n++) SY = pa<Q>(SY, pm<Q>(F._yi[n], dpdrhoi[n]));
-        const double _dpdE_new = pa<Q>(_dpdE, pm<Q>(pm<Q>(pm<Q>(pm<Q>(_dpdE, _dpdE), de), F._rho), temp));
-        const double _dpdrho_new = pa<Q>(_dpdrho, pm<Q>(pm<Q>(pm<Q>(_dpdrho, _dpdrho), drho), temp));
-        const double csqr = pa<Q>(pa<Q>(_dpdrho_new, pm<Q>(_dpdE_new, _prho)), SY);
+        for (int n = 0; n < NCOP; n++) SY = pa(SY, pm(F._yi[n], dpdrhoi[n]));
+        const double _dpdE_new = pa(_dpdE, pm(pm(pm(pm(_dpdE, _dpdE), de), F._rho), temp));
+        const double _dpdrho_new = pa(_dpdrho, pm(pm(pm(_dpdrho, _dpdrho), drho), temp));
+        const double csqr = pa(pa(_dpdrho_new, pm(_dpdE_new, _prho)), SY);
         F.b1 = _dpdE_new / csqr;
-        // the mixed form (PIN = false) divides by dp/dE once: z_n = -d_n (1 / dp/dE)
-        const double inv_dpdE = PIN ? 0.0 : 1.0 / _dpdE_new;
         double b3 = 0.0;
 #pragma unroll
         for (int n = 0; n < NCOP; n++) {
-            const double dn = pa<Q>(dpdrhoi[n], pm<Q>(pm<Q>(pm<Q>(dpdrhoi[n], dpdrhoi[n]), drhoi[n]), temp));
-            F.z[n] = PIN ? -dn / _dpdE_new : -dn * inv_dpdE;
-            b3 = pa<Q>(b3, pm<Q>(F._yi[n], F.z[n]));
+            const double dn = pa(dpdrhoi[n], pm(pm(pm(dpdrhoi[n], dpdrhoi[n]), drhoi[n]), temp));
+            F.z[n] = -dn / _dpdE_new;
+            b3 = pa(b3, pm(F._yi[n], F.z[n]));
         }
-        F.b3 = pm<Q>(b3, F.b1);
+        F.b3 = pm(b3, F.b1);
         const double c2w = (0.0 < csqr) ? 0.0 : 1.0;
-        F.c2 = pa<Q>(pm<Q>(pm<Q>(pm<Q>(Gamma0, F._P), F._rho), c2w), pm<Q>(ps<Q>(1.0, c2w), csqr));
-        F.q2 = pa<Q>(pa<Q>(pm<Q>(F._u, F._u), pm<Q>(F._v, F._v)), pm<Q>(F._w, F._w));
+        F.c2 = pa(pm(pm(pm(Gamma0, F._P), F._rho), c2w), pm(ps(1.0, c2w), csqr));
+        F.q2 = pa(pa(pm(F._u, F._u), pm(F._v, F._v)), pm(F._w, F._w));
         F._c = sqrt(F.c2);
-        F.b2 = ps<Q>(pa<Q>(1.0, pm<Q>(F.b1, F.q2)), pm<Q>(F.b1, F._H));
+        F.b2 = ps(pa(1.0, pm(F.b1, F.q2)), pm(F.b1, F._H));
         F._c1 = 1.0 / F._c;
-        F.ent0 = PIN ? ps<Q>(ps<Q>(1.0, F.b2), F.b3) / F.b1 : ((1.0 - F.b2) - F.b3) * (csqr * inv_dpdE);
+        F.ent0 = ps(ps(1.0, F.b2), F.b3) / F.b1;
     }
 }
 
