@@ -164,6 +164,18 @@ __device__ __forceinline__ double rcp_nr(double x) {
     e = fma(-x, r, 1.0);
     return fma(r, e, r);
 }
+// (i, j, k) of the linear index t of an nx x ny x nz box, x fastest: unsigned 32-bit division when
+// t fits in 32 bits (the 64-bit division is a long instruction sequence), the 64-bit form otherwise.
+__device__ __forceinline__ void split_index(long long t, int nx, int ny, int &i, int &j, int &k) {
+    if (t <= 0xffffffffLL) {
+        const unsigned u = (unsigned)t, r = u / (unsigned)nx, q = r / (unsigned)ny;
+        i = (int)(u - r * (unsigned)nx), j = (int)(r - q * (unsigned)ny), k = (int)q;
+    } else {
+        const long long r = t / nx;
+        i = (int)(t - r * nx), j = (int)(r % ny), k = (int)(r / ny);
+    }
+}
+
 // One refinement step only: about 2^-40 relative, enough for a Newton step whose iteration
 // continues until the step itself is below the tolerance.
 __device__ __forceinline__ double rcp_nr1(double x) {

@@ -238,9 +238,8 @@ __device__ __forceinline__ void states_body(const Geo &g, const DevFields &f, co
             for (int n = 5; n < E; n++) F[n * P + id] = U[3] * yi[n - 5];
         }
         // inner-cell checks (rho, p, T negative / NaN / Inf; Y NaN / Inf)
-        const int i = (int)(id % g.Xmax);
-        const long long r = id / g.Xmax;
-        const int j = (int)(r % g.Ymax), k = (int)(r / g.Ymax);
+        int i, j, k;
+        split_index(id, g.Xmax, g.Ymax, i, j, k);
         const bool inner = i >= g.Bx && i < g.Xmax - g.Bx && j >= g.By && j < g.Ymax - g.By && k >= g.Bz && k < g.Zmax - g.Bz;
         if (inner) {
             bool e1 = rho < 0.0 || bad(rho) || p < 0.0 || bad(p) || (COP && (T < 0.0 || bad(T)));
@@ -767,9 +766,9 @@ __device__ __forceinline__ void pp_body(const Geo &g, const double *__restrict__
                                         FT *__restrict__ Fw, double lambda_0, double lambda, long long t) {
     if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
     const long long P = g.pitch;
-    const int i = (int)(t % g.Xi) + g.Bx;
-    const long long r = t / g.Xi;
-    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    int i, j, k;
+    split_index(t, g.Xi, g.Yi, i, j, k);
+    i += g.Bx, j += g.By, k += g.Bz;
     const long long stride = D == 0 ? 1 : (D == 1 ? (long long)g.Xmax : (long long)g.Xmax * g.Ymax);
     const long long l = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i, rr = l + stride;
     double F_LF[E], FF_LF[E], FF[E], Fwall[E];
@@ -842,9 +841,9 @@ __device__ __forceinline__ void div_rk_body(const Geo &g, const DevFields &f, in
                                             int store_lu, long long t) {
     const long long P = g.pitch;
     if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
-    const int i = (int)(t % g.Xi) + g.Bx;
-    const long long r = t / g.Xi;
-    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    int i, j, k;
+    split_index(t, g.Xi, g.Yi, i, j, k);
+    i += g.Bx, j += g.By, k += g.Bz;
     const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long sy = g.Xmax, sz = (long long)g.Xmax * g.Ymax;
     int code = 0;
@@ -894,9 +893,9 @@ __global__ void __launch_bounds__(kThreads) k_rk(Geo g, DevFields f, int flag, d
     const long long P = g.pitch;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
-    const int i = (int)(t % g.Xi) + g.Bx;
-    const long long r = t / g.Xi;
-    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    int i, j, k;
+    split_index(t, g.Xi, g.Yi, i, j, k);
+    i += g.Bx, j += g.By, k += g.Bz;
     const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
 #pragma unroll
     for (int n = 0; n < E; n++) {
@@ -916,9 +915,9 @@ __global__ void __launch_bounds__(kThreads) k_estimate_nan(Geo g, const double *
     const long long P = g.pitch;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
-    const int i = (int)(t % g.Xi) + g.Bx;
-    const long long r = t / g.Xi;
-    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    int i, j, k;
+    split_index(t, g.Xi, g.Yi, i, j, k);
+    i += g.Bx, j += g.By, k += g.Bz;
     const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     bool e = UI[id] < 0.0;
     if (e) atomicAdd(&pos[0], 10000);

@@ -335,9 +335,8 @@ __device__ __forceinline__ void states_mixed_body(const Geo &g, const DevFields 
 #pragma unroll
             for (int n = 5; n < E; n++) F[n * P + id] = mom[d] * yf[n - 5];
         }
-        const int i = (int)(id % g.Xmax);
-        const long long r = id / g.Xmax;
-        const int j = (int)(r % g.Ymax), k = (int)(r / g.Ymax);
+        int i, j, k;
+        split_index(id, g.Xmax, g.Ymax, i, j, k);
         const bool inner = i >= g.Bx && i < g.Xmax - g.Bx && j >= g.By && j < g.Ymax - g.By && k >= g.Bz && k < g.Zmax - g.Bz;
         if (inner && (!(rho >= 0.f) || !(p >= 0.f) || isinf(rho) || isinf(p))) {
             atomicOr(&f.err[ERR_PRIM], 1);
@@ -718,9 +717,9 @@ __device__ __forceinline__ void div_rk_mixed_body(const Geo &g, const DevFields 
                                                   int store_lu, long long t) {
     const long long P = g.pitch;
     if (t >= (long long)g.Xi * g.Yi * g.Zi) return;
-    const int i = (int)(t % g.Xi) + g.Bx;
-    const long long r = t / g.Xi;
-    const int j = (int)(r % g.Yi) + g.By, k = (int)(r / g.Yi) + g.Bz;
+    int i, j, k;
+    split_index(t, g.Xi, g.Yi, i, j, k);
+    i += g.Bx, j += g.By, k += g.Bz;
     const long long id = (long long)g.Xmax * g.Ymax * k + (long long)g.Xmax * j + i;
     const long long sy = g.Xmax, sz = (long long)g.Xmax * g.Ymax;
     int code = 0;
