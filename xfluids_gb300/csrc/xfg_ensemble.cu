@@ -79,12 +79,17 @@ template <bool LLF>
 __global__ void __launch_bounds__(fz::THREADS, 2)
     kb_fused(const Member *__restrict__ M, const int *__restrict__ off, int n, FusedK k, int flag) {
     const int mi = member_of_block(off, n, blockIdx.x);
-    const Member &m = M[mi];
-    if (member_done(m)) return;
-    const int lb = blockIdx.x - off[mi], tx = (m.g.Xi + fz::TX - 1) / fz::TX;
-    const double *UI = flag == 1 ? m.f.U : (flag == 2 ? m.f.U2 : m.f.U1);
-    double *Uout = flag == 1 ? m.f.U2 : (flag == 2 ? m.f.U1 : m.f.U);
-    fused_stage_tile<LLF>(m.g, m.f, k, UI, m.f.U, Uout, flag, m.f.dtbuf[0], 1, 0, flag == 3, lb % tx, lb / tx);
+    if (member_done(M[mi])) return;
+    // local copies of the member's geometry and arrays: the tile's stores cannot alias them, so
+    // they stay in registers, and the arrays are global memory (global, not generic, accesses)
+    const Geo g = M[mi].g;
+    const DevFields f = M[mi].f;
+    __builtin_assume(__isGlobal(f.U) && __isGlobal(f.U1) && __isGlobal(f.U2) && __isGlobal(f.primf));
+    __builtin_assume(__isGlobal(f.lam) && __isGlobal(f.err) && __isGlobal(f.dtbuf));
+    const int lb = blockIdx.x - off[mi], tx = (g.Xi + fz::TX - 1) / fz::TX;
+    const double *UI = flag == 1 ? f.U : (flag == 2 ? f.U2 : f.U1);
+    double *Uout = flag == 1 ? f.U2 : (flag == 2 ? f.U1 : f.U);
+    fused_stage_tile<LLF>(g, f, k, UI, f.U, Uout, flag, f.dtbuf[0], 1, 0, flag == 3, lb % tx, lb / tx);
 }
 __global__ void __launch_bounds__(kThreads) kb_fused_ghost(const Member *__restrict__ M, const int *__restrict__ off,
                                                            int n, float gamma) {
