@@ -70,3 +70,29 @@ def test_hbm_context_reads_the_measured_peak_or_falls_back(tmp_path):
     h = bench.hbm_context(3.0e9, 20.0, peaks_path=str(tmp_path / "absent.json"))
     assert h["hbm_peak_gbs"] == 6800.0 and h["peak_source"].startswith("of fallback")
     assert bench.hbm_context(None, 20.0) is None
+
+
+def test_batched_mixing_members_are_seeded_and_sized_like_the_single_layer():
+    """The members of the batched mixing-layer ensemble: 16 temporal mixing layers of seeded sizes
+    32a x 16b x 16c, a, b, c in [4, 8], together about the single 512 x 256 x 256 layer's cells."""
+    s, th, ms = bench.mixing_members(16)
+    sizes = [(b.X_inner, b.Y_inner, b.Z_inner) for b, _, _ in ms]
+    assert sizes == [(b.X_inner, b.Y_inner, b.Z_inner) for b, _, _ in bench.mixing_members(16)[2]]
+    assert all(x % 32 == 0 and 128 <= x <= 256 and y % 16 == 0 and 64 <= y <= 128 and z % 16 == 0 and 64 <= z <= 128
+               for x, y, z in sizes)
+    cells = sum(x * y * z for x, y, z in sizes)
+    assert 0.8 * 512 * 256 * 256 <= cells <= 1.2 * 512 * 256 * 256
+    assert s.cop == 1 and s.num_species == 5 and s.scheme_order == 7
+    for b, U, T in ms:
+        assert U.size == b.Xmax * b.Ymax * b.Zmax * 9 and T.size == b.Xmax * b.Ymax * b.Zmax
+
+
+def test_per_component_names_the_worst_relative_component():
+    from xfluids_gb300.workloads import per_component
+    r = np.array([[1.0, 2.0, 0.0], [3.0, 2.0, 0.0]])
+    a = r + np.array([[1e-6, 0.0, 5e-9], [1e-6, 4e-6, 0.0]])
+    out = per_component(a, r, ["a", "b", "z"])
+    assert out["a"]["l1_rel"] == pytest.approx(1e-6 / 2.0)
+    assert out["b"]["l1_rel"] == pytest.approx(2e-6 / 2.0)
+    assert out["z"]["l1_rel"] is None and out["z"]["l1"] == pytest.approx(2.5e-9)   # zero reference: absolute only
+    assert out["worst"] == "b"
